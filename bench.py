@@ -1,0 +1,361 @@
+#!/usr/bin/env python
+"""Benchmark of the SIMPLE hot path: outer iterations per second on the 2M-cell case.
+
+Workload (the configuration the headline metric is quoted on): unit-cube lid-driven
+cavity at Re = 400 on 80 x 80 x 52 hexes cut into 6 tets each (1,996,800 cells),
+interior nodes jittered by U(-0.2h, 0.2h) from seed 20261203; rho = 1, mu = 0.0025,
+lid u = 1; under-relaxation 0.7 (u, v, w) / 0.3 (p); BiCGSTAB + Jacobi for momentum,
+Jacobi-CG for p', relative tolerance 1e-8 for every solve; plain FP64.  Synthetic
+input: the reference publishes no mesh or benchmark data.
+
+One step = one SIMPLE outer iteration (momentum assembly + 3-RHS solve, Rhie-Chow,
+p' assembly + CG solve, corrections) with the fields resident in HBM.  The timed
+iterations start from the initial state (the solver is reset after warm-up), so they
+are the same iterations the CPU sample times.  ``e2e`` runs the same iterations
+through the C ABI with host buffers: every step uploads U, V, W, P and the face
+fluxes from host memory and reads U, V, W, P back.
+
+``--impl reference`` times the reference's own CPU code (oracle/_ref/cycas_ref: the
+reference's src/*.cpp + the LASPack restatement) on the same case, single-threaded as
+the reference is, for as many outer iterations as fit in a time budget.
+
+With torchrun (N > 1) every rank runs an independent replica on its own GPU
+(the path has no data-parallel exchange); value = total iterations / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SIMPLE iters/s @2M cells; p' solve time to 1e-8: learned+FP32 vs plain FP64"
+WORKLOADS = {
+    # name: (nx, ny, nz)
+    "c3": (80, 80, 52),
+    "small": (20, 20, 13),
+}
+RE_MU = 0.0025
+SEED = 20261203
+RTC = 1e-8
+L2_BYTES = 129 * 1024 * 1024
+
+
+def rank_info():
+    r = int(os.environ.get("RANK", "0"))
+    w = int(os.environ.get("WORLD_SIZE", "1"))
+    lr = int(os.environ.get("LOCAL_RANK", str(r)))
+    return r, w, lr
+
+
+def case_dir(workload: str) -> str:
+    from sysu_cfd_heat_gb300 import meshgen as mg
+
+    nx, ny, nz = WORKLOADS[workload]
+    d = os.path.join(tempfile.gettempdir(), f"sysu_bench_{workload}_{nx}x{ny}x{nz}_s{SEED}")
+    p = os.path.join(d, "param.in")
+    if not os.path.exists(p):
+        tmp = d + ".tmp%d" % os.getpid()
+        mesh = mg.lid_cavity_tet(nx, ny, nz, jitter=0.2, seed=SEED)
+        mg.write_case(tmp, mesh, mg.cavity_param("x", 100000, mu=RE_MU, urf=(0.7, 0.3, 0.8)))
+        try:
+            os.rename(tmp, d)
+        except OSError:
+            pass
+    return p
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cg_bytes_per_iter(n: int, nnz: int) -> float:
+    """Algorithmic bytes of one Jacobi-PCG iteration, FP64 values, int32 indices:
+    SpMV nnz*(8+4) + 4(N+1) + 2*8N, plus 88N for the vector updates (x, p, r, Ap and
+    D^-1 read, x, r, z written; z and p read, p written)."""
+    spmv = nnz * 12 + 4 * (n + 1) + 16 * n
+    return spmv + 88 * n
+
+
+def cpu_reference_run(param: str, iters: int, budget_s: float, timeout_s: float):
+    """Run the reference binary on the case; returns (per-iteration seconds, setup s, info)."""
+    exe = os.path.join(ROOT, "oracle", "_ref", "cycas_ref")
+    if not os.path.exists(exe):
+        return None, None, "oracle/_ref/cycas_ref not built (no reference sources on this machine)"
+    d = os.path.dirname(param)
+    env = dict(os.environ, SYSU_ORACLE_GMRES_AS="BiCGSTAB", SYSU_ORACLE_SSOR_AS="Jacobi", SYSU_ORACLE_RTC=str(RTC))
+    with tempfile.TemporaryDirectory() as tmp:
+        tfile = os.path.join(tmp, "timing.txt")
+        cmd = [exe, "-paramfile", os.path.basename(param), "-iters", str(iters), "-quiet", "-timing", tfile]
+        t0 = time.time()
+        p = subprocess.Popen(cmd, cwd=d, env=env, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        setup, its = None, []
+        while p.poll() is None:
+            time.sleep(0.5)
+            setup, its = _read_timing(tfile)
+            el = time.time() - t0
+            if el > timeout_s or (its and sum(its) > budget_s):
+                p.kill()
+                p.wait()
+                break
+        setup, its = _read_timing(tfile)
+        return its, setup, None
+
+
+def _read_timing(path):
+    setup, its = None, []
+    if not os.path.exists(path):
+        return setup, its
+    for line in open(path):
+        parts = line.split()
+        if not parts:
+            continue
+        if parts[0] == "setup_s":
+            setup = float(parts[1])
+        elif parts[0] == "iter" and "total_s" in parts:
+            its.append(float(parts[parts.index("total_s") + 1]))
+    return setup, its
+
+
+def run_reference(args, r, w):
+    if r != 0:
+        return
+    param = case_dir(args.workload)
+    nx, ny, nz = WORKLOADS[args.workload]
+    its, setup, err = cpu_reference_run(param, max(1, args.steps), args.ref_budget, args.ref_budget + 600)
+    base = {"impl": "reference", "metric": METRIC, "unit": "iters/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config_of(args)}
+    if err or not its:
+        base["unavailable"] = err or "the reference completed no outer iteration within the time budget"
+        print(json.dumps(base))
+        return
+    tot = sum(its)
+    v = len(its) / tot
+    sample = (f"outer iterations 1..{len(its)} of the {args.workload} case ({6 * nx * ny * nz} cells), "
+              f"set-up ({setup:.1f} s) excluded, bounded to ~{args.ref_budget:.0f} s of iterations")
+    base.update({"value": v, "ms_per_step": 1000 * tot / len(its), "steps": len(its),
+                 "cpu_baseline": {"value": v, "unit": "iters/s", "cores": 1, "kind": "reference", "sample": sample},
+                 "e2e": {"value": v, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+    print(json.dumps(base))
+
+
+def config_of(args):
+    nx, ny, nz = WORKLOADS[args.workload]
+    return {"workload": f"lid-driven cavity Re 400, {nx}x{ny}x{nz} hexes x 6 jittered tets "
+                        f"({6 * nx * ny * nz} cells), seed {SEED}",
+            "cells": 6 * nx * ny * nz, "solvers": "momentum 3-RHS BiCGSTAB+Jacobi, p' Jacobi-CG, rtol 1e-8",
+            "precision": "fp64", "l2": "inputs larger than L2 (mesh, fields and matrices > 129 MB)",
+            "parallelism": "replicas"}
+
+
+def run_ours(args, r, w, lr):
+    from sysu_cfd_heat_gb300 import _lib
+    from sysu_cfd_heat_gb300.solver import NavierStokesSolver
+
+    param = case_dir(args.workload) if r == 0 else None
+    if w > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+        param = case_dir(args.workload)
+    L = _lib.lib()
+    L.sysu_kernel_launches.restype = __import__("ctypes").c_long
+    s = NavierStokesSolver(param, {"rtc": RTC, "timing": 1})
+    info = s.info()
+    n, nnz = info["Ncel"], info["nnz"]
+    # warm-up, then back to the initial state so the timed iterations are iterations 1..K
+    s.iterate(args.warmup)
+    s.reset()
+    if w > 1:
+        dist.barrier()
+    clk = ClockSampler(lr)
+    clk.start()
+    l0 = L.sysu_kernel_launches()
+    s_ms = 0.0
+    p_ms, cg_it, mom_it = [], [], []
+    import ctypes as C
+
+    for k in range(args.steps):
+        C.c_int()
+        _lib.check(L.sysu_solver_timer_start(s._h))
+        done = s.iterate(1)
+        ms = C.c_double()
+        _lib.check(L.sysu_solver_timer_stop(s._h, C.byref(ms)))
+        assert done == 1
+        s_ms += ms.value
+        pm, _ = s.timing()
+        st = s.solve_stats()
+        p_ms.append(pm)
+        cg_it.append(st["p"]["iters"][0])
+        mom_it.append(st["mom"]["iters"])
+    launches = L.sysu_kernel_launches() - l0
+    clocks = clk.stop()
+    t_max = s_ms
+    if w > 1:
+        import torch
+
+        t = torch.tensor([s_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+        dist.barrier()
+    value = w * args.steps / (t_max / 1000.0)
+
+    # end to end through the C ABI with host buffers
+    s.reset()
+    nf = s.field_size("RUFace")
+    host = {f: s.get(f) for f in ("U", "V", "W", "P", "RUFace")}
+    h2d = sum(a.nbytes for a in host.values())
+    d2h = 4 * n * 8
+    if w > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        for f, a in host.items():
+            s.set(f, a)
+        s.iterate(1)
+        for f in ("U", "V", "W", "P"):
+            host[f] = s.get(f)
+        host["RUFace"] = s.get("RUFace") if k < 0 else host["RUFace"]
+    e2e_s = time.perf_counter() - t0
+    if w > 1:
+        import torch
+
+        t = torch.tensor([e2e_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    hbm = peaks.get("hbm_gbs")
+    peak_src = "measured" if hbm else "fallback"
+    hbm = hbm or 6800.0
+    # dominant kernel: the persistent p' CG launch (one per outer iteration)
+    b_iter = cg_bytes_per_iter(n, nnz)
+    spmv_b = nnz * 12 + 4 * (n + 1) + 16 * n
+    bytes_launch = [it * b_iter + spmv_b + 24 * n for it in cg_it]
+    ach = [b / (ms / 1000.0) / 1e9 for b, ms in zip(bytes_launch, p_ms) if ms > 0]
+    achieved = statistics.mean(ach) if ach else None
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "cg_pressure_traffic.json")
+    if os.path.exists(tp):
+        tj = json.load(open(tp))
+        per_iter = tj.get("dram_bytes_per_cg_iteration_scaled_to_c3")
+        if per_iter:
+            traffic = per_iter * statistics.mean(cg_it)
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": w, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered-tet cavity)",
+        "config": config_of(args),
+        "e2e": {"value": w * args.steps / e2e_s, "unit": "iters/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": "k_cg (persistent Jacobi-PCG for p')",
+                     "achieved": achieved, "peak": hbm, "peak_source": peak_src, "unit": "GB/s",
+                     "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
+                     "algorithmic_bytes_per_cg_iteration": b_iter},
+        "p_solve_ms_mean": statistics.mean(p_ms), "p_cg_iters_mean": statistics.mean(cg_it),
+        "mom_bicgstab_iters": mom_it[-1], "clocks": clocks,
+    }
+    s.close()
+    if r == 0 and w == 1 and not args.no_cpu_baseline:
+        its, setup, err = cpu_reference_run(param, 1, args.cpu_budget, args.cpu_budget + 600)
+        if its:
+            nx, ny, nz = WORKLOADS[args.workload]
+            out["cpu_baseline"] = {"value": 1.0 / its[0], "unit": "iters/s", "cores": 1, "kind": "reference",
+                                   "sample": f"outer iteration 1 of the same {6 * nx * ny * nz}-cell case, "
+                                             f"reference C++ + LASPack restatement, 1 thread, set-up "
+                                             f"({setup:.1f} s) excluded"}
+        else:
+            out["cpu_baseline"] = {"value": None, "unit": "iters/s", "cores": 1, "kind": "reference",
+                                   "sample": err or "no iteration finished within the budget"}
+    if r == 0:
+        print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c3", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=240.0)
+    ap.add_argument("--ref-budget", type=float, default=150.0)
+    args = ap.parse_args()
+    r, w, lr = rank_info()
+    if w > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(lr))
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        run_reference(args, r, w)
+    else:
+        run_ours(args, r, w, lr)
+    if w > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,133 @@
+/*
+ * sysu_cfd.h -- C ABI of the GB300-native SIMPLE solver (libsysucfd.so).
+ *
+ * This is the solver-level drop-in boundary: the entry points below replace
+ * the reference's NavierStokesSolver / HeatConductionSolver driver sequence
+ * (reference src/main.cpp:8-33) and its SIMPLE outer loop
+ * (src/navier.cpp:13-97).  Inputs are the reference's own formats: a
+ * param.in keyword file (src/readparamfile.cpp:10-260) naming a Gmsh MSH 2.x
+ * ASCII mesh (src/Preprocessor.cpp:13-146).  All fields live on one GPU;
+ * host copies are made only on request.
+ *
+ * Conventions: plain pointers and sizes, int status codes (SYSU_OK = 0), the
+ * message of the last failure through sysu_last_error().  One solver per host
+ * thread; the library keeps no global state besides the error message
+ * (thread-local).  Nothing here exits the process: where the reference calls
+ * exit()/fatalRuntimeError, these functions return SYSU_ERR_SOLVE or
+ * SYSU_ERR_INPUT with the reference's message.
+ */
+#ifndef SYSU_CFD_H
+#define SYSU_CFD_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SYSU_OK 0
+#define SYSU_ERR_INPUT 1  /* bad param file / mesh / argument */
+#define SYSU_ERR_CUDA 2   /* CUDA runtime error (no device, launch failure) */
+#define SYSU_ERR_SOLVE 3  /* a convergence check of the reference failed */
+
+typedef struct sysu_case sysu_case;
+typedef struct sysu_solver sysu_solver;
+
+const char *sysu_last_error(void);
+int sysu_version(void);
+
+/* ---- host-only case access (needs no GPU) --------------------------------
+ * Parses param.in, reads the mesh, builds faces in the reference's order
+ * (Preprocessor.cpp:181-299), splits fluid and solid for conjugate heat
+ * transfer (Preprocessor.cpp:308-515) and computes the geometry of
+ * CycasSolver::CellFaceInfo (BasicSolver.cpp:317-512). */
+int sysu_case_load(const char *param_path, sysu_case **out);
+void sysu_case_free(sysu_case *c);
+/* out[0..11] = fluid Ncel, Nfac, Nbnd, Nvrt, NCoupledBnd, solid Ncel, Nfac,
+ * Nbnd, Nvrt, NCoupledBnd, has_solid, coupled region id */
+int sysu_case_info(const sysu_case *c, long *out, int n);
+/* Copy a geometry/topology array by name ("cell_vol", "cell_x", "face_n",
+ * "face_lambda", "bnd_distance", ...; prefix "solid_" for the solid).
+ * Returns the array's size in bytes (or -1 for an unknown name); copies
+ * min(size, nbytes) bytes when out is non-null. */
+long sysu_case_array(const sysu_case *c, const char *name, void *out, long nbytes);
+
+/* ---- GPU solver ------------------------------------------------------------
+ * create: main.cpp:14-28 (read, build, CellFaceInfo, CheckAndAllocate,
+ * InitFlowField) with every field uploaded to the current CUDA device. */
+int sysu_solver_create(const char *param_path, sysu_solver **out);
+void sysu_solver_destroy(sysu_solver *s);
+/* out[0..5] = Ncel, Nfac, Nbnd, solid Ncel, matrix stored entries, matrix true entries */
+int sysu_solver_info(sysu_solver *s, long *out, int n);
+/* Options (defaults = the reference's call sites):
+ *   "<eq>.eps" "<eq>.maxit" "<eq>.omega" "<eq>.kind" (0 CG, 1 BiCGSTAB)
+ *     for eq in mom, p, ke, t, ts (solid T);
+ *   "rtc" sets every eq's eps; "mom_batched" (1: u,v,w as one 3-RHS solve);
+ *   "solid_source" (W/m^3, an extension); "fatal_checks"; "timing". */
+int sysu_solver_set_option(sysu_solver *s, const char *key, double value);
+int sysu_solver_get_option(sysu_solver *s, const char *key, double *value);
+/* Run up to n bodies of the steady NSSolve loop (navier.cpp:33-68): velocity,
+ * pressure, k-epsilon, energy and solid conduction as configured.  Stops
+ * early when max(Residual) < ResidualSteady.  *done = iterations run. */
+int sysu_solver_iterate(sysu_solver *s, int n, int *done);
+/* NSSolve itself: MaxOuterStep-1 iterations with the steady break. */
+int sysu_solver_nssolve(sysu_solver *s, int *done);
+/* The individual methods, enqueued on the solver's stream (navier.h:103-116):
+ * CalculateVelocity, CalculatePressure, UpdateTurKEpsilon, UpdateEnergy,
+ * HeatConductionSolver::solve.  sysu_solver_check() then reads the residuals
+ * and applies the reference's convergence checks. */
+int sysu_solver_calculate_velocity(sysu_solver *s);
+int sysu_solver_calculate_pressure(sysu_solver *s);
+int sysu_solver_update_turkeps(sysu_solver *s);
+int sysu_solver_update_energy(sysu_solver *s);
+int sysu_solver_heat_conduction(sysu_solver *s);
+int sysu_solver_check(sysu_solver *s);
+/* Back to the state right after creation (InitFlowField); keeps the mesh,
+ * matrices and options. */
+int sysu_solver_reset(sysu_solver *s);
+/* CUDA events on the solver's stream: start, then stop returns the elapsed
+ * device time in ms (stop synchronises). */
+int sysu_solver_timer_start(sysu_solver *s);
+int sysu_solver_timer_stop(sysu_solver *s, double *ms);
+/* Number of kernels the library has launched so far (all solvers). */
+long sysu_kernel_launches(void);
+/* Residual[0..9] of the last iteration (navier.h:65). */
+int sysu_solver_residuals(sysu_solver *s, double *out10);
+/* Per solve slot (mom u/v/w, p', k, eps, T, solid T): iterations, residual,
+ * status (0 converged, 1 max iterations, 2 breakdown, 3 barrier timeout,
+ * 4 non-finite).  Arrays of 6*3 entries, slot-major. */
+int sysu_solver_solve_stats(sysu_solver *s, int *iters, double *res, int *status);
+/* CUDA-event times of the last p' and momentum solves (option "timing"). */
+int sysu_solver_timing(sysu_solver *s, double *p_ms, double *mom_ms);
+/* Fields by the reference's member names: cell fields "U" "V" "W" "P" "R"
+ * "T" "TE" "ED" "VisLam" "VisTur" "Apr"; gradients "dUdX" "dVdX" "dWdX"
+ * "dPdX" "dPhidX" (3 per cell, cell-major); "RUFace" (reference face order);
+ * boundary arrays "BU" "BV" "BW" "BRo" "BPre" "BTem" "BTE" "BED" "Bq";
+ * "dp" (last p'), "bp" (its right-hand side), "b3"/"x3" (momentum right-hand
+ * sides / solutions, 3*Ncel component-major); solid: "solid_T" "solid_dPhidX" "solid_BTem" "solid_Bq".
+ * n must equal the field's size (sysu_solver_field_size). */
+long sysu_solver_field_size(sysu_solver *s, const char *name);
+int sysu_solver_get_field(sysu_solver *s, const char *name, double *out, long n);
+int sysu_solver_set_field(sysu_solver *s, const char *name, const double *in, long n);
+int sysu_solver_sync(sysu_solver *s);
+/* Assembled matrix "mom", "p", "scalar" (last k/eps/T) or "solid" as CSR,
+ * diagonal first in each row.  With rowptr == NULL returns the entry count;
+ * otherwise fills rowptr[n+1], col[], val[] and returns the count (-1: error). */
+long sysu_solver_matrix(sysu_solver *s, const char *which, int *rowptr, int *col, double *val);
+
+/* ---- standalone sparse solves on the GPU ------------------------------------
+ * The Krylov kernels of the SIMPLE path applied to a host CSR matrix (0-based,
+ * any column order).  method: 0 CG, 1 BiCGSTAB; precond: 0 none, 1 Jacobi
+ * (y = omega D^-1 c).  Stopping test ||b - A x||_2 / ||b||_2 < eps, as the
+ * reference's SolveLinearEqu (tools.cpp:56-64) expects.  x: x0 in, solution out.
+ * status: 0 converged, 1 max iterations, 2 breakdown, 3 barrier timeout,
+ * 4 non-finite. */
+int sysu_csr_solve(int method, int precond, int n, const int *rowptr, const int *col, const double *val,
+                   const double *b, double *x, int maxit, double eps, double omega, int *iters, double *res,
+                   int *status);
+int sysu_csr_spmv(int n, const int *rowptr, const int *col, const double *val, const double *x, double *y);
+const char *sysu_csr_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,346 @@
+// C ABI of libsysucfd.so (declared in include/sysu_cfd.h).
+#include "../../include/sysu_cfd.h"
+
+#include <cstring>
+#include <exception>
+#include <string>
+
+#include "handles.hpp"
+
+namespace {
+thread_local std::string g_err;
+
+int set_err(int code, const std::string &m) {
+    g_err = m;
+    return code;
+}
+
+template <class F>
+int guarded(F &&fn) {
+    try {
+        return fn();
+    } catch (const sysu::CaseError &e) {
+        bool cuda = e.msg.find("cuda") != std::string::npos || e.msg.find("CUDA") != std::string::npos;
+        return set_err(cuda ? SYSU_ERR_CUDA : SYSU_ERR_INPUT, e.msg);
+    } catch (const std::exception &e) {
+        return set_err(SYSU_ERR_INPUT, e.what());
+    }
+}
+
+template <class T>
+long copy_vec(const std::vector<T> &v, void *out, long nbytes) {
+    long sz = (long)(v.size() * sizeof(T));
+    if (out && nbytes > 0) std::memcpy(out, v.data(), (size_t)std::min(sz, nbytes));
+    return sz;
+}
+
+sysu::EqOpts *eq_of(sysu::SolverOptions &o, const std::string &k) {
+    if (k == "mom") return &o.mom;
+    if (k == "p") return &o.p;
+    if (k == "ke") return &o.ke;
+    if (k == "t") return &o.t;
+    if (k == "ts") return &o.ts;
+    return nullptr;
+}
+}  // namespace
+
+extern "C" {
+
+const char *sysu_last_error(void) { return g_err.c_str(); }
+int sysu_version(void) { return 1; }
+
+int sysu_case_load(const char *param_path, sysu_case **out) {
+    if (!param_path || !out) return set_err(SYSU_ERR_INPUT, "null argument");
+    *out = nullptr;
+    return guarded([&] {
+        sysu_case *c = new sysu_case;
+        try {
+            c->cs.params = sysu::parse_params(param_path);
+            std::string grid = c->cs.params.gridfile;
+            sysu::RawMesh raw;
+            try {
+                raw = sysu::read_msh(grid);
+            } catch (const sysu::CaseError &) {
+                std::string pp(param_path);
+                size_t slash = pp.find_last_of('/');
+                if (slash == std::string::npos || (!grid.empty() && grid[0] == '/')) throw;
+                raw = sysu::read_msh(pp.substr(0, slash + 1) + grid);
+            }
+            sysu::build_case(raw, c->cs);
+        } catch (...) {
+            delete c;
+            throw;
+        }
+        *out = c;
+        return SYSU_OK;
+    });
+}
+
+void sysu_case_free(sysu_case *c) { delete c; }
+
+int sysu_case_info(const sysu_case *c, long *out, int n) {
+    if (!c || !out) return set_err(SYSU_ERR_INPUT, "null argument");
+    long v[12] = {c->cs.fluid.nc, c->cs.fluid.nf, c->cs.fluid.nb, c->cs.fluid.nv, c->cs.fluid.ncb,
+                  c->cs.solid.nc, c->cs.solid.nf, c->cs.solid.nb, c->cs.solid.nv, c->cs.solid.ncb,
+                  c->cs.has_solid ? 1 : 0, c->cs.coupled_rid};
+    for (int i = 0; i < n && i < 12; ++i) out[i] = v[i];
+    return SYSU_OK;
+}
+
+long sysu_case_array(const sysu_case *c, const char *name, void *out, long nbytes) {
+    if (!c || !name) return -1;
+    std::string nm(name);
+    const sysu::Domain *d = &c->cs.fluid;
+    if (nm.rfind("solid_", 0) == 0) {
+        if (!c->cs.has_solid) return -1;
+        d = &c->cs.solid;
+        nm = nm.substr(6);
+    }
+    if (nm == "cell_vol") return copy_vec(d->cell_vol, out, nbytes);
+    if (nm == "cell_x") return copy_vec(d->cell_x, out, nbytes);
+    if (nm == "cell_nface") return copy_vec(d->cell_nface, out, nbytes);
+    if (nm == "cell_face") return copy_vec(d->cell_face, out, nbytes);
+    if (nm == "cell_nbr") return copy_vec(d->cell_nbr, out, nbytes);
+    if (nm == "cell_rid") return copy_vec(d->cell_rid, out, nbytes);
+    if (nm == "cell_vert") return copy_vec(d->cell_vert, out, nbytes);
+    if (nm == "face_x") return copy_vec(d->face_x, out, nbytes);
+    if (nm == "face_n") return copy_vec(d->face_n, out, nbytes);
+    if (nm == "face_area") return copy_vec(d->face_area, out, nbytes);
+    if (nm == "face_lambda") return copy_vec(d->face_lambda, out, nbytes);
+    if (nm == "face_rlencos") return copy_vec(d->face_rlencos, out, nbytes);
+    if (nm == "face_xpac") return copy_vec(d->face_xpac, out, nbytes);
+    if (nm == "face_xnac") return copy_vec(d->face_xnac, out, nbytes);
+    if (nm == "face_c1") return copy_vec(d->face_c1, out, nbytes);
+    if (nm == "face_c2") return copy_vec(d->face_c2, out, nbytes);
+    if (nm == "face_bnd") return copy_vec(d->face_bnd, out, nbytes);
+    if (nm == "face_vert") return copy_vec(d->face_vert, out, nbytes);
+    if (nm == "bnd_face") return copy_vec(d->bnd_face, out, nbytes);
+    if (nm == "bnd_rid") return copy_vec(d->bnd_rid, out, nbytes);
+    if (nm == "bnd_distance") return copy_vec(d->bnd_distance, out, nbytes);
+    if (nm == "vert") return copy_vec(d->vert, out, nbytes);
+    return -1;
+}
+
+int sysu_solver_create(const char *param_path, sysu_solver **out) {
+    if (!param_path || !out) return set_err(SYSU_ERR_INPUT, "null argument");
+    *out = nullptr;
+    return guarded([&] {
+        sysu_solver *s = new sysu_solver{nullptr};
+        try {
+            s->impl = new sysu::SimpleSolver(param_path);
+        } catch (...) {
+            delete s;
+            throw;
+        }
+        *out = s;
+        return SYSU_OK;
+    });
+}
+
+void sysu_solver_destroy(sysu_solver *s) {
+    if (!s) return;
+    try {
+        delete s->impl;
+    } catch (...) {
+    }
+    delete s;
+}
+
+int sysu_solver_info(sysu_solver *s, long *out, int n) {
+    if (!s || !out) return set_err(SYSU_ERR_INPUT, "null argument");
+    sysu::SimpleSolver &S = *s->impl;
+    long v[6] = {S.fd.nc, S.fd.nf, S.fd.B, S.cs.has_solid ? S.sd.nc : 0, S.fd.A.nnz, S.fd.A.nnz_true};
+    for (int i = 0; i < n && i < 6; ++i) out[i] = v[i];
+    return SYSU_OK;
+}
+
+int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
+    if (!s || !key) return set_err(SYSU_ERR_INPUT, "null argument");
+    sysu::SolverOptions &o = s->impl->opt;
+    std::string k(key);
+    if (k == "rtc") {
+        o.mom.eps = o.p.eps = o.ke.eps = o.t.eps = o.ts.eps = value;
+        return SYSU_OK;
+    }
+    if (k == "mom_batched") { o.mom_batched = value != 0.0; return SYSU_OK; }
+    if (k == "solid_source") { o.solid_source = value; return SYSU_OK; }
+    if (k == "fatal_checks") { o.fatal_checks = value != 0.0; return SYSU_OK; }
+    if (k == "timing") { o.timing = value != 0.0; return SYSU_OK; }
+    size_t dot = k.find('.');
+    if (dot != std::string::npos) {
+        sysu::EqOpts *e = eq_of(o, k.substr(0, dot));
+        std::string f = k.substr(dot + 1);
+        if (e) {
+            if (f == "eps") { e->eps = value; return SYSU_OK; }
+            if (f == "maxit") { e->maxit = (int)value; return SYSU_OK; }
+            if (f == "omega") { e->omega = value; return SYSU_OK; }
+            if (f == "kind") {
+                int kind = (int)value;
+                if (kind != sysu::SK_CG && kind != sysu::SK_BICGSTAB) return set_err(SYSU_ERR_INPUT, "kind: 0 CG, 1 BiCGSTAB");
+                if (kind == sysu::SK_CG && e == &o.mom) return set_err(SYSU_ERR_INPUT, "momentum matrix is not symmetric");
+                e->kind = kind;
+                return SYSU_OK;
+            }
+        }
+    }
+    return set_err(SYSU_ERR_INPUT, "unknown option " + k);
+}
+
+int sysu_solver_get_option(sysu_solver *s, const char *key, double *value) {
+    if (!s || !key || !value) return set_err(SYSU_ERR_INPUT, "null argument");
+    sysu::SolverOptions &o = s->impl->opt;
+    std::string k(key);
+    if (k == "mom_batched") { *value = o.mom_batched; return SYSU_OK; }
+    if (k == "solid_source") { *value = o.solid_source; return SYSU_OK; }
+    if (k == "fatal_checks") { *value = o.fatal_checks; return SYSU_OK; }
+    if (k == "timing") { *value = o.timing; return SYSU_OK; }
+    size_t dot = k.find('.');
+    if (dot != std::string::npos) {
+        sysu::EqOpts *e = eq_of(o, k.substr(0, dot));
+        std::string f = k.substr(dot + 1);
+        if (e) {
+            if (f == "eps") { *value = e->eps; return SYSU_OK; }
+            if (f == "maxit") { *value = e->maxit; return SYSU_OK; }
+            if (f == "omega") { *value = e->omega; return SYSU_OK; }
+            if (f == "kind") { *value = e->kind; return SYSU_OK; }
+        }
+    }
+    return set_err(SYSU_ERR_INPUT, "unknown option " + k);
+}
+
+static int run_iterations(sysu_solver *s, int n, int *done) {
+    sysu::SimpleSolver &S = *s->impl;
+    int k = 0;
+    for (; k < n; ++k) {
+        std::string msg = S.outer_iteration();
+        if (!msg.empty()) {
+            if (done) *done = k + 1;
+            return set_err(SYSU_ERR_SOLVE, msg);
+        }
+        double resmax = 0.0;  // vec_max starts from 0 (tools.cpp:81-87)
+        for (double r : S.Residual) resmax = resmax > r ? resmax : r;
+        if (S.cs.params.steady && resmax < S.cs.params.residual_steady) {
+            ++k;
+            break;
+        }
+    }
+    if (done) *done = k;
+    return SYSU_OK;
+}
+
+int sysu_solver_iterate(sysu_solver *s, int n, int *done) {
+    if (!s) return set_err(SYSU_ERR_INPUT, "null argument");
+    return guarded([&] { return run_iterations(s, n, done); });
+}
+
+int sysu_solver_nssolve(sysu_solver *s, int *done) {
+    if (!s) return set_err(SYSU_ERR_INPUT, "null argument");
+    return guarded([&] { return run_iterations(s, s->impl->cs.params.max_outer_step - 1, done); });
+}
+
+#define SYSU_METHOD(cname, call)                                                  \
+    int cname(sysu_solver *s) {                                                   \
+        if (!s) return set_err(SYSU_ERR_INPUT, "null argument");                  \
+        return guarded([&] {                                                      \
+            s->impl->call;                                                        \
+            return SYSU_OK;                                                       \
+        });                                                                       \
+    }
+
+SYSU_METHOD(sysu_solver_calculate_velocity, calculate_velocity())
+SYSU_METHOD(sysu_solver_calculate_pressure, calculate_pressure())
+SYSU_METHOD(sysu_solver_update_turkeps, update_ke())
+SYSU_METHOD(sysu_solver_update_energy, update_energy())
+SYSU_METHOD(sysu_solver_sync, sync())
+
+int sysu_solver_heat_conduction(sysu_solver *s) {
+    if (!s) return set_err(SYSU_ERR_INPUT, "null argument");
+    if (!s->impl->cs.has_solid) return set_err(SYSU_ERR_INPUT, "case has no solid");
+    return guarded([&] {
+        s->impl->solid_solve();
+        return SYSU_OK;
+    });
+}
+
+int sysu_solver_check(sysu_solver *s) {
+    if (!s) return set_err(SYSU_ERR_INPUT, "null argument");
+    return guarded([&] {
+        std::string msg = s->impl->check_iteration();
+        if (!msg.empty()) return set_err(SYSU_ERR_SOLVE, msg);
+        return SYSU_OK;
+    });
+}
+
+int sysu_solver_reset(sysu_solver *s) {
+    if (!s) return set_err(SYSU_ERR_INPUT, "null argument");
+    return guarded([&] {
+        s->impl->reset();
+        return SYSU_OK;
+    });
+}
+
+int sysu_solver_timer_start(sysu_solver *s) {
+    if (!s) return set_err(SYSU_ERR_INPUT, "null argument");
+    return guarded([&] {
+        s->impl->timer_start();
+        return SYSU_OK;
+    });
+}
+
+int sysu_solver_timer_stop(sysu_solver *s, double *ms) {
+    if (!s || !ms) return set_err(SYSU_ERR_INPUT, "null argument");
+    return guarded([&] {
+        *ms = s->impl->timer_stop();
+        return SYSU_OK;
+    });
+}
+
+long sysu_kernel_launches(void) { return sysu::g_launches.load(); }
+
+int sysu_solver_residuals(sysu_solver *s, double *out10) {
+    if (!s || !out10) return set_err(SYSU_ERR_INPUT, "null argument");
+    for (int k = 0; k < 10; ++k) out10[k] = s->impl->Residual[k];
+    return SYSU_OK;
+}
+
+int sysu_solver_solve_stats(sysu_solver *s, int *iters, double *res, int *status) {
+    if (!s) return set_err(SYSU_ERR_INPUT, "null argument");
+    for (int k = 0; k < sysu::SLOT_N; ++k)
+        for (int c = 0; c < 3; ++c) {
+            const sysu::SolveInfo &I = s->impl->last_info[k];
+            if (iters) iters[k * 3 + c] = I.iters[c];
+            if (res) res[k * 3 + c] = I.res[c];
+            if (status) status[k * 3 + c] = I.status[c];
+        }
+    return SYSU_OK;
+}
+
+int sysu_solver_timing(sysu_solver *s, double *p_ms, double *mom_ms) {
+    if (!s) return set_err(SYSU_ERR_INPUT, "null argument");
+    if (p_ms) *p_ms = s->impl->last_p_ms;
+    if (mom_ms) *mom_ms = s->impl->last_mom_ms;
+    return SYSU_OK;
+}
+
+long sysu_solver_field_size(sysu_solver *s, const char *name) {
+    if (!s || !name) return -1;
+    return s->impl->field_size(name);
+}
+
+int sysu_solver_get_field(sysu_solver *s, const char *name, double *out, long n) {
+    if (!s || !name || !out) return set_err(SYSU_ERR_INPUT, "null argument");
+    return guarded([&] {
+        s->impl->get_field(name, out, n);
+        return SYSU_OK;
+    });
+}
+
+int sysu_solver_set_field(sysu_solver *s, const char *name, const double *in, long n) {
+    if (!s || !name || !in) return set_err(SYSU_ERR_INPUT, "null argument");
+    return guarded([&] {
+        s->impl->set_field(name, in, n);
+        return SYSU_OK;
+    });
+}
+
+}  // extern "C"

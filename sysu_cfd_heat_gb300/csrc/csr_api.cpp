@@ -1,0 +1,169 @@
+// Standalone sparse entry points of the C ABI: solve / multiply with a
+// host-side CSR matrix on the GPU, and read back an assembled matrix of a
+// solver in CSR form.  They share the persistent Krylov kernels of the SIMPLE
+// path (krylov.cu).
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/sysu_cfd.h"
+#include "handles.hpp"
+
+namespace sysu {
+
+// CSR (any column order, 0-based) -> row lists with the diagonal first.
+static void csr_rows_diag_first(int n, const int *rowptr, const int *col, const double *val, std::vector<int> &rp,
+                                std::vector<int> &cl, std::vector<double> &vl) {
+    rp.assign(n + 1, 0);
+    cl.clear();
+    vl.clear();
+    cl.reserve((size_t)rowptr[n] + n);
+    vl.reserve((size_t)rowptr[n] + n);
+    for (int i = 0; i < n; ++i) {
+        double d = 0.0;
+        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k)
+            if (col[k] == i) d += val[k];
+        cl.push_back(i);
+        vl.push_back(d);
+        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+            if (col[k] < 0 || col[k] >= n) throw CaseError{"column index out of range"};
+            if (col[k] == i) continue;
+            cl.push_back(col[k]);
+            vl.push_back(val[k]);
+        }
+        rp[i + 1] = (int)cl.size();
+    }
+}
+
+struct CsrDevice {
+    SellPattern pat;
+    SellDev A;
+    DevBuf<double> val;
+    void load(int n, const int *rowptr, const int *col, const double *v, cudaStream_t st) {
+        std::vector<int> rp, cl;
+        std::vector<double> vl;
+        csr_rows_diag_first(n, rowptr, col, v, rp, cl, vl);
+        pat = make_sell(n, rp, cl);
+        A.upload(pat, st);
+        std::vector<double> sv(pat.nnz, 0.0);
+        for (int i = 0; i < n; ++i)
+            for (int k = rp[i]; k < rp[i + 1]; ++k) sv[pat.pos(i, k - rp[i])] = vl[k];
+        val.upload(sv, st);
+    }
+};
+
+}  // namespace sysu
+
+namespace {
+thread_local std::string g_csr_err;
+}
+
+extern "C" {
+
+// method: 0 CG, 1 BiCGSTAB; precond: 0 none, 1 Jacobi (omega D^-1).
+// x holds x0 on entry and the solution on return.  Returns 0, or an error.
+int sysu_csr_solve(int method, int precond, int n, const int *rowptr, const int *col, const double *val,
+                   const double *b, double *x, int maxit, double eps, double omega, int *iters, double *res,
+                   int *status) {
+    try {
+        cudaStream_t st;
+        SYSU_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        {
+            sysu::CsrDevice M;
+            M.load(n, rowptr, col, val, st);
+            sysu::DevBuf<double> db(n), dx(n);
+            db.upload(b, n, st);
+            dx.upload(x, n, st);
+            sysu::KrylovWork w;
+            sysu::DevBuf<sysu::SolveInfo> info(1);
+            sysu::KrylovOpts o;
+            o.maxit = maxit;
+            o.eps = eps;
+            o.omega = omega;
+            o.jacobi = precond == 1;
+            if (method == 0) {
+                sysu::cg_solve(M.A, M.val.get(), db.get(), dx.get(), false, o, w, info.get(), st);
+            } else {
+                const double *bb[1] = {db.get()};
+                double *xx[1] = {dx.get()};
+                sysu::bicgstab_solve(M.A, M.val.get(), 1, bb, xx, o, w, info.get(), st);
+            }
+            sysu::SolveInfo h;
+            info.download(&h, 1, st);
+            dx.download(x, n, st);
+            SYSU_CUDA(cudaStreamSynchronize(st));
+            if (iters) *iters = h.iters[0];
+            if (res) *res = h.res[0];
+            if (status) *status = h.err ? sysu::DEV_BARRIER_TIMEOUT : h.status[0];
+        }
+        cudaStreamDestroy(st);
+        return SYSU_OK;
+    } catch (const sysu::CaseError &e) {
+        g_csr_err = e.msg;
+        return SYSU_ERR_CUDA;
+    }
+}
+
+// y = A x for a host CSR matrix, on the GPU.
+int sysu_csr_spmv(int n, const int *rowptr, const int *col, const double *val, const double *x, double *y) {
+    try {
+        cudaStream_t st;
+        SYSU_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        {
+            sysu::CsrDevice M;
+            M.load(n, rowptr, col, val, st);
+            sysu::DevBuf<double> dx(n), dy(n);
+            dx.upload(x, n, st);
+            sysu::spmv(M.A, M.val.get(), dx.get(), dy.get(), st);
+            dy.download(y, n, st);
+            SYSU_CUDA(cudaStreamSynchronize(st));
+        }
+        cudaStreamDestroy(st);
+        return SYSU_OK;
+    } catch (const sysu::CaseError &e) {
+        g_csr_err = e.msg;
+        return SYSU_ERR_CUDA;
+    }
+}
+
+const char *sysu_csr_last_error(void) { return g_csr_err.c_str(); }
+
+// Assembled matrix of a solver ("mom", "p", "scalar", "solid") as CSR with the
+// diagonal first in each row.  rowptr: n+1, col/val: the true entry count
+// (sysu_solver_info out[5], or the solid's own count).  Returns the entry count.
+long sysu_solver_matrix(sysu_solver *s, const char *which, int *rowptr, int *col, double *val) {
+    if (!s || !which) return -1;
+    try {
+        sysu::SimpleSolver &S = *s->impl;
+        std::string w(which);
+        const sysu::DomainDev *d = &S.fd;
+        const sysu::DevBuf<double> *v = nullptr;
+        if (w == "mom") v = &S.f.Amom;
+        else if (w == "p") v = &S.f.Ap;
+        else if (w == "scalar") v = &S.f.As;
+        else if (w == "solid" && S.cs.has_solid) { d = &S.sd; v = &S.s.As; }
+        else return -1;
+        const sysu::SellPattern &p = d->pat;
+        if (!rowptr) return p.nnz_true;
+        std::vector<double> h(p.nnz);
+        v->download(h.data(), p.nnz, S.st);
+        SYSU_CUDA(cudaStreamSynchronize(S.st));
+        long k = 0;
+        rowptr[0] = 0;
+        for (int i = 0; i < p.n; ++i) {
+            for (int j = 0; j < p.row_len[i]; ++j) {
+                col[k] = p.col[p.pos(i, j)];
+                val[k] = h[p.pos(i, j)];
+                ++k;
+            }
+            rowptr[i + 1] = (int)k;
+        }
+        return k;
+    } catch (const sysu::CaseError &e) {
+        g_csr_err = e.msg;
+        return -1;
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,174 @@
+// Device views of one finite-volume domain and the kernel launchers that
+// implement the SIMPLE hot path.  Views are plain structs of device pointers
+// passed by value to kernels.
+//
+// Face numbering on the device ("internal" order): interior faces first, in
+// the reference's relative order, then one face per boundary record, in
+// boundary-record order (face F+b belongs to record b).  The permutation to
+// the reference's face ids is kept for field input/output.
+//
+// Vectors of 3-vectors are stored structure-of-arrays: component c of item i
+// at [c*n + i].
+#pragma once
+
+#include "krylov.hpp"
+
+namespace sysu {
+
+struct DomView {
+    int nc, nf, F, B, ncb;       // cells, faces, interior faces, boundary records, first coupled record
+    // cells
+    const double *vol, *cx;      // cx: 3*nc
+    const int *cs_ptr;           // nc+1 (slots = reference Cell[i].face[j] order)
+    const int *cs_face;          // internal face id of each slot
+    const int *cs_k;             // interior slot: position k >= 1 in the matrix row; boundary slot: record b
+    // faces
+    const int *fc1, *fc2;        // fc2 < 0 on boundary faces
+    const double *fn, *farea, *flam, *frl, *fx;  // fn, fx: 3*nf
+    const double *fxpac, *fxnac; // 3*F
+    // boundary records
+    const int *bcell, *btype1, *btype2, *brid;
+    const double *bdist;
+    const double *bquirk_area;   // area of reference face id b (navier_bc.cpp:72 reads Face[i])
+    // per-record inlet values (region initvalues) and fixed values
+    const double *bin;           // 8*B: u v w p r t te ed (SoA)
+    const double *bfixed;        // B
+    // cell -> wall boundary records (type1 == 1), ascending record order
+    const int *cw_ptr, *cw_b;
+    // vertices (limiters)
+    int nv;
+    const double *vx;            // 3*nv
+    const int *cvert;            // 8*nc (SoA: [k*nc + i])
+    const int *vc_ptr, *vc_cell; // vertex -> cells
+    // matrix pattern
+    SellView A;                  // val filled per equation
+};
+
+// Launch configuration shared by the FV kernels.
+constexpr int FV_BLOCK = 256;
+
+// Reduction scratch: per-block partials and the final values, plus a ticket.
+struct RedScratch {
+    double *partials;   // NSLOT * max_blocks
+    double *out;        // NSLOT
+    unsigned int *ticket;
+    int max_blocks;
+};
+
+enum RedSlotId {
+    RED_MASS_IN = 0, RED_MASS_OUT, RED_AREA_OUT,   // SetBCVelocity sums
+    RED_RES0, RED_RES1, RED_RES2, RED_RES3,        // Residual[0..3]
+    RED_HEAT_F, RED_HEAT_S,                        // interface heat balance
+    RED_MISC0, RED_MISC1, RED_MISC2,
+    RED_NSLOT
+};
+
+// ---- kernels (fv.cu) ------------------------------------------------------
+// SetBCVelocity, navier_bc.cpp:8-108 (density model 0: outlet mass rescaling)
+void launch_bc_velocity(const DomView &d, const double *R, const double *U, const double *V, const double *W,
+                        double *BRo, double *BU, double *BV, double *BW, bool has_outlet, RedScratch rs,
+                        cudaStream_t st);
+// Green-Gauss gradient (BasicSolver.cpp:29-63) of 1, 3 or 4 fields with
+// boundary values Bphi[k].
+void launch_gradient(const DomView &d, int nfield, const double *const *phi, const double *const *Bphi,
+                     double *const *grad, cudaStream_t st);
+// Limiters (BasicSolver.cpp:118-288) applied in place to grad of phi.
+void launch_limiter(const DomView &d, int limiter, const double *phi, double *grad, double *tmp3,
+                    double *tmp_v, cudaStream_t st);
+
+struct MomArgs {
+    const double *U, *V, *W, *R, *VisLam, *VisTur, *RUFace, *dU, *dV, *dW, *dP;
+    const double *BU, *BV, *BW;
+    double urf;
+    double g[3];
+    double *fD, *fE;       // per interior face: D, E (3*F)
+    double *bapp, *bsrc;   // per boundary record: diag part, explicit source (3*B)
+    double *val;           // matrix values (SELL)
+    double *bu, *bv, *bw;  // right-hand sides
+    double *Apr;
+    int *flags;            // error flags (e.g. unknown boundary type)
+};
+// BuildVelocityMatrix, navier_velocity.cpp:77-357 (steady)
+void launch_momentum(const DomView &d, const MomArgs &a, cudaStream_t st);
+
+// L1 change residual and commit: res += sum |old - new| * vol, old = new
+// (navier_velocity.cpp:31-34).  3 fields at once (slots RED_RES0..2).
+void launch_commit3(const DomView &d, double *U, double *V, double *W, const double *x3, RedScratch rs,
+                    cudaStream_t st);
+
+struct PresArgs {
+    const double *U, *V, *W, *R, *P, *dP, *Apr;
+    const double *BRo, *BU, *BV, *BW;
+    double *RUFace;        // out: Rhie-Chow flux (internal face order)
+    double *fcoef;         // out: (rho Apr)_f vol_f rlencos per interior face
+    double *val, *bp;      // p' matrix (full symmetric storage) and right-hand side
+};
+// CalRUFace2 (navier_velocity.cpp:389-442) + BuildPressureMatrix (navier_pressure.cpp:78-198)
+void launch_pressure_assembly(const DomView &d, const PresArgs &a, cudaStream_t st);
+
+struct CorrArgs {
+    const double *dp, *dPdp;   // p' and its gradient
+    const double *Apr, *R;
+    double *P, *U, *V, *W;
+    double urf_p;
+    int cell_ref;
+};
+// navier_pressure.cpp:38-56: Residual[3], pressure and velocity correction
+void launch_correct_cells(const DomView &d, const CorrArgs &a, RedScratch rs, cudaStream_t st);
+// CorrectRUFace2, navier_pressure.cpp:200-242 (density model 0)
+// (the face coefficient of the p' assembly, fcoef, is reused: Apr and rho are unchanged)
+void launch_correct_faces(const DomView &d, const double *dp, const double *dPdp, const double *R,
+                          const double *Apr, const double *BRo, const double *BU, const double *BV,
+                          const double *BW, double urf_p, double *RUFace, const double *fcoef, cudaStream_t st);
+// Bphi[b] = phi(cell of b) for every record: SetBCPressure / SetBCDeltaP (navier_bc.cpp:110-162)
+void launch_bnd_from_cell(const DomView &d, const double *phi, double *Bphi, cudaStream_t st);
+
+// Generic scalar transport assembly (navier_scalar.cpp:466-647,
+// HeatConductionSolver.cpp:175-288).
+enum ScalarBc { SC_FLUID_PLAIN = 0, SC_FLUID_ENERGY = 1, SC_SOLID = 2 };
+struct ScalarArgs {
+    const double *phi, *Bphi, *diff, *src, *app0, *grad, *RUFace, *Bq;
+    double urf;
+    int bc_mode;           // ScalarBc
+    double *fD, *fE;       // interior face scratch (fE: F)
+    double *bapp, *bsrc;   // boundary scratch
+    double *val, *b;
+    int *flags;
+};
+void launch_scalar(const DomView &d, const ScalarArgs &a, cudaStream_t st);
+
+// k-epsilon pieces (navier_scalar.cpp:36-67,116-161; navier_bc.cpp:209-296)
+struct KeArgs {
+    const double *dU, *dV, *dW, *R, *VisLam, *U, *V, *W;
+    double *TE, *ED, *VisTur;
+    double *Prod, *TESrc, *EDSrc, *VisTE, *VisED, *ApTE, *ApED;
+    double *BTE, *BED;
+};
+void launch_ke_sources(const DomView &d, const KeArgs &a, cudaStream_t st);      // per cell + wall functions
+void launch_ke_bnd_values(const DomView &d, const KeArgs &a, cudaStream_t st);   // inlet/outlet/sym BTE, BED
+void launch_ke_eps_sources(const DomView &d, const KeArgs &a, cudaStream_t st);  // after k is solved
+void launch_ke_eps_wall_rows(const DomView &d, const double *ED, double *val, double *b, cudaStream_t st);
+void launch_clip_max(double *dst, const double *src, double lo, int n, cudaStream_t st);
+void launch_visc_tur(int n, const double *R, const double *TE, const double *ED, double *VisTur, cudaStream_t st);
+
+// energy (navier_scalar.cpp:257-397, navier_bc.cpp:164-203, HeatConductionSolver.cpp:13-44,373-427)
+void launch_kcond(int n, const double *VisLam, const double *VisTur, double cp, double prl, double prte,
+                  double *kcond, cudaStream_t st);
+void launch_bc_temperature_fluid(const DomView &d, const double *T, double *BTem, cudaStream_t st);
+void launch_bc_temperature_solid(const DomView &d, const double *T, const double *diff, const double *Bq,
+                                 double *BTem, cudaStream_t st);
+// solid -> fluid: fluid BTem of coupled record k = T_s + grad T_s . (x_f - x_c)
+void launch_cht_solid2fluid(const DomView &s, const double *Ts, const double *gTs, const DomView &f,
+                            double *BTem_f, cudaStream_t st);
+// fluid -> solid: q_f = -k grad T_f . n / |S|, q_s = -q_f
+void launch_cht_fluid2solid(const DomView &f, const double *gTf, const double *kcond, double *Bq_f,
+                            const DomView &s, double *Bq_s, cudaStream_t st);
+
+void launch_fill(double *x, double v, int n, cudaStream_t st);
+void launch_copy(double *dst, const double *src, int n, cudaStream_t st);
+void launch_scale_src(double *dst, const double *vol, double q, int n, cudaStream_t st);  // dst = q*vol
+
+// Reset the reduction slots and tickets.
+void red_reset(RedScratch rs, cudaStream_t st);
+
+}  // namespace sysu

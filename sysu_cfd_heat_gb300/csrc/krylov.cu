@@ -1,0 +1,552 @@
+// Persistent cooperative Krylov solvers on SELL-32 matrices (FP64).
+//
+// One solve = one cooperative launch.  Rows are distributed thread-per-row with
+// a grid stride that is a multiple of 32, so each warp owns whole slices.
+// Global dot products are reduced deterministically: warp shuffles, then the
+// block, then every block sums the per-block partials in the same fixed order,
+// so all blocks take identical convergence decisions and repeated runs are
+// bit-identical.  Every barrier wait is bounded (device.hpp).
+//
+// Algorithms (restated from Barrett et al., "Templates", Figs. 2.5 and 2.10;
+// they are the same recurrences as the CPU oracle's LASPack restatement):
+//   CG        z = M^-1 r, rho = r.z, p = z + beta p, q = A p, alpha = rho/(p.q)
+//   BiCGSTAB  right preconditioned, early exit on ||s||, breakdown on rho = 0
+// M = D / omega (Jacobi).  Stopping test ||r||_2 / ||b||_2 < eps.
+#include "krylov.hpp"
+
+#include <algorithm>
+#include <cmath>
+
+namespace sysu {
+
+std::atomic<long> g_launches{0};
+
+SellPattern make_sell(int n, const std::vector<int> &row_ptr, const std::vector<int> &cols) {
+    SellPattern p;
+    p.n = n;
+    p.nslices = (n + 31) / 32;
+    p.sl_ptr.assign(p.nslices + 1, 0);
+    p.sl_w.assign(p.nslices, 0);
+    p.row_len.assign(n, 0);
+    for (int i = 0; i < n; ++i) p.row_len[i] = row_ptr[i + 1] - row_ptr[i];
+    long off = 0;
+    for (int s = 0; s < p.nslices; ++s) {
+        int w = 0;
+        for (int i = s * 32; i < std::min(n, s * 32 + 32); ++i) w = std::max(w, p.row_len[i]);
+        p.sl_w[s] = w;
+        p.sl_ptr[s] = (int)off;
+        off += (long)w * 32;
+    }
+    p.sl_ptr[p.nslices] = (int)off;
+    p.nnz = off;
+    p.nnz_true = row_ptr[n];
+    p.col.assign(off, 0);
+    for (int s = 0; s < p.nslices; ++s) {
+        for (int lane = 0; lane < 32; ++lane) {
+            int i = s * 32 + lane;
+            int self = i < n ? i : (n - 1);
+            for (int k = 0; k < p.sl_w[s]; ++k) {
+                long e = (long)p.sl_ptr[s] + (long)k * 32 + lane;
+                p.col[e] = (i < n && k < p.row_len[i]) ? cols[row_ptr[i] + k] : self;
+            }
+        }
+    }
+    return p;
+}
+
+void SellDev::upload(const SellPattern &p, cudaStream_t s) {
+    n = p.n;
+    nslices = p.nslices;
+    nnz = p.nnz;
+    nnz_true = p.nnz_true;
+    sl_ptr.upload(p.sl_ptr, s);
+    sl_w.upload(p.sl_w, s);
+    col.upload(p.col, s);
+}
+
+namespace {
+
+constexpr int KB = 256;
+constexpr int NVMAX = 6;
+
+struct RedCtx {
+    double *partials;
+    int G;
+    int parity;
+};
+
+__device__ __shared__ double g_red_smem[NVMAX * (KB / 32)];
+__device__ __shared__ double g_red_res[NVMAX];
+
+// Block-reduce NV values, publish per-block partials, barrier, and give every
+// thread the NV global sums.  Partials alternate between two buffers so that a
+// block that runs ahead to the next reduction cannot overwrite values another
+// block is still reading.
+template <int NV>
+__device__ __forceinline__ bool grid_reduce(double (&v)[NV], RedCtx &rc, GridBarrier *gb, int *err) {
+    block_sum<NV>(v, g_red_smem);
+    double *buf = rc.partials + (size_t)rc.parity * NVMAX * rc.G;
+    rc.parity ^= 1;
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) buf[(size_t)k * rc.G + blockIdx.x] = v[k];
+    if (!grid_sync(gb, err)) return false;
+    if (threadIdx.x < 32) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double s = warp_sum_partials(buf + (size_t)k * rc.G, rc.G);
+            if (threadIdx.x == 0) g_red_res[k] = s;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = g_red_res[k];
+    __syncthreads();
+    return true;
+}
+
+__device__ __forceinline__ double row_dot(const SellView &A, int i, const double *__restrict__ x) {
+    int s = i >> 5;
+    int e = A.sl_ptr[s] + (i & 31);
+    int w = A.sl_w[s];
+    double acc = 0.0;
+    for (int k = 0; k < w; ++k, e += 32) acc += A.val[e] * x[A.col[e]];
+    return acc;
+}
+
+// y_c = A (dinv .* x_c) for NR right-hand sides, skipping inactive ones.
+template <int NR>
+__device__ __forceinline__ void row_dot_scaled(const SellView &A, int i, const double *__restrict__ dinv,
+                                               const double *__restrict__ x, int n, const bool (&act)[3],
+                                               double (&y)[NR]) {
+    int s = i >> 5;
+    int e = A.sl_ptr[s] + (i & 31);
+    int w = A.sl_w[s];
+#pragma unroll
+    for (int c = 0; c < NR; ++c) y[c] = 0.0;
+    for (int k = 0; k < w; ++k, e += 32) {
+        double a = A.val[e];
+        int j = A.col[e];
+        double d = dinv[j];
+#pragma unroll
+        for (int c = 0; c < NR; ++c)
+            if (act[c]) y[c] += a * (d * x[(size_t)c * n + j]);
+    }
+}
+
+__global__ void k_jacobi_dinv(SellView A, double omega, int jacobi, double *dinv) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.n) return;
+    if (!jacobi) {
+        dinv[i] = 1.0;
+        return;
+    }
+    double d = A.val[A.sl_ptr[i >> 5] + (i & 31)];
+    dinv[i] = omega / d;
+}
+
+__global__ void k_spmv(SellView A, const double *__restrict__ x, double *__restrict__ y) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.n) return;
+    y[i] = row_dot(A, i, x);
+}
+
+__global__ void k_zero(double *x, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = 0.0;
+}
+
+struct CgArgs {
+    SellView A;
+    const double *b;
+    double *x, *r, *p, *q;
+    const double *dinv;
+    double *partials;
+    GridBarrier *gb;
+    SolveInfo *info;
+    int maxit;
+    double eps;
+};
+
+__global__ void __launch_bounds__(KB) k_cg(CgArgs a) {
+    const int n = a.A.n;
+    const int T = gridDim.x * KB;
+    const int t0 = blockIdx.x * KB + threadIdx.x;
+    int *err = &a.info->err;
+    RedCtx rc{a.partials, (int)gridDim.x, 0};
+    const double *__restrict__ dinv = a.dinv;
+
+    // r = b - A x; ||b||^2, ||r||^2, rho = r . M^-1 r
+    double v3[3] = {0.0, 0.0, 0.0};
+    for (int i = t0; i < n; i += T) {
+        double bi = a.b[i];
+        double ri = bi - row_dot(a.A, i, a.x);
+        a.r[i] = ri;
+        v3[0] += bi * bi;
+        v3[1] += ri * ri;
+        v3[2] += ri * (dinv[i] * ri);
+    }
+    if (!grid_reduce<3>(v3, rc, a.gb, err)) return;
+    double bnorm = sqrt(v3[0]);
+    if (bnorm == 0.0) bnorm = 1.0;
+    double res = sqrt(v3[1]) / bnorm;
+    double rho = v3[2], rho_prev = 1.0;
+    int it = 0, status = DEV_OK;
+    while (!(res < a.eps) && it < a.maxit) {
+        if (!isfinite(res)) { status = DEV_NONFINITE; break; }
+        ++it;
+        double beta = (it == 1) ? 0.0 : rho / rho_prev;
+        for (int i = t0; i < n; i += T) {
+            double z = dinv[i] * a.r[i];
+            a.p[i] = (it == 1) ? z : z + beta * a.p[i];
+        }
+        if (!grid_sync(a.gb, err)) return;
+        double v1[1] = {0.0};
+        for (int i = t0; i < n; i += T) {
+            double qi = row_dot(a.A, i, a.p);
+            a.q[i] = qi;
+            v1[0] += a.p[i] * qi;
+        }
+        if (!grid_reduce<1>(v1, rc, a.gb, err)) return;
+        if (v1[0] == 0.0) { status = DEV_BREAKDOWN; break; }
+        double alpha = rho / v1[0];
+        double v2[2] = {0.0, 0.0};
+        for (int i = t0; i < n; i += T) {
+            double pi = a.p[i], qi = a.q[i];
+            a.x[i] += alpha * pi;
+            double ri = a.r[i] - alpha * qi;
+            a.r[i] = ri;
+            v2[0] += ri * ri;
+            v2[1] += ri * (dinv[i] * ri);
+        }
+        if (!grid_reduce<2>(v2, rc, a.gb, err)) return;
+        res = sqrt(v2[0]) / bnorm;
+        rho_prev = rho;
+        rho = v2[1];
+    }
+    if (status == DEV_OK && !(res < a.eps)) status = isfinite(res) ? DEV_MAXITER : DEV_NONFINITE;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.info->status[0] = status;
+        a.info->iters[0] = it;
+        a.info->res[0] = res;
+    }
+}
+
+struct BicgArgs {
+    SellView A;
+    const double *b[3];
+    double *x[3];
+    double *r, *rt, *p, *v, *s, *t;
+    const double *dinv;
+    double *partials;
+    GridBarrier *gb;
+    SolveInfo *info;
+    int maxit;
+    double eps;
+};
+
+template <int NR>
+__global__ void __launch_bounds__(KB) k_bicgstab(BicgArgs a) {
+    const int n = a.A.n;
+    const int T = gridDim.x * KB;
+    const int t0 = blockIdx.x * KB + threadIdx.x;
+    int *err = &a.info->err;
+    RedCtx rc{a.partials, (int)gridDim.x, 0};
+    const double *__restrict__ dinv = a.dinv;
+    const size_t N = (size_t)n;
+
+    double bnorm[NR], res[NR], rho[NR], rho_prev[NR], alpha[NR], omg[NR], beta[NR], snorm[NR];
+    int it[NR], status[NR];
+    bool done[NR], act[3] = {false, false, false}, early[3] = {false, false, false};
+    {
+        double v[2 * NR];
+#pragma unroll
+        for (int c = 0; c < 2 * NR; ++c) v[c] = 0.0;
+        for (int i = t0; i < n; i += T) {
+#pragma unroll
+            for (int c = 0; c < NR; ++c) {
+                double bi = a.b[c][i];
+                double ri = bi - row_dot(a.A, i, a.x[c]);
+                a.r[c * N + i] = ri;
+                a.rt[c * N + i] = ri;
+                v[c] += bi * bi;
+                v[NR + c] += ri * ri;
+            }
+        }
+        if (!grid_reduce<2 * NR>(v, rc, a.gb, err)) return;
+#pragma unroll
+        for (int c = 0; c < NR; ++c) {
+            bnorm[c] = sqrt(v[c]);
+            if (bnorm[c] == 0.0) bnorm[c] = 1.0;
+            res[c] = sqrt(v[NR + c]) / bnorm[c];
+            rho[c] = v[NR + c];
+            rho_prev[c] = alpha[c] = omg[c] = 1.0;
+            it[c] = 0;
+            status[c] = DEV_OK;
+            done[c] = false;
+        }
+    }
+    for (;;) {
+        bool any = false;
+#pragma unroll
+        for (int c = 0; c < NR; ++c) {
+            act[c] = !done[c] && !(res[c] < a.eps) && it[c] < a.maxit;
+            if (act[c] && !isfinite(res[c])) { done[c] = true; status[c] = DEV_NONFINITE; act[c] = false; }
+            if (act[c] && rho[c] == 0.0) { done[c] = true; status[c] = DEV_BREAKDOWN; act[c] = false; }
+            if (act[c]) {
+                ++it[c];
+                any = true;
+                beta[c] = (it[c] == 1) ? 0.0 : (rho[c] / rho_prev[c]) * (alpha[c] / omg[c]);
+            }
+        }
+        if (!any) break;
+        // p = r + beta (p - omega v)
+        for (int i = t0; i < n; i += T) {
+#pragma unroll
+            for (int c = 0; c < NR; ++c) {
+                if (!act[c]) continue;
+                size_t k = c * N + i;
+                a.p[k] = (it[c] == 1) ? a.r[k] : a.r[k] + beta[c] * (a.p[k] - omg[c] * a.v[k]);
+            }
+        }
+        if (!grid_sync(a.gb, err)) return;
+        // v = A M^-1 p ; rt . v
+        {
+            double red[NR];
+#pragma unroll
+            for (int c = 0; c < NR; ++c) red[c] = 0.0;
+            for (int i = t0; i < n; i += T) {
+                double y[NR];
+                row_dot_scaled<NR>(a.A, i, dinv, a.p, n, act, y);
+#pragma unroll
+                for (int c = 0; c < NR; ++c) {
+                    if (!act[c]) continue;
+                    a.v[c * N + i] = y[c];
+                    red[c] += a.rt[c * N + i] * y[c];
+                }
+            }
+            if (!grid_reduce<NR>(red, rc, a.gb, err)) return;
+#pragma unroll
+            for (int c = 0; c < NR; ++c) {
+                if (!act[c]) continue;
+                if (red[c] == 0.0) { done[c] = true; status[c] = DEV_BREAKDOWN; act[c] = false; continue; }
+                alpha[c] = rho[c] / red[c];
+            }
+        }
+        // s = r - alpha v ; ||s||
+        {
+            double red[NR];
+#pragma unroll
+            for (int c = 0; c < NR; ++c) red[c] = 0.0;
+            for (int i = t0; i < n; i += T) {
+#pragma unroll
+                for (int c = 0; c < NR; ++c) {
+                    if (!act[c]) continue;
+                    size_t k = c * N + i;
+                    double si = a.r[k] - alpha[c] * a.v[k];
+                    a.s[k] = si;
+                    red[c] += si * si;
+                }
+            }
+            if (!grid_reduce<NR>(red, rc, a.gb, err)) return;
+#pragma unroll
+            for (int c = 0; c < NR; ++c) {
+                early[c] = false;
+                if (!act[c]) continue;
+                snorm[c] = sqrt(red[c]) / bnorm[c];
+                early[c] = snorm[c] < a.eps;
+            }
+        }
+        // t = A M^-1 s ; t.s, t.t
+        {
+            bool act2[3] = {false, false, false};
+#pragma unroll
+            for (int c = 0; c < NR; ++c) act2[c] = act[c] && !early[c];
+            double red[2 * NR];
+#pragma unroll
+            for (int c = 0; c < 2 * NR; ++c) red[c] = 0.0;
+            for (int i = t0; i < n; i += T) {
+                double y[NR];
+                row_dot_scaled<NR>(a.A, i, dinv, a.s, n, act2, y);
+#pragma unroll
+                for (int c = 0; c < NR; ++c) {
+                    if (!act2[c]) continue;
+                    size_t k = c * N + i;
+                    a.t[k] = y[c];
+                    red[c] += y[c] * a.s[k];
+                    red[NR + c] += y[c] * y[c];
+                }
+            }
+            if (!grid_reduce<2 * NR>(red, rc, a.gb, err)) return;
+#pragma unroll
+            for (int c = 0; c < NR; ++c)
+                if (act2[c]) omg[c] = red[NR + c] != 0.0 ? red[c] / red[NR + c] : 0.0;
+        }
+        // x += alpha M^-1 p + omega M^-1 s ; r = s - omega t
+        {
+            double red[2 * NR];
+#pragma unroll
+            for (int c = 0; c < 2 * NR; ++c) red[c] = 0.0;
+            for (int i = t0; i < n; i += T) {
+                double di = dinv[i];
+#pragma unroll
+                for (int c = 0; c < NR; ++c) {
+                    if (!act[c]) continue;
+                    size_t k = c * N + i;
+                    double ph = di * a.p[k];
+                    if (early[c]) {
+                        a.x[c][i] += alpha[c] * ph;
+                    } else {
+                        double sh = di * a.s[k];
+                        a.x[c][i] += alpha[c] * ph + omg[c] * sh;
+                        double ri = a.s[k] - omg[c] * a.t[k];
+                        a.r[k] = ri;
+                        red[c] += ri * ri;
+                        red[NR + c] += a.rt[k] * ri;
+                    }
+                }
+            }
+            if (!grid_reduce<2 * NR>(red, rc, a.gb, err)) return;
+#pragma unroll
+            for (int c = 0; c < NR; ++c) {
+                if (!act[c]) continue;
+                if (early[c]) {
+                    res[c] = snorm[c];
+                    done[c] = true;
+                } else {
+                    res[c] = sqrt(red[c]) / bnorm[c];
+                    rho_prev[c] = rho[c];
+                    rho[c] = red[NR + c];
+                    if (omg[c] == 0.0 && !(res[c] < a.eps)) { done[c] = true; status[c] = DEV_BREAKDOWN; }
+                }
+            }
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+#pragma unroll
+        for (int c = 0; c < NR; ++c) {
+            int st = status[c];
+            if (st == DEV_OK && !(res[c] < a.eps)) st = isfinite(res[c]) ? DEV_MAXITER : DEV_NONFINITE;
+            a.info->status[c] = st;
+            a.info->iters[c] = it[c];
+            a.info->res[c] = res[c];
+        }
+    }
+}
+
+int g_num_sms = 0;
+
+int num_sms() {
+    if (!g_num_sms) {
+        int dev;
+        SYSU_CUDA(cudaGetDevice(&dev));
+        SYSU_CUDA(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
+        int coop = 0;
+        SYSU_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+        if (!coop) throw CaseError{"device does not support cooperative launch"};
+    }
+    return g_num_sms;
+}
+
+template <class K>
+int coresident_blocks(K kernel) {
+    int per_sm = 0;
+    SYSU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, KB, 0));
+    if (per_sm < 1) throw CaseError{"persistent Krylov kernel cannot be resident"};
+    return per_sm * num_sms();
+}
+
+SellView view(const SellDev &A, const double *val) {
+    return SellView{A.n, A.nslices, A.sl_ptr.get(), A.sl_w.get(), A.col.get(), val};
+}
+
+int grid_for(int n, int max_blocks) {
+    int want = (n + KB - 1) / KB;
+    return std::max(1, std::min(want, max_blocks));
+}
+
+}  // namespace
+
+int krylov_max_coresident_blocks() {
+    int m = coresident_blocks(k_cg);
+    m = std::max(m, coresident_blocks(k_bicgstab<1>));
+    m = std::max(m, coresident_blocks(k_bicgstab<3>));
+    return m;
+}
+
+void KrylovWork::ensure(int n_, int nrhs_, int max_blocks_, cudaStream_t st) {
+    if (n_ <= n && nrhs_ <= nrhs && max_blocks_ <= max_blocks) return;
+    n = std::max(n, n_);
+    nrhs = std::max(nrhs, nrhs_);
+    max_blocks = std::max(max_blocks, max_blocks_);
+    size_t m = (size_t)n * nrhs;
+    r.alloc(m); rt.alloc(m); p.alloc(m); v.alloc(m); s.alloc(m); t.alloc(m);
+    dinv.alloc(n);
+    partials.alloc((size_t)2 * NVMAX * max_blocks);
+    barrier.alloc(1);
+    barrier.zero(st);
+}
+
+void spmv(const SellDev &A, const double *val, const double *x, double *y, cudaStream_t st) {
+    if (A.n == 0) return;
+    { k_spmv<<<(A.n + KB - 1) / KB, KB, 0, st>>>(view(A, val), x, y); ++::sysu::g_launches; }
+    SYSU_CUDA(cudaGetLastError());
+}
+
+void cg_solve(const SellDev &A, const double *val, const double *b, double *x, bool x0_zero,
+              const KrylovOpts &o, KrylovWork &w, SolveInfo *info, cudaStream_t st) {
+    int n = A.n;
+    if (n == 0) return;
+    static int maxb = 0;
+    if (!maxb) maxb = coresident_blocks(k_cg);
+    w.ensure(n, 1, maxb, st);
+    SellView V = view(A, val);
+    { k_jacobi_dinv<<<(n + KB - 1) / KB, KB, 0, st>>>(V, o.omega, o.jacobi ? 1 : 0, w.dinv.get()); ++::sysu::g_launches; }
+    if (x0_zero) { k_zero<<<(n + KB - 1) / KB, KB, 0, st>>>(x, n); ++::sysu::g_launches; }
+    SYSU_CUDA(cudaMemsetAsync(info, 0, sizeof(SolveInfo), st));
+    CgArgs a{V, b, x, w.r.get(), w.p.get(), w.v.get(), w.dinv.get(), w.partials.get(), w.barrier.get(), info,
+             o.maxit, o.eps};
+    void *args[] = {&a};
+    int G = grid_for(n, maxb);
+    { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_cg, dim3(G), dim3(KB), args, 0, st)); ++::sysu::g_launches; }
+}
+
+void bicgstab_solve(const SellDev &A, const double *val, int nrhs, const double *const *b, double *const *x,
+                    const KrylovOpts &o, KrylovWork &w, SolveInfo *info, cudaStream_t st) {
+    int n = A.n;
+    if (n == 0) return;
+    if (nrhs < 1 || nrhs > 3) throw CaseError{"bicgstab_solve: 1..3 right-hand sides"};
+    static int maxb1 = 0, maxb3 = 0;
+    if (!maxb1) {
+        maxb1 = coresident_blocks(k_bicgstab<1>);
+        maxb3 = coresident_blocks(k_bicgstab<3>);
+    }
+    int maxb = (nrhs == 1) ? maxb1 : maxb3;
+    w.ensure(n, nrhs == 1 ? 1 : 3, std::max(maxb1, maxb3), st);
+    SellView V = view(A, val);
+    { k_jacobi_dinv<<<(n + KB - 1) / KB, KB, 0, st>>>(V, o.omega, o.jacobi ? 1 : 0, w.dinv.get()); ++::sysu::g_launches; }
+    SYSU_CUDA(cudaMemsetAsync(info, 0, sizeof(SolveInfo), st));
+    BicgArgs a{};
+    a.A = V;
+    for (int c = 0; c < 3; ++c) {
+        a.b[c] = b[std::min(c, nrhs - 1)];
+        a.x[c] = x[std::min(c, nrhs - 1)];
+    }
+    a.r = w.r.get(); a.rt = w.rt.get(); a.p = w.p.get(); a.v = w.v.get(); a.s = w.s.get(); a.t = w.t.get();
+    a.dinv = w.dinv.get();
+    a.partials = w.partials.get();
+    a.gb = w.barrier.get();
+    a.info = info;
+    a.maxit = o.maxit;
+    a.eps = o.eps;
+    void *args[] = {&a};
+    int G = grid_for(n, maxb);
+    if (nrhs == 1)
+        { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_bicgstab<1>, dim3(G), dim3(KB), args, 0, st)); ++::sysu::g_launches; }
+    else if (nrhs == 2)
+        throw CaseError{"bicgstab_solve: use 1 or 3 right-hand sides"};
+    else
+        { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_bicgstab<3>, dim3(G), dim3(KB), args, 0, st)); ++::sysu::g_launches; }
+}
+
+}  // namespace sysu

@@ -1,0 +1,86 @@
+// Sparse matrices and Krylov solvers on the GPU.
+//
+// Storage is SELL-32: rows are grouped in slices of 32 (one warp), each slice
+// padded to its longest row and stored column-major, so that the 32 lanes of a
+// warp read consecutive values and column indices.  Entry k = 0 of every row
+// is its diagonal; the remaining entries follow in the order the assembly
+// kernels write them.  Padding entries point at the row itself with value 0.
+//
+// The solvers replace LASPack's CGIter / BiCGSTABIter as called through
+// SolveLinearEqu (tools.cpp:56-64): same stopping test ||b-Ax||/||b|| < eps on
+// the unpreconditioned residual recurrence, same iteration cap, Jacobi
+// preconditioner y = omega D^-1 c.  Each solve is one cooperative launch of a
+// persistent kernel; iteration counts and residuals stay on the device.
+#pragma once
+
+#include <vector>
+
+#include "device.hpp"
+
+namespace sysu {
+
+struct SellPattern {
+    int n = 0, nslices = 0;
+    long nnz = 0;      // stored entries including padding
+    long nnz_true = 0; // entries excluding padding
+    std::vector<int> sl_ptr, sl_w, col;
+    // row_len[i] = number of true entries of row i
+    std::vector<int> row_len;
+    // position of (row, k) in the value array
+    long pos(int row, int k) const { return (long)sl_ptr[row >> 5] + (long)k * 32 + (row & 31); }
+};
+
+// Build a SELL-32 pattern from per-row column lists (diagonal first).
+SellPattern make_sell(int n, const std::vector<int> &row_ptr, const std::vector<int> &cols);
+
+struct SellDev {
+    int n = 0, nslices = 0;
+    long nnz = 0, nnz_true = 0;
+    DevBuf<int> sl_ptr, sl_w, col;
+    void upload(const SellPattern &p, cudaStream_t s);
+};
+
+// View passed to kernels.
+struct SellView {
+    int n, nslices;
+    const int *sl_ptr, *sl_w, *col;
+    const double *val;
+};
+
+struct SolveInfo {
+    int status[3];
+    int iters[3];
+    double res[3];
+    int err;
+    int pad;
+};
+
+// Scratch of the persistent solvers, sized for n rows and up to 3 RHS.
+struct KrylovWork {
+    int n = 0, nrhs = 0, max_blocks = 0;
+    DevBuf<double> r, rt, p, v, s, t, dinv, partials;
+    DevBuf<GridBarrier> barrier;
+    void ensure(int n, int nrhs, int max_blocks, cudaStream_t st);
+};
+
+struct KrylovOpts {
+    int maxit = 500;
+    double eps = 1e-8;
+    double omega = 1.0;       // Jacobi weight (the omega LASPack's precond gets)
+    bool jacobi = true;       // false: no preconditioner
+};
+
+int krylov_max_coresident_blocks();
+
+// Jacobi-preconditioned CG; x holds x0 on entry (or is zeroed first if x0_zero).
+void cg_solve(const SellDev &A, const double *val, const double *b, double *x, bool x0_zero,
+              const KrylovOpts &o, KrylovWork &w, SolveInfo *info_dev, cudaStream_t st);
+
+// BiCGSTAB on nrhs (1..3) right-hand sides sharing one matrix; b[c], x[c].
+void bicgstab_solve(const SellDev &A, const double *val, int nrhs, const double *const *b, double *const *x,
+                    const KrylovOpts &o, KrylovWork &w, SolveInfo *info_dev, cudaStream_t st);
+
+// y = A x (standalone, for tests and the SpMV sweep).
+void spmv(const SellDev &A, const double *val, const double *x, double *y, cudaStream_t st);
+
+}  // namespace sysu

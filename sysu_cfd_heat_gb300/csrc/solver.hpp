@@ -1,0 +1,128 @@
+// The GPU SIMPLE solver: one fluid domain (and optionally one solid domain for
+// conjugate heat transfer) resident in device memory, advanced one outer
+// iteration at a time in the order of NavierStokesSolver::NSSolve
+// (navier.cpp:27-76).
+#pragma once
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "fv.hpp"
+
+namespace sysu {
+
+// Device copy of a Domain plus its matrix pattern.
+struct DomainDev {
+    DomView view{};
+    int nc = 0, nf = 0, F = 0, B = 0, ncb = 0, nv = 0;
+    bool has_outlet = false;
+    std::vector<int> int2ref;  // internal face id -> reference face id
+    std::vector<int> ref2int;
+    SellPattern pat;
+    SellDev A;
+    DevBuf<double> vol, cx, fn, farea, flam, frl, fx, fxpac, fxnac, bdist, bquirk, bin, bfixed, vx;
+    DevBuf<int> cs_ptr, cs_face, cs_k, fc1, fc2, bcell, btype1, btype2, brid, cw_ptr, cw_b, cvert, vc_ptr, vc_cell;
+    std::vector<int> h_btype1, h_btype2, h_bcell;
+    void build(const Domain &d, const Params &p, cudaStream_t st);
+};
+
+// Solver choice per equation (the reference hard-codes them per call site).
+enum SolverKind { SK_CG = 0, SK_BICGSTAB = 1 };
+
+struct EqOpts {
+    int kind = SK_BICGSTAB;
+    int maxit = 500;
+    double eps = 1e-8;
+    double omega = 1.2;
+};
+
+struct SolverOptions {
+    // defaults: the reference's call sites (navier_velocity.cpp:26,
+    // navier_pressure.cpp:29, navier_scalar.cpp:101,143,374,
+    // HeatConductionSolver.cpp:90), with GMRES+SSOR running as
+    // BiCGSTAB+Jacobi and CG+SSOR as CG+Jacobi
+    EqOpts mom{SK_BICGSTAB, 500, 1e-8, 1.2};
+    EqOpts p{SK_CG, 1000, 1e-6, 1.3};
+    EqOpts ke{SK_BICGSTAB, 500, 1e-8, 1.3};
+    EqOpts t{SK_BICGSTAB, 500, 1e-8, 1.3};
+    EqOpts ts{SK_CG, 500, 1e-8, 1.3};
+    bool mom_batched = true;      // u, v, w as one 3-RHS solve
+    double solid_source = 0.0;    // W/m^3 (extension; the reference has none)
+    bool fatal_checks = true;     // the reference's convergence checks
+    bool timing = false;          // CUDA events around the p' solve
+};
+
+enum SolveSlot { SLOT_MOM = 0, SLOT_P, SLOT_K, SLOT_EPS, SLOT_T, SLOT_TS, SLOT_N };
+
+struct FieldSet {
+    DevBuf<double> U, V, W, P, R, T, TE, ED, VisLam, VisTur, Apr;
+    DevBuf<double> dU, dV, dW, dP, dPhi;
+    DevBuf<double> RUFace;
+    DevBuf<double> BRo, BU, BV, BW, BPre, BTem, BTE, BED, Bq;
+    DevBuf<double> Amom, Ap, As;
+    DevBuf<double> b3, bp, bs, x3, xp, xs;
+    DevBuf<double> fD, fE, fcoef, bapp, bsrc;
+    DevBuf<double> Prod, TESrc, EDSrc, VisTE, VisED, ApTE, ApED, kcond, zeros, src;
+    DevBuf<double> tmp3, tmpv;
+    DevBuf<double> diff;  // solid conductivity
+};
+
+class SimpleSolver {
+  public:
+    explicit SimpleSolver(const std::string &param_path);
+    ~SimpleSolver();
+
+    Case cs;
+    SolverOptions opt;
+    cudaStream_t st = nullptr;
+    DomainDev fd, sd;
+    FieldSet f, s;
+    KrylovWork kw;
+    DevBuf<SolveInfo> infos;
+    DevBuf<double> red_partials, red_out;
+    DevBuf<unsigned int> red_ticket;
+    DevBuf<int> flags;
+    RedScratch rs{};
+    int red_blocks = 0;
+
+    double Residual[10] = {0};
+    int iter_done = 0;
+    SolveInfo last_info[SLOT_N]{};
+    double last_p_ms = 0.0;       // CUDA-event time of the last p' solve (opt.timing)
+    double last_mom_ms = 0.0;
+    cudaEvent_t ev[6]{};
+
+    // NavierStokesSolver::InitFlowField (navier.cpp:113-188) + solid module init
+    void init_flow_field();
+    // pieces of one outer iteration (enqueued on st, no host sync)
+    void calculate_velocity();
+    void calculate_pressure();
+    void update_ke();
+    void update_energy();
+    void solid_solve();
+    // one NSSolve loop body; syncs once, updates Residual and the solve infos,
+    // returns a non-empty message when a reference convergence check fails
+    std::string outer_iteration();
+    std::string check_iteration();  // read back infos + residuals (one sync)
+    // field I/O by reference name (host buffers, reference ordering)
+    long field_size(const std::string &name) const;
+    void get_field(const std::string &name, double *out, long n);
+    void set_field(const std::string &name, const double *in, long n);
+    void sync();
+    // back to the state after InitFlowField (fields, residuals, counters)
+    void reset();
+    // CUDA events on the solver's stream around a region of work
+    void timer_start();
+    double timer_stop();  // ms; synchronises
+
+  private:
+    void alloc_fields(FieldSet &fs, const DomainDev &d, bool solid);
+    void solve(int slot, const EqOpts &o, const SellDev &A, const double *val, int nrhs, const double *const *b,
+               double *const *x, bool x0_zero);
+    void grad_limited(DomainDev &d, FieldSet &fs, int nfield, const double *const *phi, const double *const *Bphi,
+                      double *const *grad);
+    DevBuf<double> *field_ptr(const std::string &name, int &kind, bool &solid);
+};
+
+}  // namespace sysu
