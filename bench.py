@@ -197,7 +197,9 @@ def config_of(args):
     return {"workload": f"lid-driven cavity Re 400, {nx}x{ny}x{nz} hexes x 6 jittered tets "
                         f"({6 * nx * ny * nz} cells), seed {SEED}",
             "cells": 6 * nx * ny * nz, "solvers": "momentum 3-RHS BiCGSTAB+Jacobi, p' Jacobi-CG, rtol 1e-8",
-            "precision": "fp64", "l2": "inputs larger than L2 (mesh, fields and matrices > 129 MB)",
+            "precision": "fp64",
+            "l2": ("inputs larger than L2 (mesh, fields and matrices > 129 MB)" if nx * ny * nz * 6 > 1000000
+                   else "small case: resident in L2 (development runs only)"),
             "parallelism": "replicas"}
 
 
@@ -212,8 +214,9 @@ def run_ours(args, r, w, lr):
         dist.barrier()
         param = case_dir(args.workload)
     L = _lib.lib()
-    L.sysu_kernel_launches.restype = __import__("ctypes").c_long
     s = NavierStokesSolver(param, {"rtc": RTC, "timing": 1})
+    if args.p_maxit:
+        s.set_option("p.maxit", args.p_maxit)
     info = s.info()
     n, nnz = info["Ncel"], info["nnz"]
     # warm-up, then back to the initial state so the timed iterations are iterations 1..K
@@ -226,16 +229,12 @@ def run_ours(args, r, w, lr):
     l0 = L.sysu_kernel_launches()
     s_ms = 0.0
     p_ms, cg_it, mom_it = [], [], []
-    import ctypes as C
-
     for k in range(args.steps):
-        C.c_int()
-        _lib.check(L.sysu_solver_timer_start(s._h))
+        s.timer_start()
         done = s.iterate(1)
-        ms = C.c_double()
-        _lib.check(L.sysu_solver_timer_stop(s._h, C.byref(ms)))
+        ms = s.timer_stop()
         assert done == 1
-        s_ms += ms.value
+        s_ms += ms
         pm, _ = s.timing()
         st = s.solve_stats()
         p_ms.append(pm)
@@ -255,10 +254,10 @@ def run_ours(args, r, w, lr):
 
     # end to end through the C ABI with host buffers
     s.reset()
-    nf = s.field_size("RUFace")
-    host = {f: s.get(f) for f in ("U", "V", "W", "P", "RUFace")}
+    state = ("U", "V", "W", "P", "RUFace")
+    host = {f: s.get(f) for f in state}
     h2d = sum(a.nbytes for a in host.values())
-    d2h = 4 * n * 8
+    d2h = h2d
     if w > 1:
         dist.barrier()
     t0 = time.perf_counter()
@@ -266,9 +265,8 @@ def run_ours(args, r, w, lr):
         for f, a in host.items():
             s.set(f, a)
         s.iterate(1)
-        for f in ("U", "V", "W", "P"):
+        for f in state:
             host[f] = s.get(f)
-        host["RUFace"] = s.get("RUFace") if k < 0 else host["RUFace"]
     e2e_s = time.perf_counter() - t0
     if w > 1:
         import torch
@@ -339,6 +337,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=240.0)
     ap.add_argument("--ref-budget", type=float, default=150.0)
+    ap.add_argument("--p-maxit", type=int, default=0,
+                    help="cap the p' CG iterations (short profiling runs only; not a bench setting)")
     args = ap.parse_args()
     r, w, lr = rank_info()
     if w > 1:

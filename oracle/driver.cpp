@@ -26,6 +26,18 @@
 
 ErrorHandler *errorHandler;  // defined by the reference's main.cpp, which is not linked
 
+#ifdef SYSU_GPU_LASPACK
+// linked against the GPU LASPack ABI: no per-iterator timing statistics there
+struct LaspackOracleStats {
+    long calls[3];
+    long iters[3];
+    double seconds[3];
+};
+static LaspackOracleStats g_nostats;
+static void laspack_oracle_reset_stats() {}
+static const LaspackOracleStats *laspack_oracle_stats() { return &g_nostats; }
+#endif
+
 namespace {
 
 std::string g_dump;

@@ -59,7 +59,10 @@ class Params:
 def parse_params(path: str) -> Params:
     p = Params()
     raw = open(path, "rb").read().decode()
-    for line in raw.split("\n"):
+    lines = raw.split("\n")
+    if lines and lines[-1] == "":  # std::getline yields no line after a final newline
+        lines.pop()
+    for line in lines:
         if line.startswith("//") or len(line) == 1:
             continue
         kw = [t.strip() for t in line.split(",")]
@@ -391,6 +394,7 @@ class Domain:
         self.m = m
         self.g = geometry(m)
         self.nc, self.nf, self.nb = len(m.cells), len(m.c1), len(m.bface)
+        self.ncb = m.ncb
         self.inner = np.where(m.c2 >= 0)[0]
         self.bc1 = m.c1[m.bface]
         self.t1 = np.array([p.regions[r].type1 for r in m.brid])

@@ -57,6 +57,15 @@ def lib() -> C.CDLL:
             "sysu_solver_get_field": (C.c_int, [vp, cp, dp, C.c_long]),
             "sysu_solver_set_field": (C.c_int, [vp, cp, dp, C.c_long]),
             "sysu_solver_sync": (C.c_int, [vp]),
+            "sysu_solver_reset": (C.c_int, [vp]),
+            "sysu_solver_timer_start": (C.c_int, [vp]),
+            "sysu_solver_timer_stop": (C.c_int, [vp, dp]),
+            "sysu_kernel_launches": (C.c_long, []),
+            "sysu_solver_matrix": (C.c_long, [vp, cp, vp, vp, vp]),
+            "sysu_csr_solve": (C.c_int, [C.c_int, C.c_int, C.c_int, ip, ip, dp, dp, dp, C.c_int, C.c_double,
+                                         C.c_double, ip, dp, ip]),
+            "sysu_csr_spmv": (C.c_int, [C.c_int, ip, ip, dp, dp, dp]),
+            "sysu_csr_last_error": (cp, []),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)

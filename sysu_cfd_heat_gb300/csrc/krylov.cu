@@ -151,6 +151,13 @@ __global__ void k_spmv(SellView A, const double *__restrict__ x, double *__restr
     y[i] = row_dot(A, i, x);
 }
 
+__global__ void k_jacobi_apply(SellView A, double omega, const double *c, double *y) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.n) return;
+    double d = A.val[A.sl_ptr[i >> 5] + (i & 31)];
+    y[i] = omega * c[i] / d;
+}
+
 __global__ void k_zero(double *x, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) x[i] = 0.0;
@@ -490,6 +497,12 @@ void KrylovWork::ensure(int n_, int nrhs_, int max_blocks_, cudaStream_t st) {
 void spmv(const SellDev &A, const double *val, const double *x, double *y, cudaStream_t st) {
     if (A.n == 0) return;
     { k_spmv<<<(A.n + KB - 1) / KB, KB, 0, st>>>(view(A, val), x, y); ++::sysu::g_launches; }
+    SYSU_CUDA(cudaGetLastError());
+}
+
+void jacobi_apply(const SellDev &A, const double *val, double omega, const double *c, double *y, cudaStream_t st) {
+    if (A.n == 0) return;
+    { k_jacobi_apply<<<(A.n + KB - 1) / KB, KB, 0, st>>>(view(A, val), omega, c, y); ++::sysu::g_launches; }
     SYSU_CUDA(cudaGetLastError());
 }
 

@@ -83,4 +83,7 @@ void bicgstab_solve(const SellDev &A, const double *val, int nrhs, const double 
 // y = A x (standalone, for tests and the SpMV sweep).
 void spmv(const SellDev &A, const double *val, const double *x, double *y, cudaStream_t st);
 
+// y = omega D^-1 c (the Jacobi preconditioner applied once).
+void jacobi_apply(const SellDev &A, const double *val, double omega, const double *c, double *y, cudaStream_t st);
+
 }  // namespace sysu

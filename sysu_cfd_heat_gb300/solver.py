@@ -105,6 +105,19 @@ class NavierStokesSolver:
     def sync(self) -> None:
         check(lib().sysu_solver_sync(self._h))
 
+    def reset(self) -> None:
+        """Back to the state right after creation (InitFlowField)."""
+        check(lib().sysu_solver_reset(self._h))
+
+    def timer_start(self) -> None:
+        check(lib().sysu_solver_timer_start(self._h))
+
+    def timer_stop(self) -> float:
+        """Device time (ms) on the solver's stream since timer_start()."""
+        ms = C.c_double()
+        check(lib().sysu_solver_timer_stop(self._h, C.byref(ms)))
+        return ms.value
+
     @property
     def Residual(self) -> np.ndarray:
         out = np.zeros(10)
