@@ -239,6 +239,137 @@ __global__ void __launch_bounds__(KB) k_cg(CgArgs a) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Mixed precision: FP32 inner Jacobi-CG inside FP64 defect correction.
+__device__ __forceinline__ float row_dot32(const SellView &A, const float *__restrict__ val32, int i,
+                                           const float *__restrict__ x) {
+    int s = i >> 5;
+    int e = A.sl_ptr[s] + (i & 31);
+    int w = A.sl_w[s];
+    float acc = 0.f;
+    for (int k = 0; k < w; ++k, e += 32) acc = fmaf(val32[e], x[A.col[e]], acc);
+    return acc;
+}
+
+struct CgMixedArgs {
+    SellView A;  // FP64 values
+    const float *val32;
+    const double *b;
+    double *x, *r64;
+    float *r32, *p32, *q32, *e32;
+    const float *dinv32;
+    double *partials;
+    GridBarrier *gb;
+    SolveInfo *info;
+    int maxit, max_refine;
+    double eps, inner_tol;
+};
+
+__global__ void __launch_bounds__(KB) k_cg_mixed(CgMixedArgs a) {
+    const int n = a.A.n;
+    const int T = gridDim.x * KB;
+    const int t0 = blockIdx.x * KB + threadIdx.x;
+    int *err = &a.info->err;
+    RedCtx rc{a.partials, (int)gridDim.x, 0};
+    const float *__restrict__ dinv = a.dinv32;
+
+    // FP64 residual of the initial guess
+    double v2[2] = {0.0, 0.0};
+    for (int i = t0; i < n; i += T) {
+        double bi = a.b[i];
+        double ri = bi - row_dot(a.A, i, a.x);
+        a.r64[i] = ri;
+        v2[0] += bi * bi;
+        v2[1] += ri * ri;
+    }
+    if (!grid_reduce<2>(v2, rc, a.gb, err)) return;
+    double bnorm = sqrt(v2[0]);
+    if (bnorm == 0.0) bnorm = 1.0;
+    double res = sqrt(v2[1]) / bnorm;
+    int total = 0, nref = 0, status = DEV_OK;
+    while (!(res < a.eps) && total < a.maxit && nref < a.max_refine) {
+        if (!isfinite(res)) { status = DEV_NONFINITE; break; }
+        ++nref;
+        // inner solve A32 e = r, e0 = 0.  Per-thread partial sums in FP32 over a
+        // few rows, FP64 across threads and blocks.
+        float f0 = 0.f, f1 = 0.f;
+        for (int i = t0; i < n; i += T) {
+            float ri = (float)a.r64[i];
+            a.r32[i] = ri;
+            a.e32[i] = 0.f;
+            f0 = fmaf(ri, dinv[i] * ri, f0);
+            f1 = fmaf(ri, ri, f1);
+        }
+        double v[2] = {(double)f0, (double)f1};
+        if (!grid_reduce<2>(v, rc, a.gb, err)) return;
+        double rho = v[0], rho_prev = 1.0;
+        const double tol2 = a.inner_tol * a.inner_tol * v[1];
+        int it = 0;
+        while (total < a.maxit) {
+            ++it;
+            ++total;
+            float beta = (it == 1) ? 0.f : (float)(rho / rho_prev);
+            for (int i = t0; i < n; i += T) {
+                float z = dinv[i] * a.r32[i];
+                a.p32[i] = (it == 1) ? z : fmaf(beta, a.p32[i], z);
+            }
+            if (!grid_sync(a.gb, err)) return;
+            float g0 = 0.f;
+            for (int i = t0; i < n; i += T) {
+                float qi = row_dot32(a.A, a.val32, i, a.p32);
+                a.q32[i] = qi;
+                g0 = fmaf(a.p32[i], qi, g0);
+            }
+            double v1[1] = {(double)g0};
+            if (!grid_reduce<1>(v1, rc, a.gb, err)) return;
+            if (v1[0] == 0.0) break;
+            float alpha = (float)(rho / v1[0]);
+            float h0 = 0.f, h1 = 0.f;
+            for (int i = t0; i < n; i += T) {
+                a.e32[i] = fmaf(alpha, a.p32[i], a.e32[i]);
+                float ri = fmaf(-alpha, a.q32[i], a.r32[i]);
+                a.r32[i] = ri;
+                h0 = fmaf(ri, ri, h0);
+                h1 = fmaf(ri, dinv[i] * ri, h1);
+            }
+            double w2[2] = {(double)h0, (double)h1};
+            if (!grid_reduce<2>(w2, rc, a.gb, err)) return;
+            rho_prev = rho;
+            rho = w2[1];
+            if (w2[0] <= tol2 || !(rho == rho)) break;
+        }
+        // FP64 correction and true residual
+        for (int i = t0; i < n; i += T) a.x[i] += (double)a.e32[i];
+        if (!grid_sync(a.gb, err)) return;
+        double v1[1] = {0.0};
+        for (int i = t0; i < n; i += T) {
+            double ri = a.b[i] - row_dot(a.A, i, a.x);
+            a.r64[i] = ri;
+            v1[0] += ri * ri;
+        }
+        if (!grid_reduce<1>(v1, rc, a.gb, err)) return;
+        res = sqrt(v1[0]) / bnorm;
+    }
+    if (status == DEV_OK && !(res < a.eps)) status = isfinite(res) ? DEV_MAXITER : DEV_NONFINITE;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.info->status[0] = status;
+        a.info->iters[0] = total;
+        a.info->res[0] = res;
+        a.info->refinements = nref;
+    }
+}
+
+__global__ void k_to_fp32(long n, const double *src, float *dst) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = (float)src[i];
+}
+
+__global__ void k_dinv32(SellView A, double omega, float *dinv) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.n) return;
+    dinv[i] = (float)(omega / A.val[A.sl_ptr[i >> 5] + (i & 31)]);
+}
+
 struct BicgArgs {
     SellView A;
     const double *b[3];
@@ -492,6 +623,50 @@ void KrylovWork::ensure(int n_, int nrhs_, int max_blocks_, cudaStream_t st) {
     partials.alloc((size_t)2 * NVMAX * max_blocks);
     barrier.alloc(1);
     barrier.zero(st);
+}
+
+void KrylovWork::ensure32(int n_, cudaStream_t st) {
+    if (r32.size() >= (size_t)n_) return;
+    r32.alloc(n_); p32.alloc(n_); q32.alloc(n_); e32.alloc(n_); dinv32.alloc(n_);
+    (void)st;
+}
+
+void sell_to_fp32(const SellDev &A, const double *val, float *val32, cudaStream_t st) {
+    if (A.nnz == 0) return;
+    { k_to_fp32<<<(unsigned)((A.nnz + KB - 1) / KB), KB, 0, st>>>(A.nnz, val, val32); ++::sysu::g_launches; }
+    SYSU_CUDA(cudaGetLastError());
+}
+
+void cg_solve_mixed(const SellDev &A, const double *val, const float *val32, const double *b, double *x,
+                    bool x0_zero, const KrylovOpts &o, KrylovWork &w, SolveInfo *info, cudaStream_t st) {
+    int n = A.n;
+    if (n == 0) return;
+    static int maxb = 0;
+    if (!maxb) maxb = coresident_blocks(k_cg_mixed);
+    w.ensure(n, 1, maxb, st);
+    w.ensure32(n, st);
+    SellView V = view(A, val);
+    { k_dinv32<<<(n + KB - 1) / KB, KB, 0, st>>>(V, o.omega, w.dinv32.get()); ++::sysu::g_launches; }
+    if (x0_zero) { k_zero<<<(n + KB - 1) / KB, KB, 0, st>>>(x, n); ++::sysu::g_launches; }
+    SYSU_CUDA(cudaMemsetAsync(info, 0, sizeof(SolveInfo), st));
+    CgMixedArgs a{};
+    a.A = V;
+    a.val32 = val32;
+    a.b = b;
+    a.x = x;
+    a.r64 = w.r.get();
+    a.r32 = w.r32.get(); a.p32 = w.p32.get(); a.q32 = w.q32.get(); a.e32 = w.e32.get();
+    a.dinv32 = w.dinv32.get();
+    a.partials = w.partials.get();
+    a.gb = w.barrier.get();
+    a.info = info;
+    a.maxit = o.maxit;
+    a.max_refine = o.max_refine;
+    a.eps = o.eps;
+    a.inner_tol = o.inner_tol;
+    void *args[] = {&a};
+    int G = grid_for(n, maxb);
+    { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_cg_mixed, dim3(G), dim3(KB), args, 0, st)); ++::sysu::g_launches; }
 }
 
 void spmv(const SellDev &A, const double *val, const double *x, double *y, cudaStream_t st) {

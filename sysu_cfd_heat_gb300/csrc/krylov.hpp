@@ -52,15 +52,17 @@ struct SolveInfo {
     int iters[3];
     double res[3];
     int err;
-    int pad;
+    int refinements;  // mixed precision: FP64 defect-correction sweeps
 };
 
 // Scratch of the persistent solvers, sized for n rows and up to 3 RHS.
 struct KrylovWork {
     int n = 0, nrhs = 0, max_blocks = 0;
     DevBuf<double> r, rt, p, v, s, t, dinv, partials;
+    DevBuf<float> r32, p32, q32, e32, dinv32;  // mixed-precision inner solve
     DevBuf<GridBarrier> barrier;
     void ensure(int n, int nrhs, int max_blocks, cudaStream_t st);
+    void ensure32(int n, cudaStream_t st);
 };
 
 struct KrylovOpts {
@@ -68,7 +70,19 @@ struct KrylovOpts {
     double eps = 1e-8;
     double omega = 1.0;       // Jacobi weight (the omega LASPack's precond gets)
     bool jacobi = true;       // false: no preconditioner
+    double inner_tol = 1e-4;  // mixed precision: relative reduction per FP32 inner solve
+    int max_refine = 50;      // mixed precision: FP64 defect-correction sweeps
 };
+
+// Copy FP64 SELL values to FP32 (same pattern).
+void sell_to_fp32(const SellDev &A, const double *val, float *val32, cudaStream_t st);
+
+// Mixed precision CG: FP64 defect correction (r = b - A x in FP64, x += e in
+// FP64) around FP32 Jacobi-CG inner solves A e = r of relative tolerance
+// inner_tol; inner dot products are summed in FP64 across threads.  Stops on
+// the FP64 residual ||b - A x|| / ||b|| < eps; iters = total inner iterations.
+void cg_solve_mixed(const SellDev &A, const double *val, const float *val32, const double *b, double *x,
+                    bool x0_zero, const KrylovOpts &o, KrylovWork &w, SolveInfo *info_dev, cudaStream_t st);
 
 int krylov_max_coresident_blocks();
 
