@@ -126,6 +126,28 @@ int sysu_csr_solve(int method, int precond, int n, const int *rowptr, const int 
 int sysu_csr_spmv(int n, const int *rowptr, const int *col, const double *val, const double *x, double *y);
 const char *sysu_csr_last_error(void);
 
+/* ---- Jacobi-CG that allocates nothing ----------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc:
+ * applications that own all device memory through their own pool and do not
+ * let a library allocate behind their back, or loops that must not pay the
+ * device-wide synchronisation of cudaMalloc/cudaFree.  The caller passes its
+ * own DEVICE buffers: CSR d_rowptr[n+1], d_col[nnz], d_val[nnz] (0-based), d_b[n],
+ * d_x[n] (x0 in, solution out); same algorithm and stopping test as
+ * sysu_csr_solve with method CG and precond Jacobi.  Scratch is one static
+ * device array of 8.4 MB, present on every GPU that loads the library:
+ *   - n must be <= SYSU_NOALLOC_MAX_ROWS, larger systems are rejected
+ *     (SYSU_ERR_INPUT, message in sysu_noalloc_last_error());
+ *   - every call shares the array; calls that overlap on the GPU race on it;
+ *   - the first call on a device looks up the array's address with that device
+ *     current -- make it before any stream capture.
+ * stream: a cudaStream_t (NULL = default stream); the call waits for the
+ * stream to read iters / res / status back. */
+#define SYSU_NOALLOC_MAX_ROWS 262144
+int sysu_csr_cg_noalloc(int n, const int *d_rowptr, const int *d_col, const double *d_val, const double *d_b,
+                        double *d_x, int maxit, double eps, double omega, void *stream, int *iters, double *res,
+                        int *status);
+const char *sysu_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif
