@@ -217,6 +217,8 @@ def run_ours(args, r, w, lr):
     s = NavierStokesSolver(param, {"rtc": RTC, "timing": 1})
     if args.p_maxit:
         s.set_option("p.maxit", args.p_maxit)
+    if args.p_mixed:
+        s.set_option("p.mixed", 1)
     info = s.info()
     n, nnz = info["Ncel"], info["nnz"]
     # warm-up, then back to the initial state so the timed iterations are iterations 1..K
@@ -290,11 +292,44 @@ def run_ours(args, r, w, lr):
     achieved = statistics.mean(ach) if ach else None
     traffic = None
     tp = os.path.join(ROOT, "profiles", "cg_pressure_traffic.json")
-    if os.path.exists(tp):
+    if args.workload == "c3" and not args.p_mixed and os.path.exists(tp):
         tj = json.load(open(tp))
         per_iter = tj.get("dram_bytes_per_cg_iteration_scaled_to_c3")
         if per_iter:
             traffic = per_iter * statistics.mean(cg_it)
+
+    # the mixed-precision form (FP32 inner CG in FP64 defect correction) on the same iterations
+    forms = {"fp64": {"iters_per_s": value, "ms_per_step": t_max / args.steps,
+                      "p_solve_ms_mean": statistics.mean(p_ms), "p_cg_iters_mean": statistics.mean(cg_it)}}
+    if not args.p_maxit and not args.p_mixed:
+        s.set_option("p.mixed", 1)
+        s.reset()
+        m_ms, m_p, m_it = 0.0, [], []
+        for k in range(args.steps):
+            s.timer_start()
+            s.iterate(1)
+            m_ms += s.timer_stop()
+            m_p.append(s.timing()[0])
+            m_it.append(s.solve_stats()["p"]["iters"][0])
+        forms["mixed_fp32_fp64"] = {"iters_per_s": args.steps / (m_ms / 1000.0), "ms_per_step": m_ms / args.steps,
+                                    "p_solve_ms_mean": statistics.mean(m_p),
+                                    "p_cg_inner_iters_mean": statistics.mean(m_it)}
+        s.set_option("p.mixed", 0)
+        # p' solve of outer iteration 1 to the 1e-8 relative residual, without the 1000 cap
+        to8 = {}
+        for name, mixed in (("fp64", 0), ("mixed_fp32_fp64", 1)):
+            s.set_option("p.mixed", mixed)
+            s.set_option("p.maxit", 100000)
+            s.reset()
+            s.CalculateVelocity()
+            s.CalculatePressure()
+            s.check()
+            st = s.solve_stats()["p"]
+            to8[name] = {"ms": s.timing()[0], "iters": st["iters"][0], "rel_residual": st["res"][0],
+                         "converged": st["status"][0] == 0}
+        s.set_option("p.mixed", 0)
+        s.set_option("p.maxit", 1000)
+        forms["p_solve_to_1e-8_outer_iteration_1"] = to8
 
     out = {
         "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": w, "steps": args.steps,
@@ -309,7 +344,7 @@ def run_ours(args, r, w, lr):
                      "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
                      "algorithmic_bytes_per_cg_iteration": b_iter},
         "p_solve_ms_mean": statistics.mean(p_ms), "p_cg_iters_mean": statistics.mean(cg_it),
-        "mom_bicgstab_iters": mom_it[-1], "clocks": clocks,
+        "mom_bicgstab_iters": mom_it[-1], "clocks": clocks, "forms": forms,
     }
     s.close()
     if r == 0 and w == 1 and not args.no_cpu_baseline:
@@ -339,6 +374,8 @@ def main():
     ap.add_argument("--ref-budget", type=float, default=150.0)
     ap.add_argument("--p-maxit", type=int, default=0,
                     help="cap the p' CG iterations (short profiling runs only; not a bench setting)")
+    ap.add_argument("--p-mixed", action="store_true",
+                    help="time the mixed-precision p' form as the main form (profiling runs)")
     args = ap.parse_args()
     r, w, lr = rank_info()
     if w > 1:

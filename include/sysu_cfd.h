@@ -60,6 +60,8 @@ int sysu_solver_info(sysu_solver *s, long *out, int n);
 /* Options (defaults = the reference's call sites):
  *   "<eq>.eps" "<eq>.maxit" "<eq>.omega" "<eq>.kind" (0 CG, 1 BiCGSTAB)
  *     for eq in mom, p, ke, t, ts (solid T);
+ *   "<eq>.mixed" (CG equations p, ts: FP32 inner CG in FP64 defect
+ *     correction, stopping on the FP64 residual) and "<eq>.inner_tol";
  *   "rtc" sets every eq's eps; "mom_batched" (1: u,v,w as one 3-RHS solve);
  *   "solid_source" (W/m^3, an extension); "fatal_checks"; "timing". */
 int sysu_solver_set_option(sysu_solver *s, const char *key, double value);
@@ -89,6 +91,11 @@ int sysu_solver_timer_start(sysu_solver *s);
 int sysu_solver_timer_stop(sysu_solver *s, double *ms);
 /* Number of kernels the library has launched so far (all solvers). */
 long sysu_kernel_launches(void);
+/* With option "profile_phases" on: %globaltimer stamps (ns) taken by block 0
+ * of the last CG solve at the start of each iteration, after the direction
+ * update, after the product + reduction and after the update + reduction --
+ * 4 per iteration for the first 64 iterations (n <= 256). */
+int sysu_solver_cg_phases(sysu_solver *s, unsigned long long *out, int n);
 /* Residual[0..9] of the last iteration (navier.h:65). */
 int sysu_solver_residuals(sysu_solver *s, double *out10);
 /* Per solve slot (mom u/v/w, p', k, eps, T, solid T): iterations, residual,
@@ -115,7 +122,8 @@ long sysu_solver_matrix(sysu_solver *s, const char *which, int *rowptr, int *col
 
 /* ---- standalone sparse solves on the GPU ------------------------------------
  * The Krylov kernels of the SIMPLE path applied to a host CSR matrix (0-based,
- * any column order).  method: 0 CG, 1 BiCGSTAB; precond: 0 none, 1 Jacobi
+ * any column order).  method: 0 CG, 1 BiCGSTAB, 2 CG with FP32 inner solves in
+ * FP64 defect correction (Jacobi only; iters = inner iterations); precond: 0 none, 1 Jacobi
  * (y = omega D^-1 c).  Stopping test ||b - A x||_2 / ||b||_2 < eps, as the
  * reference's SolveLinearEqu (tools.cpp:56-64) expects.  x: x0 in, solution out.
  * status: 0 converged, 1 max iterations, 2 breakdown, 3 barrier timeout,

@@ -166,6 +166,18 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
     if (k == "solid_source") { o.solid_source = value; return SYSU_OK; }
     if (k == "fatal_checks") { o.fatal_checks = value != 0.0; return SYSU_OK; }
     if (k == "timing") { o.timing = value != 0.0; return SYSU_OK; }
+    if (k == "profile_phases") {
+        return guarded([&] {
+            sysu::SimpleSolver &S = *s->impl;
+            o.profile_phases = value != 0.0;
+            if (o.profile_phases && !S.phase_ts.get()) {
+                S.phase_ts.alloc(4 * 64);
+                S.phase_ts.zero(S.st);
+            }
+            S.kw.phase_ts = o.profile_phases ? S.phase_ts.get() : nullptr;
+            return SYSU_OK;
+        });
+    }
     size_t dot = k.find('.');
     if (dot != std::string::npos) {
         sysu::EqOpts *e = eq_of(o, k.substr(0, dot));
@@ -174,6 +186,13 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
             if (f == "eps") { e->eps = value; return SYSU_OK; }
             if (f == "maxit") { e->maxit = (int)value; return SYSU_OK; }
             if (f == "omega") { e->omega = value; return SYSU_OK; }
+            if (f == "mixed") {
+                if (value != 0.0 && e->kind != sysu::SK_CG)
+                    return set_err(SYSU_ERR_INPUT, "mixed precision is available for CG solves (p, ts)");
+                e->mixed = value != 0.0;
+                return SYSU_OK;
+            }
+            if (f == "inner_tol") { e->inner_tol = value; return SYSU_OK; }
             if (f == "kind") {
                 int kind = (int)value;
                 if (kind != sysu::SK_CG && kind != sysu::SK_BICGSTAB) return set_err(SYSU_ERR_INPUT, "kind: 0 CG, 1 BiCGSTAB");
@@ -194,6 +213,7 @@ int sysu_solver_get_option(sysu_solver *s, const char *key, double *value) {
     if (k == "solid_source") { *value = o.solid_source; return SYSU_OK; }
     if (k == "fatal_checks") { *value = o.fatal_checks; return SYSU_OK; }
     if (k == "timing") { *value = o.timing; return SYSU_OK; }
+    if (k == "profile_phases") { *value = o.profile_phases; return SYSU_OK; }
     size_t dot = k.find('.');
     if (dot != std::string::npos) {
         sysu::EqOpts *e = eq_of(o, k.substr(0, dot));
@@ -203,6 +223,8 @@ int sysu_solver_get_option(sysu_solver *s, const char *key, double *value) {
             if (f == "maxit") { *value = e->maxit; return SYSU_OK; }
             if (f == "omega") { *value = e->omega; return SYSU_OK; }
             if (f == "kind") { *value = e->kind; return SYSU_OK; }
+            if (f == "mixed") { *value = e->mixed; return SYSU_OK; }
+            if (f == "inner_tol") { *value = e->inner_tol; return SYSU_OK; }
         }
     }
     return set_err(SYSU_ERR_INPUT, "unknown option " + k);
@@ -296,6 +318,18 @@ int sysu_solver_timer_stop(sysu_solver *s, double *ms) {
 }
 
 long sysu_kernel_launches(void) { return sysu::g_launches.load(); }
+
+int sysu_solver_cg_phases(sysu_solver *s, unsigned long long *out, int n) {
+    if (!s || !out) return set_err(SYSU_ERR_INPUT, "null argument");
+    return guarded([&] {
+        sysu::SimpleSolver &S = *s->impl;
+        if (!S.phase_ts.get()) return set_err(SYSU_ERR_INPUT, "option profile_phases is off");
+        int m = n < 256 ? n : 256;
+        S.phase_ts.download(out, (size_t)m, S.st);
+        S.sync();
+        return SYSU_OK;
+    });
+}
 
 int sysu_solver_residuals(sysu_solver *s, double *out10) {
     if (!s || !out10) return set_err(SYSU_ERR_INPUT, "null argument");

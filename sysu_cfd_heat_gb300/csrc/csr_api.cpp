@@ -84,6 +84,11 @@ int sysu_csr_solve(int method, int precond, int n, const int *rowptr, const int 
             o.jacobi = precond == 1;
             if (method == 0) {
                 sysu::cg_solve(M.A, M.val.get(), db.get(), dx.get(), false, o, w, info.get(), st);
+            } else if (method == 2) {
+                if (precond != 1) throw sysu::CaseError{"the mixed-precision CG uses the Jacobi preconditioner"};
+                sysu::DevBuf<float> v32(M.A.nnz);
+                sysu::sell_to_fp32(M.A, M.val.get(), v32.get(), st);
+                sysu::cg_solve_mixed(M.A, M.val.get(), v32.get(), db.get(), dx.get(), false, o, w, info.get(), st);
             } else {
                 const double *bb[1] = {db.get()};
                 double *xx[1] = {dx.get()};

@@ -155,6 +155,30 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double *smem) {
     }
 }
 
+// Deterministic block sum of NV values per thread; the result is valid in
+// thread 0 only (warp 0 alone combines the warp sums, which keeps the FP64
+// work per block small).  smem must hold NV * (blockDim.x/32) doubles.
+template <int NV>
+__device__ __forceinline__ void block_sum_t0(double (&v)[NV], double *smem) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(FULL_MASK, v[k], o);
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) smem[k * nw + warp] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double s = 0.0;
+            for (int w = 0; w < nw; ++w) s += smem[k * nw + w];
+            v[k] = s;
+        }
+    }
+}
+
 // Sum of `count` partials laid out partials[k*stride + b], b < count, computed
 // by one warp in a fixed order (identical in every block); all lanes get it.
 __device__ __forceinline__ double warp_sum_partials(const double *partials, int count) {

@@ -61,6 +61,7 @@ struct KrylovWork {
     DevBuf<double> r, rt, p, v, s, t, dinv, partials;
     DevBuf<float> r32, p32, q32, e32, dinv32;  // mixed-precision inner solve
     DevBuf<GridBarrier> barrier;
+    unsigned long long *phase_ts = nullptr;  // optional: 4 timestamps per CG iteration, first 64
     void ensure(int n, int nrhs, int max_blocks, cudaStream_t st);
     void ensure32(int n, cudaStream_t st);
 };
@@ -70,21 +71,21 @@ struct KrylovOpts {
     double eps = 1e-8;
     double omega = 1.0;       // Jacobi weight (the omega LASPack's precond gets)
     bool jacobi = true;       // false: no preconditioner
-    double inner_tol = 1e-4;  // mixed precision: relative reduction per FP32 inner solve
-    int max_refine = 50;      // mixed precision: FP64 defect-correction sweeps
+    double inner_tol = 0.1;   // mixed precision: FP32 residual drop that triggers a reliable update
 };
 
 // Copy FP64 SELL values to FP32 (same pattern).
 void sell_to_fp32(const SellDev &A, const double *val, float *val32, cudaStream_t st);
 
-// Mixed precision CG: FP64 defect correction (r = b - A x in FP64, x += e in
-// FP64) around FP32 Jacobi-CG inner solves A e = r of relative tolerance
-// inner_tol; inner dot products are summed in FP64 across threads.  Stops on
-// the FP64 residual ||b - A x|| / ||b|| < eps; iters = total inner iterations.
+// Mixed precision CG: FP32 Jacobi-CG recurrences with reliable updates -- each
+// time the FP32 residual has fallen by inner_tol, the FP32 correction is added
+// to the FP64 x and the FP64 residual b - A x replaces the FP32 one, keeping
+// the search direction (defect correction without restarting).  Dot products
+// are summed in FP64 across threads.  Stops on the FP64 residual
+// ||b - A x|| / ||b|| < eps; iters = FP32 iterations, refinements = updates.
 void cg_solve_mixed(const SellDev &A, const double *val, const float *val32, const double *b, double *x,
                     bool x0_zero, const KrylovOpts &o, KrylovWork &w, SolveInfo *info_dev, cudaStream_t st);
 
-int krylov_max_coresident_blocks();
 
 // Jacobi-preconditioned CG; x holds x0 on entry (or is zeroed first if x0_zero).
 void cg_solve(const SellDev &A, const double *val, const double *b, double *x, bool x0_zero,

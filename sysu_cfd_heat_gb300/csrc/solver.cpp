@@ -330,6 +330,15 @@ void SimpleSolver::solve(int slot, const EqOpts &o, const SellDev &A, const doub
     SolveInfo *info = infos.get() + slot;
     if (o.kind == SK_CG) {
         if (nrhs != 1) throw CaseError{"CG solves one right-hand side"};
+        if (o.mixed) {
+            // FP32 copy of this equation's matrix, then FP32 inner / FP64 outer CG
+            DevBuf<float> &v32 = (&A == &sd.A) ? s.As32 : f.Ap32;
+            if (v32.size() < (size_t)A.nnz) v32.alloc(A.nnz);
+            sell_to_fp32(A, val, v32.get(), st);
+            ko.inner_tol = o.inner_tol;
+            cg_solve_mixed(A, val, v32.get(), b[0], x[0], x0_zero, ko, kw, info, st);
+            return;
+        }
         cg_solve(A, val, b[0], x[0], x0_zero, ko, kw, info, st);
         return;
     }

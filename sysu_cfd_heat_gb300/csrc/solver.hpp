@@ -35,6 +35,8 @@ struct EqOpts {
     int maxit = 500;
     double eps = 1e-8;
     double omega = 1.2;
+    int mixed = 0;            // CG only: FP32 inner solves in FP64 defect correction
+    double inner_tol = 0.1;   // FP32 residual drop between reliable updates
 };
 
 struct SolverOptions {
@@ -51,6 +53,7 @@ struct SolverOptions {
     double solid_source = 0.0;    // W/m^3 (extension; the reference has none)
     bool fatal_checks = true;     // the reference's convergence checks
     bool timing = false;          // CUDA events around the p' solve
+    bool profile_phases = false;  // %globaltimer stamps at the CG phase boundaries
 };
 
 enum SolveSlot { SLOT_MOM = 0, SLOT_P, SLOT_K, SLOT_EPS, SLOT_T, SLOT_TS, SLOT_N };
@@ -66,6 +69,7 @@ struct FieldSet {
     DevBuf<double> Prod, TESrc, EDSrc, VisTE, VisED, ApTE, ApED, kcond, zeros, src;
     DevBuf<double> tmp3, tmpv;
     DevBuf<double> diff;  // solid conductivity
+    DevBuf<float> Ap32, As32;  // FP32 copies for mixed-precision solves
 };
 
 class SimpleSolver {
@@ -83,6 +87,7 @@ class SimpleSolver {
     DevBuf<double> red_partials, red_out;
     DevBuf<unsigned int> red_ticket;
     DevBuf<int> flags;
+    DevBuf<unsigned long long> phase_ts;
     RedScratch rs{};
     int red_blocks = 0;
 

@@ -141,6 +141,14 @@ class NavierStokesSolver:
         check(lib().sysu_solver_timing(self._h, C.byref(p), C.byref(m)))
         return p.value, m.value
 
+    def cg_phases(self) -> np.ndarray:
+        """%globaltimer stamps (ns) of the last CG solve, shape (64, 4): iteration
+        start, after the direction update, after the product, after the update
+        (option profile_phases)."""
+        ts = np.zeros(256, np.uint64)
+        check(lib().sysu_solver_cg_phases(self._h, ts.ctypes.data, 256))
+        return ts.reshape(64, 4)
+
     # -- fields ----------------------------------------------------------------------
     def field_size(self, name: str) -> int:
         n = lib().sysu_solver_field_size(self._h, name.encode())
@@ -191,7 +199,7 @@ def csr_solve(rowptr, col, val, b, x0=None, method: str = "CG", precond: str = "
     n = len(rowptr) - 1
     x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64)
     it, rs, stt = C.c_int(), C.c_double(), C.c_int()
-    code = fn({"CG": 0, "BiCGSTAB": 1}[method], {"none": 0, "Jacobi": 1}[precond], n,
+    code = fn({"CG": 0, "BiCGSTAB": 1, "CG-mixed": 2}[method], {"none": 0, "Jacobi": 1}[precond], n,
               rowptr.ctypes.data_as(ip), col.ctypes.data_as(ip), _dptr(val), _dptr(b), _dptr(x), maxit, eps, omega,
               C.byref(it), C.byref(rs), C.byref(stt))
     if code != 0:
