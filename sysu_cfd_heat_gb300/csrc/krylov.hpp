@@ -35,6 +35,7 @@ SellPattern make_sell(int n, const std::vector<int> &row_ptr, const std::vector<
 
 struct SellDev {
     int n = 0, nslices = 0;
+    int wmax = 0;      // widest slice (entries per row incl. padding)
     long nnz = 0, nnz_true = 0;
     DevBuf<int> sl_ptr, sl_w, col;
     void upload(const SellPattern &p, cudaStream_t s);
@@ -59,7 +60,7 @@ struct SolveInfo {
 struct KrylovWork {
     int n = 0, nrhs = 0, max_blocks = 0;
     DevBuf<double> r, rt, p, v, s, t, dinv, partials;
-    DevBuf<float> r32, p32, q32, e32, dinv32;  // mixed-precision inner solve
+    DevBuf<float> r32, z32, p32, q32, e32, dinv32;  // mixed-precision inner solve
     DevBuf<GridBarrier> barrier;
     unsigned long long *phase_ts = nullptr;  // optional: 4 timestamps per CG iteration, first 64
     void ensure(int n, int nrhs, int max_blocks, cudaStream_t st);
