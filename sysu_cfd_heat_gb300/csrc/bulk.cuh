@@ -127,7 +127,7 @@ __device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence
 
 // Capacity of the copy rings of the persistent kernels (slots per CTA).
 struct CopyRing {
-    static constexpr int DMAX = 4;
+    static constexpr int DMAX = 6;
     uint64_t bar[DMAX];
 };
 

@@ -2,39 +2,38 @@
 // with reliable FP64 updates.  Replaces LASPack's CGIter as the reference calls
 // it for the pressure correction and the solid conduction equation
 // (navier_pressure.cpp:29, HeatConductionSolver.cpp:90 through SolveLinearEqu,
-// tools.cpp:56-64): same recurrences (Barrett et al., "Templates", Fig. 2.5),
-// same stopping test ||b - A x||_2 / ||b||_2 < eps, same iteration cap.
+// tools.cpp:56-64): same stopping test ||b - A x||_2 / ||b||_2 < eps, same
+// iteration cap, and the iterates of Jacobi-PCG (Barrett et al., "Templates",
+// Fig. 2.5) in exact arithmetic.
 //
 // One solve = one cooperative launch of a persistent kernel, one 1024-thread
-// CTA per SM: 31 consumer warps and one producer warp.  Each CTA owns a
-// contiguous range of slices (32-row groups of the SELL matrix), cut into
-// tiles of TS = 31 slices -- one row per consumer thread.  An iteration is
-// three phases over the CTA's tiles:
-//   U  p = z + beta p                    reads z, p        writes p
-//   S  q = A p, p.q                      reads val, col    writes q   (gathers p)
+// CTA per SM.  Each CTA owns a contiguous range of slices (32-row groups of
+// the SELL matrix).  An iteration is two phases, each closed by an exact grid
+// reduction (exact_sum.cuh):
+//   S  w = A z, p = z + beta p, q = w + beta q, p.q      (gathers z)
 //   X  x += alpha p, r -= alpha q, z = M^-1 r, r.r, r.z
-//                                        reads p q x r dinv  writes x, r, z
-// separated by a grid barrier (U -> S) and two deterministic grid reductions.
-// Every operand a phase streams (everything but the gathered p) is moved into
-// shared memory by bulk asynchronous copies (cp.async.bulk, the TMA engine's
-// 1-D form) through a ring of D slots, so the DRAM stream runs ahead of the
-// arithmetic: while the consumers compute tile j, tiles j+1 .. j+D-1 are in
-// flight, also across phase boundaries and grid barriers.  The matrix is
-// copied with an L2 evict-first policy so the vectors (about 100 MB at 2M rows
-// in FP64) stay in the 126 MB L2 between phases.
+// S carries the direction update of Templates' loop (p = z + beta p) and keeps
+// q = A p by the recurrence A (z + beta p) = A z + beta A p, so no separate grid
+// barrier is needed between the direction update and the product.
 //
-// Ring protocol (per CTA): job j = (phase, tile) in consumption order lives in
-// slot j % D.  A slot's "full" mbarrier completes when its bytes land, its
-// "empty" mbarrier when all consumer warps are done with it.  Lane 0 of the
-// producer warp issues jobs in order as soon as the previous user of the slot
-// has been released, within a budget of released jobs.  Tiles of a phase that
-// read vectors the previous phase wrote are released at that phase's end,
-// after every thread's fence.proxy.async (which orders its plain stores before
-// later bulk-copy reads) and a block barrier; the matrix tiles of S are
-// released with U.  In its loop over phase P the producer blocks (bounded)
-// only for P's own tiles and issues later ones only when a slot is free, so it
-// always reaches the block barrier at the end of P.  Every wait is bounded; a
-// CTA drains its copies before it leaves.
+// S streams the matrix: tiles of TS = 31 slices (992 rows, one per consumer
+// thread) are moved into shared memory by bulk asynchronous copies
+// (cp.async.bulk, the TMA engine's 1-D form) through a ring of D slots.  Warp 31
+// is the producer: it issues a tile as soon as its slot has been released by
+// the 31 consumer warps, and queues the next iteration's first tiles at the
+// start of X, so S starts on landed data.  The matrix is copied with an L2
+// evict-first policy so that the Krylov vectors stay in L2.  X runs over the
+// CTA's rows with plain coalesced loads (all 32 warps, no per-tile
+// synchronisation).
+//
+// Ring protocol (per CTA): tile job j lives in slot j % D; a slot's "full"
+// mbarrier completes when its bytes land, its "empty" mbarrier when all
+// consumer warps are done with it.  The producer warp runs converged (lane 0
+// issues and takes the barrier decisions, broadcast by shuffle).  It blocks
+// (bounded) only for tiles of the running S phase and otherwise issues only
+// into free slots, so it always reaches the block barriers.  Only the matrix,
+// which no kernel thread writes, goes through the async proxy.  Every wait is
+// bounded; a CTA drains its copies before it leaves.
 #include <climits>
 
 #include "bulk.cuh"
@@ -48,14 +47,12 @@ constexpr int CG_PRODUCER = KBC / 32 - 1;
 constexpr int CG_MAX_TS = CG_CONSUMERS;             // 31 slices = 992 rows per tile
 constexpr unsigned CG_SMEM_BUDGET = 200 * 1024;     // dynamic shared memory for the ring
 
-enum CgPhase { PH_U = 0, PH_S = 1, PH_X = 2 };
-
 // Launch plan: slices per tile, ring depth, slot size.
 struct CgPlan {
     int ts = CG_MAX_TS;
     int depth = 2;
     unsigned slot = 0;     // bytes per slot (multiple of 128)
-    int direct = 0;        // 1: S tiles read val/col from global (rows too long for a slot)
+    int direct = 0;        // 1: tiles read val/col from global memory (rows too long for a slot)
     unsigned smem = 0;     // dynamic shared memory bytes
 };
 
@@ -109,28 +106,26 @@ __device__ __forceinline__ void set_fail(int *err) {
     atomicExch(err, (int)DEV_BARRIER_TIMEOUT);
 }
 
-// Ring state.  The consumer side (Ring, in registers) is uniform across the
-// consumer warps; the producer side (Producer, in shared memory) is touched by
-// the producer lane only.  A CTA runs its ring at depth min(D, nt).
+// Consumer side of the ring (registers, uniform across the consumer warps).
 struct Ring {
     int depth;
     unsigned slot;
-    int cslot;          // slot of the next job to consume
+    int cslot;          // slot of the next tile to consume
     unsigned cpar;      // its full-barrier phase parity
 };
+// Producer side (shared memory, read and written by the producer warp).
 struct Producer {
-    long long issued;   // jobs issued
-    long long allowed;  // jobs released so far (issue limit)
+    long long issued;   // tiles issued
     int nt;
-    int islot;          // slot of the next job to issue
+    int islot;          // slot of the next tile to issue
     unsigned ipar;      // its round parity
-    int iph, itile;     // phase and tile of the next job to issue
-    int primed;         // jobs issued so far, saturating at depth
+    int itile;          // its tile
+    int primed;         // tiles issued so far, saturating at depth
 };
 __shared__ Producer g_prod;
 
-// First matrix entry of every tile of the CTA (entry offsets of the S tiles),
-// so that issuing a tile needs no global load.
+// First matrix entry of every tile of the CTA, so that issuing or reading a
+// tile needs no global load of the slice pointers.
 constexpr int CG_TILE_TABLE = 1024;
 __shared__ int g_tile_e[CG_TILE_TABLE + 1];
 
@@ -138,33 +133,26 @@ __device__ __forceinline__ int tile_entry(const Part &P, const int *sl_ptr, int 
     return t <= CG_TILE_TABLE ? g_tile_e[t] : __ldg(sl_ptr + min(P.sb + t * P.ts, P.se));
 }
 
-
 __device__ __forceinline__ bool is_producer() { return (threadIdx.x >> 5) == CG_PRODUCER; }
-__device__ __forceinline__ bool is_producer_lane() { return threadIdx.x == CG_PRODUCER * 32; }
 
 __device__ __forceinline__ unsigned char *cslot_ptr(const Ring &R) { return g_slots + (size_t)R.cslot * R.slot; }
 
-// Producer warp (all 32 lanes, converged): issue jobs in order within the
-// budget; wait (bounded) for a slot only for jobs before `must_end`, stop at
-// the first busy slot otherwise.  Lane 0 issues the copies and takes the
-// barrier decisions, broadcast to the warp, so the warp never diverges across
-// the block barriers and warp collectives that follow.  The state is worked on
-// in registers (the copy instructions clobber memory).
+// Producer warp (all 32 lanes, converged): issue tiles in order while slots
+// are free; wait (bounded) for a slot only for tiles before `must_end`.  Lane 0
+// issues the copies and takes the barrier decisions, broadcast to the warp.
+// The state is worked on in registers (the copy instructions clobber memory).
 template <class Issue>
 __device__ __forceinline__ bool produce(const Ring &R, long long must_end, Issue &&issue) {
     Producer &Q = g_prod;
     const bool lead = (threadIdx.x & 31) == 0;
-    long long issued = Q.issued;
-    const long long allowed = Q.allowed;
-    if (issued >= allowed) return true;
     const int nt = Q.nt, depth = R.depth;
-    int islot = Q.islot, iph = Q.iph, itile = Q.itile, primed = Q.primed;
+    long long issued = Q.issued;
+    int islot = Q.islot, itile = Q.itile, primed = Q.primed;
     unsigned ipar = Q.ipar;
-    const uint64_t pol_stream = l2_policy_evict_first();
-    const uint64_t pol_keep = l2_policy_evict_last();
+    const uint64_t pol = l2_policy_evict_first();
     bool ok = true;
-    while (issued < allowed) {
-        if (primed == depth) {  // the slot's previous job must be released by all consumers
+    for (;;) {
+        if (primed == depth) {  // the slot's previous tile must be released by all consumers
             int free_slot = lead ? (int)mbar_test_wait(&g_empty[islot], ipar ^ 1u) : 0;
             free_slot = __shfl_sync(FULL_MASK, free_slot, 0);
             if (!free_slot) {
@@ -175,10 +163,10 @@ __device__ __forceinline__ bool produce(const Ring &R, long long must_end, Issue
         } else {
             ++primed;
         }
-        if (lead) issue(iph, itile, g_slots + (size_t)islot * R.slot, &g_full[islot], pol_stream, pol_keep);
+        if (lead) issue(itile, g_slots + (size_t)islot * R.slot, &g_full[islot], pol);
         __syncwarp();
         if (++islot == depth) { islot = 0; ipar ^= 1u; }
-        if (++itile == nt) { itile = 0; if (++iph == 3) iph = 0; }
+        if (++itile == nt) itile = 0;
         ++issued;
     }
     __syncwarp();
@@ -186,7 +174,6 @@ __device__ __forceinline__ bool produce(const Ring &R, long long must_end, Issue
         Q.issued = issued;
         Q.islot = islot;
         Q.ipar = ipar;
-        Q.iph = iph;
         Q.itile = itile;
         Q.primed = primed;
     }
@@ -194,16 +181,16 @@ __device__ __forceinline__ bool produce(const Ring &R, long long must_end, Issue
     return ok;
 }
 
-// The producer warp's part of a phase: issue the phase's remaining tiles
-// (jobs before must_end) and whatever later tiles fit.
+// Producer warp: the running S phase's tiles up to must_end (blocking) and
+// whatever fits in free slots after them.
 template <class Issue>
-__device__ __forceinline__ void producer_phase(const Ring &R, long long must_end, Issue &&issue, int *err) {
-    if (!is_producer()) return;
-    bool ok = __all_sync(FULL_MASK, !fail_flag()) ? produce(R, must_end, issue) : true;
+__device__ __forceinline__ void producer_tiles(const Ring &R, long long must_end, Issue &&issue, int *err) {
+    if (!__all_sync(FULL_MASK, !fail_flag())) return;
+    bool ok = produce(R, must_end, issue);
     if (!ok && (threadIdx.x & 31) == 0) set_fail(err);
 }
 
-// Consumer warps: wait until the next job has landed.  The outcome is uniform
+// Consumer warps: wait until the next tile has landed.  The outcome is uniform
 // per warp; false after a timed-out wait (recorded in g_fail and *err).
 __device__ __forceinline__ bool acquire(const Ring &R, int *err) {
     bool ok = !__any_sync(FULL_MASK, fail_flag() != 0);
@@ -225,7 +212,7 @@ __device__ __forceinline__ void release(Ring &R) {
 // slot (a slot's copies complete in order), so none is in flight when the CTA
 // leaves, whether or not its tile was consumed.
 __device__ __forceinline__ void drain(const Ring &R) {
-    if (!is_producer_lane()) return;
+    if (threadIdx.x != CG_PRODUCER * 32) return;
     long long issued = g_prod.issued;
     for (int s = 0; s < R.depth; ++s) {
         long long last = issued - 1 - ((issued - 1 - s) % R.depth + R.depth) % R.depth;
@@ -234,8 +221,7 @@ __device__ __forceinline__ void drain(const Ring &R) {
     }
 }
 
-__device__ __forceinline__ void ring_init(Ring &R, const CgPlan &pl, const Part &P, const int *sl_ptr,
-                                          long long allowed) {
+__device__ __forceinline__ void ring_init(Ring &R, const CgPlan &pl, const Part &P, const int *sl_ptr) {
     const int nt = P.nt;
     for (int t = threadIdx.x; t <= min(nt, CG_TILE_TABLE); t += blockDim.x)
         g_tile_e[t] = __ldg(sl_ptr + min(P.sb + t * P.ts, P.se));
@@ -246,11 +232,10 @@ __device__ __forceinline__ void ring_init(Ring &R, const CgPlan &pl, const Part 
     if (threadIdx.x == 0) {
         Producer &Q = g_prod;
         Q.issued = 0;
-        Q.allowed = allowed;
         Q.nt = nt;
         Q.islot = 0;
         Q.ipar = 0u;
-        Q.iph = Q.itile = 0;
+        Q.itile = 0;
         Q.primed = 0;
         for (int k = 0; k < R.depth; ++k) {
             mbar_init(&g_full[k], 1);
@@ -262,22 +247,6 @@ __device__ __forceinline__ void ring_init(Ring &R, const CgPlan &pl, const Part 
     __syncthreads();
 }
 
-// Every thread at the end of a phase: publish this phase's plain stores to the
-// async proxy (one fence per thread per phase), block barrier, then the
-// producer releases `more` further jobs -- tiles of the next phase, whose
-// copies read those stores -- and issues what fits, so they land while the
-// CTA waits in the grid barrier that follows.
-template <class Issue>
-__device__ __forceinline__ void phase_end(const Ring &R, int more, Issue &&issue, int *err) {
-    fence_proxy_async_global();
-    __syncthreads();
-    if (is_producer() && __all_sync(FULL_MASK, !fail_flag())) {
-        if ((threadIdx.x & 31) == 0) g_prod.allowed += more;
-        __syncwarp();
-        if (!produce(R, 0, issue) && (threadIdx.x & 31) == 0) set_fail(err);
-    }
-}
-
 // Loop state code from the squared residual: 1 converged (||r||^2 < thr,
 // thr = eps^2 ||b||^2, the stopping test ||r|| / ||b|| < eps without a square
 // root or division per iteration), 2 not finite, 0 go on.
@@ -286,7 +255,7 @@ __device__ __forceinline__ double stop_code(double rr, double thr) {
 }
 
 // One SELL row of a tile: the column indices of up to 8 entries, then their
-// gathers, then the FMAs.
+// gathers, then the FMAs.  diag = x of the row itself (entry 0 is the diagonal).
 template <class V, class X, class Acc>
 __device__ __forceinline__ Acc tile_row_dot(const V *vs, const int *cs, int e, int w, const X *__restrict__ x,
                                             X &diag) {
@@ -311,6 +280,23 @@ __device__ __forceinline__ Acc tile_row_dot(const V *vs, const int *cs, int e, i
     return acc;
 }
 
+// The tile copy of the matrix (values, then the column indices) for tile t.
+template <class V>
+__device__ __forceinline__ void issue_matrix_tile(const Part &P, const SellView &A, const V *val, int direct, int t,
+                                                  unsigned char *dst, uint64_t *bar, uint64_t pol) {
+    if (direct) {
+        mbar_arrive_expect_tx(bar, 0);
+        return;
+    }
+    long e0 = tile_entry(P, A.sl_ptr, t), e1 = tile_entry(P, A.sl_ptr, t + 1);
+    unsigned bv = (unsigned)((e1 - e0) * sizeof(V)), bc = (unsigned)((e1 - e0) * 4);
+    mbar_arrive_expect_tx(bar, bv + bc);
+    if (bv) {
+        bulk_g2s(dst, val + e0, bv, bar, pol);
+        bulk_g2s(dst + bv, A.col + e0, bc, bar, pol);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // FP64
 __global__ void __launch_bounds__(KBC, 1) k_cg_pipe(CgPipeArgs a) {
@@ -321,10 +307,13 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_pipe(CgPipeArgs a) {
     RedCtx rc{a.partials, (int)gridDim.x, 0};
     const Part P = make_part(n, a.A.nslices, a.plan.ts);
     const int nt = P.nt;
-    const unsigned VS = (unsigned)P.ts * 32 * sizeof(double);  // vector stride in a slot
     const int R0 = P.sb * 32, R1 = min(P.se * 32, n);
     Ring R;
-    ring_init(R, a.plan, P, a.A.sl_ptr, 2LL * nt);  // U and S tiles of the first iteration
+    ring_init(R, a.plan, P, a.A.sl_ptr);
+    auto issue = [&](int t, unsigned char *dst, uint64_t *bar, uint64_t pol) {
+        issue_matrix_tile<double>(P, a.A, a.A.val, a.plan.direct, t, dst, bar, pol);
+    };
+    if (prod) producer_tiles(R, 0, issue, err);  // the first tiles land during the initial residual
 
     // r = b - A x, z = M^-1 r; ||b||^2, ||r||^2, r.z
     double v3[3] = {0.0, 0.0, 0.0};
@@ -334,11 +323,10 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_pipe(CgPipeArgs a) {
         double zi = a.dinv[i] * ri;
         a.r[i] = ri;
         a.z[i] = zi;
-        v3[0] += bi * bi;
-        v3[1] += ri * ri;
-        v3[2] += ri * zi;
+        v3[0] = fma(bi, bi, v3[0]);
+        v3[1] = fma(ri, ri, v3[1]);
+        v3[2] = fma(ri, zi, v3[2]);
     }
-    fence_proxy_async_global();
     if (!grid_sum_t0<3>(v3, rc, a.gb, err)) { drain(R); return; }
     // thread-0 scalar state, kept in shared memory (no registers in the other threads)
     __shared__ double s_state[4];
@@ -353,38 +341,7 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_pipe(CgPipeArgs a) {
     }
     __syncthreads();
 
-    auto issue = [&](int ph, int t, unsigned char *dst, uint64_t *bar, uint64_t pol_stream, uint64_t pol_keep) {
-        int s0, s1, r0, nr;
-        P.tile(t, s0, s1, r0, nr);
-        unsigned vb = (unsigned)(nr * 8) & ~15u;
-        if (ph == PH_S) {
-            if (a.plan.direct) { mbar_arrive_expect_tx(bar, 0); return; }
-            long e0 = tile_entry(P, a.A.sl_ptr, t), e1 = tile_entry(P, a.A.sl_ptr, t + 1);
-            unsigned bv = (unsigned)((e1 - e0) * 8), bc = (unsigned)((e1 - e0) * 4);
-            mbar_arrive_expect_tx(bar, bv + bc);
-            if (bv) {
-                bulk_g2s(dst, a.A.val + e0, bv, bar, pol_stream);
-                bulk_g2s(dst + bv, a.A.col + e0, bc, bar, pol_stream);
-            }
-        } else if (ph == PH_U) {
-            mbar_arrive_expect_tx(bar, 2 * vb);
-            if (vb) {
-                bulk_g2s(dst, a.z + r0, vb, bar, pol_keep);
-                bulk_g2s(dst + VS, a.p + r0, vb, bar, pol_keep);
-            }
-        } else {
-            mbar_arrive_expect_tx(bar, 5 * vb);
-            if (vb) {
-                bulk_g2s(dst, a.p + r0, vb, bar, pol_keep);
-                bulk_g2s(dst + VS, a.q + r0, vb, bar, pol_keep);
-                bulk_g2s(dst + 2 * VS, a.x + r0, vb, bar, pol_keep);
-                bulk_g2s(dst + 3 * VS, a.r + r0, vb, bar, pol_keep);
-                bulk_g2s(dst + 4 * VS, a.dinv + r0, vb, bar, pol_keep);
-            }
-        }
-    };
-
-    long long base = 0;  // job index of the current phase's first tile
+    long long base = 0;  // job index of the running S phase's first tile
     int it = 0, status = DEV_OK;
     for (;;) {
         double code = g_bc[0], beta = g_bc[1];
@@ -393,38 +350,19 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_pipe(CgPipeArgs a) {
         if (code == 2.0) { status = DEV_NONFINITE; break; }
         ++it;
         stamp(a.ts, it, 0);
-        // U
-        if (prod) {
-            producer_phase(R, base + nt, issue, err);
-        } else {
-            for (int t = 0; t < nt; ++t) {
-                if (!acquire(R, err)) break;
-                const double *sp = reinterpret_cast<const double *>(cslot_ptr(R));
-                int s0, s1, r0, nr;
-                P.tile(t, s0, s1, r0, nr);
-                if (tid < nr) {
-                    int i = r0 + tid;
-                    bool tma = tid < (nr & ~1);
-                    double zi = tma ? sp[tid] : a.z[i];
-                    double pi = tma ? sp[VS / 8 + tid] : a.p[i];
-                    a.p[i] = (it == 1) ? zi : fma(beta, pi, zi);
-                }
-                release(R);
-            }
-        }
-        base += nt;
-        if (!grid_sync(a.gb, err) || fail_flag()) break;
-        stamp(a.ts, it, 1);
-        // S
+        // S: w = A z, p = z + beta p, q = w + beta q, p.q
         double v1[1] = {0.0};
         if (prod) {
-            producer_phase(R, base + nt, issue, err);
+            producer_tiles(R, base + nt, issue, err);
         } else {
             for (int t = 0; t < nt; ++t) {
                 if (!acquire(R, err)) break;
                 int s0, s1, r0, nr;
                 P.tile(t, s0, s1, r0, nr);
                 if (tid < nr) {
+                    const int i = r0 + tid;
+                    double pi = 0.0, qi = 0.0;
+                    if (it > 1) { pi = a.p[i]; qi = a.q[i]; }
                     int s = s0 + (tid >> 5);
                     int e0 = tile_entry(P, a.A.sl_ptr, t), e1 = tile_entry(P, a.A.sl_ptr, t + 1);
                     int es = __ldg(a.A.sl_ptr + s) - e0 + (tid & 31);
@@ -438,18 +376,20 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_pipe(CgPipeArgs a) {
                         vs = reinterpret_cast<const double *>(cslot_ptr(R));
                         cs = reinterpret_cast<const int *>(cslot_ptr(R) + (size_t)(e1 - e0) * 8);
                     }
-                    double pi;
-                    double qi = tile_row_dot<double, double, double>(vs, cs, es, w, a.p, pi);
-                    a.q[r0 + tid] = qi;
+                    double zi;
+                    double wi = tile_row_dot<double, double, double>(vs, cs, es, w, a.z, zi);
+                    pi = fma(beta, pi, zi);
+                    qi = fma(beta, qi, wi);
+                    a.p[i] = pi;
+                    a.q[i] = qi;
                     v1[0] = fma(pi, qi, v1[0]);
                 }
                 release(R);
             }
         }
         base += nt;
-        phase_end(R, nt, issue, err);  // X tiles read p and q
         if (!grid_sum_t0<1>(v1, rc, a.gb, err) || fail_flag()) break;
-        stamp(a.ts, it, 2);
+        stamp(a.ts, it, 1);
         if (tid == 0) {
             g_bc[2] = v1[0] == 0.0 ? 0.0 : rho / v1[0];
             g_bc[3] = v1[0] == 0.0 ? 1.0 : 0.0;
@@ -457,41 +397,23 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_pipe(CgPipeArgs a) {
         __syncthreads();
         double alpha = g_bc[2];
         if (g_bc[3] != 0.0) { status = DEV_BREAKDOWN; break; }
-        // X
+        // X: the producer first queues the next S phase's tiles
+        if (prod) producer_tiles(R, 0, issue, err);
         double v2[2] = {0.0, 0.0};
-        if (prod) {
-            producer_phase(R, base + nt, issue, err);
-        } else {
-            for (int t = 0; t < nt; ++t) {
-                if (!acquire(R, err)) break;
-                const double *sp = reinterpret_cast<const double *>(cslot_ptr(R));
-                int s0, s1, r0, nr;
-                P.tile(t, s0, s1, r0, nr);
-                if (tid < nr) {
-                    int i = r0 + tid;
-                    const unsigned V = VS / 8;
-                    double pi, qi, xi, ri, di;
-                    if (tid < (nr & ~1)) {
-                        pi = sp[tid]; qi = sp[V + tid]; xi = sp[2 * V + tid]; ri = sp[3 * V + tid]; di = sp[4 * V + tid];
-                    } else {
-                        pi = a.p[i]; qi = a.q[i]; xi = a.x[i]; ri = a.r[i]; di = a.dinv[i];
-                    }
-                    xi = fma(alpha, pi, xi);
-                    ri = fma(-alpha, qi, ri);
-                    double zi = di * ri;
-                    a.x[i] = xi;
-                    a.r[i] = ri;
-                    a.z[i] = zi;
-                    v2[0] = fma(ri, ri, v2[0]);
-                    v2[1] = fma(ri, zi, v2[1]);
-                }
-                release(R);
-            }
+#pragma unroll 4
+        for (int i = R0 + tid; i < R1; i += KBC) {
+            double pi = a.p[i], qi = a.q[i], xi = a.x[i], ri = a.r[i], di = a.dinv[i];
+            xi = fma(alpha, pi, xi);
+            ri = fma(-alpha, qi, ri);
+            double zi = di * ri;
+            a.x[i] = xi;
+            a.r[i] = ri;
+            a.z[i] = zi;
+            v2[0] = fma(ri, ri, v2[0]);
+            v2[1] = fma(ri, zi, v2[1]);
         }
-        base += nt;
-        phase_end(R, 2 * nt, issue, err);  // next U tiles read z and p; S tiles
         if (!grid_sum_t0<2>(v2, rc, a.gb, err) || fail_flag()) break;
-        stamp(a.ts, it, 3);
+        stamp(a.ts, it, 2);
         if (tid == 0) {
             rr = v2[0];
             g_bc[0] = stop_code(rr, thr);
@@ -518,7 +440,7 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_pipe(CgPipeArgs a) {
 // FP64 solution, e is zeroed, the FP64 residual b - A x replaces the FP32 one
 // and the search direction is kept, so the Krylov process is not restarted.
 // Convergence is decided on that FP64 residual only.  Per-thread partial dot
-// products run in FP32 over the thread's rows; FP64 across threads.
+// products run in FP32 over the thread's rows; exact sums across threads.
 __global__ void __launch_bounds__(KBC, 1) k_cg_mixed_pipe(CgPipeArgs a) {
     const int n = a.A.n;
     const int tid = threadIdx.x;
@@ -527,11 +449,14 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_mixed_pipe(CgPipeArgs a) {
     RedCtx rc{a.partials, (int)gridDim.x, 0};
     const Part P = make_part(n, a.A.nslices, a.plan.ts);
     const int nt = P.nt;
-    const unsigned VS = (unsigned)P.ts * 32 * sizeof(float);
     const int R0 = P.sb * 32, R1 = min(P.se * 32, n);
     const float *__restrict__ dinv = a.dinv32;
     Ring R;
-    ring_init(R, a.plan, P, a.A.sl_ptr, 0);
+    ring_init(R, a.plan, P, a.A.sl_ptr);
+    auto issue = [&](int t, unsigned char *dst, uint64_t *bar, uint64_t pol) {
+        issue_matrix_tile<float>(P, a.A, a.val32, a.plan.direct, t, dst, bar, pol);
+    };
+    if (prod) producer_tiles(R, 0, issue, err);
 
     // FP64 residual of the initial guess and its FP32 copy
     double v3[3] = {0.0, 0.0, 0.0};
@@ -543,12 +468,11 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_mixed_pipe(CgPipeArgs a) {
         a.r32[i] = rf;
         a.z32[i] = zf;
         a.e32[i] = 0.f;
-        v3[0] += bi * bi;
-        v3[1] += ri * ri;
+        v3[0] = fma(bi, bi, v3[0]);
+        v3[1] = fma(ri, ri, v3[1]);
         f2 = fmaf(rf, zf, f2);
     }
     v3[2] = (double)f2;
-    fence_proxy_async_global();
     if (!grid_sum_t0<3>(v3, rc, a.gb, err)) { drain(R); return; }
     // thread-0 scalar state, kept in shared memory (no registers in the other threads);
     // rr_ref: FP64 ||b - A x||^2 at the last reliable update
@@ -564,38 +488,7 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_mixed_pipe(CgPipeArgs a) {
     }
     __syncthreads();
 
-    auto issue = [&](int ph, int t, unsigned char *dst, uint64_t *bar, uint64_t pol_stream, uint64_t pol_keep) {
-        int s0, s1, r0, nr;
-        P.tile(t, s0, s1, r0, nr);
-        unsigned vb = (unsigned)(nr * 4) & ~15u;
-        if (ph == PH_S) {
-            if (a.plan.direct) { mbar_arrive_expect_tx(bar, 0); return; }
-            long e0 = tile_entry(P, a.A.sl_ptr, t), e1 = tile_entry(P, a.A.sl_ptr, t + 1);
-            unsigned bv = (unsigned)((e1 - e0) * 4);
-            mbar_arrive_expect_tx(bar, 2 * bv);
-            if (bv) {
-                bulk_g2s(dst, a.val32 + e0, bv, bar, pol_stream);
-                bulk_g2s(dst + bv, a.A.col + e0, bv, bar, pol_stream);
-            }
-        } else if (ph == PH_U) {
-            mbar_arrive_expect_tx(bar, 2 * vb);
-            if (vb) {
-                bulk_g2s(dst, a.z32 + r0, vb, bar, pol_keep);
-                bulk_g2s(dst + VS, a.p32 + r0, vb, bar, pol_keep);
-            }
-        } else {
-            mbar_arrive_expect_tx(bar, 5 * vb);
-            if (vb) {
-                bulk_g2s(dst, a.p32 + r0, vb, bar, pol_keep);
-                bulk_g2s(dst + VS, a.q32 + r0, vb, bar, pol_keep);
-                bulk_g2s(dst + 2 * VS, a.e32 + r0, vb, bar, pol_keep);
-                bulk_g2s(dst + 3 * VS, a.r32 + r0, vb, bar, pol_keep);
-                bulk_g2s(dst + 4 * VS, dinv + r0, vb, bar, pol_keep);
-            }
-        }
-    };
-
-    long long base = 0;  // job index of the current phase's first tile
+    long long base = 0;
     int total = 0, nupd = 0, status = DEV_OK;
     for (;;) {
         double code = g_bc[0];  // from the FP64 residual of the last update
@@ -605,40 +498,18 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_mixed_pipe(CgPipeArgs a) {
         if (code == 2.0) { status = DEV_NONFINITE; break; }
         ++total;
         stamp(a.ts, total, 0);
-        // U tiles read z, which a reliable update rewrites: they are released
-        // only here, with this iteration's S tiles (X tiles at the end of S)
-        if (is_producer_lane()) g_prod.allowed = base + 2LL * nt;
-        __syncwarp();
-        if (prod) {
-            producer_phase(R, base + nt, issue, err);
-        } else {
-            for (int t = 0; t < nt; ++t) {
-                if (!acquire(R, err)) break;
-                const float *sp = reinterpret_cast<const float *>(cslot_ptr(R));
-                int s0, s1, r0, nr;
-                P.tile(t, s0, s1, r0, nr);
-                if (tid < nr) {
-                    int i = r0 + tid;
-                    bool tma = tid < (nr & ~3);
-                    float zi = tma ? sp[tid] : a.z32[i];
-                    float pi = tma ? sp[VS / 4 + tid] : a.p32[i];
-                    a.p32[i] = (total == 1) ? zi : fmaf(beta, pi, zi);
-                }
-                release(R);
-            }
-        }
-        base += nt;
-        if (!grid_sync(a.gb, err) || fail_flag()) break;
-        stamp(a.ts, total, 1);
         float g0 = 0.f;
         if (prod) {
-            producer_phase(R, base + nt, issue, err);
+            producer_tiles(R, base + nt, issue, err);
         } else {
             for (int t = 0; t < nt; ++t) {
                 if (!acquire(R, err)) break;
                 int s0, s1, r0, nr;
                 P.tile(t, s0, s1, r0, nr);
                 if (tid < nr) {
+                    const int i = r0 + tid;
+                    float pi = 0.f, qi = 0.f;
+                    if (total > 1) { pi = a.p32[i]; qi = a.q32[i]; }
                     int s = s0 + (tid >> 5);
                     int e0 = tile_entry(P, a.A.sl_ptr, t), e1 = tile_entry(P, a.A.sl_ptr, t + 1);
                     int es = __ldg(a.A.sl_ptr + s) - e0 + (tid & 31);
@@ -652,19 +523,21 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_mixed_pipe(CgPipeArgs a) {
                         vs = reinterpret_cast<const float *>(cslot_ptr(R));
                         cs = reinterpret_cast<const int *>(cslot_ptr(R) + (size_t)(e1 - e0) * 4);
                     }
-                    float pi;
-                    float qi = tile_row_dot<float, float, float>(vs, cs, es, w, a.p32, pi);
-                    a.q32[r0 + tid] = qi;
+                    float zi;
+                    float wi = tile_row_dot<float, float, float>(vs, cs, es, w, a.z32, zi);
+                    pi = fmaf(beta, pi, zi);
+                    qi = fmaf(beta, qi, wi);
+                    a.p32[i] = pi;
+                    a.q32[i] = qi;
                     g0 = fmaf(pi, qi, g0);
                 }
                 release(R);
             }
         }
         base += nt;
-        phase_end(R, nt, issue, err);  // X tiles read p and q
         double v1[1] = {(double)g0};
         if (!grid_sum_t0<1>(v1, rc, a.gb, err) || fail_flag()) break;
-        stamp(a.ts, total, 2);
+        stamp(a.ts, total, 1);
         if (tid == 0) {
             g_bc[2] = v1[0] == 0.0 ? 0.0 : rho / v1[0];
             g_bc[3] = v1[0] == 0.0 ? 1.0 : 0.0;
@@ -672,41 +545,23 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_mixed_pipe(CgPipeArgs a) {
         __syncthreads();
         float alpha = (float)g_bc[2];
         if (g_bc[3] != 0.0) { status = DEV_BREAKDOWN; break; }
+        if (prod) producer_tiles(R, 0, issue, err);
         float h0 = 0.f, h1 = 0.f;
-        if (prod) {
-            producer_phase(R, base + nt, issue, err);
-        } else {
-            for (int t = 0; t < nt; ++t) {
-                if (!acquire(R, err)) break;
-                const float *sp = reinterpret_cast<const float *>(cslot_ptr(R));
-                int s0, s1, r0, nr;
-                P.tile(t, s0, s1, r0, nr);
-                if (tid < nr) {
-                    int i = r0 + tid;
-                    const unsigned V = VS / 4;
-                    float pi, qi, ei, ri, di;
-                    if (tid < (nr & ~3)) {
-                        pi = sp[tid]; qi = sp[V + tid]; ei = sp[2 * V + tid]; ri = sp[3 * V + tid]; di = sp[4 * V + tid];
-                    } else {
-                        pi = a.p32[i]; qi = a.q32[i]; ei = a.e32[i]; ri = a.r32[i]; di = dinv[i];
-                    }
-                    ei = fmaf(alpha, pi, ei);
-                    ri = fmaf(-alpha, qi, ri);
-                    float zi = di * ri;
-                    a.e32[i] = ei;
-                    a.r32[i] = ri;
-                    a.z32[i] = zi;
-                    h0 = fmaf(ri, ri, h0);
-                    h1 = fmaf(ri, zi, h1);
-                }
-                release(R);
-            }
+#pragma unroll 4
+        for (int i = R0 + tid; i < R1; i += KBC) {
+            float pi = a.p32[i], qi = a.q32[i], ei = a.e32[i], ri = a.r32[i], di = dinv[i];
+            ei = fmaf(alpha, pi, ei);
+            ri = fmaf(-alpha, qi, ri);
+            float zi = di * ri;
+            a.e32[i] = ei;
+            a.r32[i] = ri;
+            a.z32[i] = zi;
+            h0 = fmaf(ri, ri, h0);
+            h1 = fmaf(ri, zi, h1);
         }
-        base += nt;
-        phase_end(R, 0, issue, err);  // next U tiles read z and p
         double w2[2] = {(double)h0, (double)h1};
         if (!grid_sum_t0<2>(w2, rc, a.gb, err) || fail_flag()) break;
-        stamp(a.ts, total, 3);
+        stamp(a.ts, total, 2);
         if (tid == 0) {
             // reliable update once the FP32 residual fell by inner_tol since the
             // last one, when it looks converged, or at the iteration cap
@@ -732,11 +587,10 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_mixed_pipe(CgPipeArgs a) {
                 float rf = (float)ri, zf = dinv[i] * rf;
                 a.r32[i] = rf;
                 a.z32[i] = zf;
-                u[0] += ri * ri;
+                u[0] = fma(ri, ri, u[0]);
                 fz = fmaf(rf, zf, fz);
             }
             u[1] = (double)fz;
-            fence_proxy_async_global();
             if (!grid_sum_t0<2>(u, rc, a.gb, err)) break;
             if (tid == 0) {
                 rr_ref = u[0];
@@ -773,9 +627,7 @@ CgPlan plan_cg(int wmax, int ebytes) {
     CgPlan pl;
     auto round128 = [](unsigned b) { return (b + 127u) & ~127u; };
     for (int ts = CG_MAX_TS; ts >= 1; ts /= 2) {
-        unsigned vec = 5u * ts * 32 * ebytes;
-        unsigned mat = (unsigned)ts * 32 * (unsigned)wmax * (unsigned)(ebytes + 4);
-        unsigned slot = round128(std::max(vec, mat));
+        unsigned slot = round128((unsigned)ts * 32 * (unsigned)std::max(wmax, 1) * (unsigned)(ebytes + 4));
         int depth = (int)std::min<unsigned>(CopyRing::DMAX, CG_SMEM_BUDGET / slot);
         if (depth >= 2) {
             pl.ts = ts;
@@ -785,11 +637,11 @@ CgPlan plan_cg(int wmax, int ebytes) {
             return pl;
         }
     }
-    // rows too long for a slot: S tiles read the matrix from global memory
+    // rows too long for a slot: tiles read the matrix from global memory
     pl.ts = CG_MAX_TS;
     pl.direct = 1;
-    pl.slot = round128(5u * CG_MAX_TS * 32 * ebytes);
-    pl.depth = (int)std::min<unsigned>(CopyRing::DMAX, CG_SMEM_BUDGET / pl.slot);
+    pl.slot = 128;
+    pl.depth = 2;
     pl.smem = pl.slot * pl.depth;
     return pl;
 }
@@ -817,7 +669,7 @@ void cg_solve(const SellDev &A, const double *val, const double *b, double *x, b
     static int maxb = 0;
     if (!maxb) maxb = cg_max_blocks(k_cg_pipe);
     w.ensure(n, 1, maxb, st);
-    check_aligned16({x, val, A.col.get(), w.r.get(), w.s.get(), w.p.get(), w.v.get(), w.dinv.get()});
+    check_aligned16({val, A.col.get()});
     SellView V = view(A, val);
     { k_jacobi_dinv<<<(n + KB - 1) / KB, KB, 0, st>>>(V, o.omega, o.jacobi ? 1 : 0, w.dinv.get()); ++::sysu::g_launches; }
     if (x0_zero) { k_zero<<<(n + KB - 1) / KB, KB, 0, st>>>(x, n); ++::sysu::g_launches; }
@@ -851,8 +703,7 @@ void cg_solve_mixed(const SellDev &A, const double *val, const float *val32, con
     if (!maxb) maxb = cg_max_blocks(k_cg_mixed_pipe);
     w.ensure(n, 1, maxb, st);
     w.ensure32(n, st);
-    check_aligned16({x, val32, A.col.get(), w.r32.get(), w.z32.get(), w.p32.get(), w.q32.get(),
-                     w.e32.get(), w.dinv32.get()});
+    check_aligned16({val32, A.col.get()});
     SellView V = view(A, val);
     { k_dinv32<<<(n + KB - 1) / KB, KB, 0, st>>>(V, o.omega, w.dinv32.get()); ++::sysu::g_launches; }
     if (x0_zero) { k_zero<<<(n + KB - 1) / KB, KB, 0, st>>>(x, n); ++::sysu::g_launches; }
