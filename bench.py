@@ -48,6 +48,7 @@ RE_MU = 0.0025
 SEED = 20261203
 RTC = 1e-8
 L2_BYTES = 129 * 1024 * 1024
+FP64_PEAK_TFLOPS = 1.25
 
 
 def rank_info():
@@ -121,12 +122,21 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cg_bytes_per_iter(n: int, nnz: int) -> float:
-    """Algorithmic bytes of one Jacobi-PCG iteration, FP64 values, int32 indices:
-    SpMV nnz*(8+4) + 4(N+1) + 2*8N, plus 88N for the vector updates (x, p, r, Ap and
-    D^-1 read, x, r, z written; z and p read, p written)."""
-    spmv = nnz * 12 + 4 * (n + 1) + 16 * n
-    return spmv + 88 * n
+def cg_bytes_per_iter(n: int, nnz: int, fp32: bool = False) -> float:
+    """Algorithmic bytes of one CG iteration of the p' kernel (two phases):
+    S reads the matrix once (values + int32 columns), gathers z once (one value per
+    row), reads and writes p and q; X reads p, q, x (or the correction e), r,
+    D^-1 and writes x (e), r, z.  FP64: nnz*12 + 104*N; FP32 recurrences:
+    nnz*8 + 52*N."""
+    if fp32:
+        return nnz * 8 + 52 * n
+    return nnz * 12 + 104 * n
+
+
+def cg_flops_per_iter(n: int, nnz_true: int) -> float:
+    """FP64 flops of one CG iteration: 2 per stored-true matrix entry, 6 per row in S
+    (p, q updates, p.q), 9 per row in X (x, r, z, r.r, r.z)."""
+    return 2.0 * nnz_true + 15.0 * n
 
 
 def cpu_reference_run(param: str, iters: int, budget_s: float, timeout_s: float):
@@ -286,10 +296,13 @@ def run_ours(args, r, w, lr):
     hbm = hbm or 6800.0
     # dominant kernel: the persistent p' CG launch (one per outer iteration)
     b_iter = cg_bytes_per_iter(n, nnz)
-    spmv_b = nnz * 12 + 4 * (n + 1) + 16 * n
-    bytes_launch = [it * b_iter + spmv_b + 24 * n for it in cg_it]
+    init_b = nnz * 12 + 48 * n  # initial residual: matrix, x gathered, b, D^-1 read, r, z written
+    bytes_launch = [it * b_iter + init_b for it in cg_it]
     ach = [b / (ms / 1000.0) / 1e9 for b, ms in zip(bytes_launch, p_ms) if ms > 0]
     achieved = statistics.mean(ach) if ach else None
+    f_iter = cg_flops_per_iter(n, nnz)
+    dp = [it * f_iter / (ms / 1000.0) / 1e12 for it, ms in zip(cg_it, p_ms) if ms > 0]
+    dp_tflops = statistics.mean(dp) if dp else None
     traffic = None
     tp = os.path.join(ROOT, "profiles", "cg_pressure_traffic.json")
     if args.workload == "c3" and not args.p_mixed and os.path.exists(tp):
@@ -311,9 +324,15 @@ def run_ours(args, r, w, lr):
             m_ms += s.timer_stop()
             m_p.append(s.timing()[0])
             m_it.append(s.solve_stats()["p"]["iters"][0])
+        b32 = cg_bytes_per_iter(n, nnz, fp32=True)
+        init32 = nnz * 12 + 40 * n
+        ach32 = statistics.mean([(it * b32 + init32) / (ms / 1000.0) / 1e9 for it, ms in zip(m_it, m_p) if ms > 0])
         forms["mixed_fp32_fp64"] = {"iters_per_s": args.steps / (m_ms / 1000.0), "ms_per_step": m_ms / args.steps,
                                     "p_solve_ms_mean": statistics.mean(m_p),
-                                    "p_cg_inner_iters_mean": statistics.mean(m_it)}
+                                    "p_cg_inner_iters_mean": statistics.mean(m_it),
+                                    "roofline": {"bound": "hbm", "kernel": "k_cg_mixed_pipe", "achieved": ach32,
+                                                 "peak": hbm, "unit": "GB/s", "frac": ach32 / hbm,
+                                                 "algorithmic_bytes_per_cg_iteration": b32}}
         s.set_option("p.mixed", 0)
         # p' solve of outer iteration 1 to the 1e-8 relative residual, without the 1000 cap
         to8 = {}
@@ -339,10 +358,14 @@ def run_ours(args, r, w, lr):
         "e2e": {"value": w * args.steps / e2e_s, "unit": "iters/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": "k_cg (persistent Jacobi-PCG for p')",
+        "roofline": {"bound": "hbm", "kernel": "k_cg_pipe (persistent Jacobi-PCG for p')",
                      "achieved": achieved, "peak": hbm, "peak_source": peak_src, "unit": "GB/s",
                      "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
                      "algorithmic_bytes_per_cg_iteration": b_iter},
+        "fp64_pipe": {"kernel": "k_cg_pipe", "achieved_tflops": dp_tflops, "peak_tflops": FP64_PEAK_TFLOPS,
+                      "peak_source": "nominal GB300 FP64 rate (2 FMA lanes per SM per clock)",
+                      "frac": (dp_tflops / FP64_PEAK_TFLOPS) if dp_tflops else None,
+                      "flops_per_cg_iteration": f_iter},
         "p_solve_ms_mean": statistics.mean(p_ms), "p_cg_iters_mean": statistics.mean(cg_it),
         "mom_bicgstab_iters": mom_it[-1], "clocks": clocks, "forms": forms,
     }
