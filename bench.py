@@ -202,6 +202,33 @@ def run_reference(args, r, w):
     print(json.dumps(base))
 
 
+def spmv_bytes(n: int, nnz: int, sv: int) -> float:
+    """Algorithmic bytes of one y = A x: nnz (value + int32 column), N+1 row pointers,
+    x and y once each."""
+    return nnz * (sv + 4) + 4 * (n + 1) + 2 * n * sv
+
+
+def spmv_sweep(s, n: int, nnz: int, hbm: float, at=(1, 10, 100), reps: int = 10) -> dict:
+    """y = A x on the p' and momentum matrices as assembled after the given outer
+    iterations (FP64 values and their FP32 copy), L2 flushed before each product."""
+    out = {}
+    s.reset()
+    done = 0
+    for k in at:
+        s.iterate(k - done)
+        done = k
+        row = {}
+        for which in ("p", "mom"):
+            for fp32 in (False, True):
+                ms = s.spmv_timing(which, fp32, reps)
+                b = spmv_bytes(n, nnz, 4 if fp32 else 8)
+                gbs = b / (ms / 1000.0) / 1e9
+                row[f"{which}_{'fp32' if fp32 else 'fp64'}"] = {"ms": ms, "GB/s": gbs, "frac_of_hbm": gbs / hbm,
+                                                                 "algorithmic_bytes": b}
+        out[f"after_outer_iteration_{k}"] = row
+    return out
+
+
 def config_of(args):
     nx, ny, nz = WORKLOADS[args.workload]
     return {"workload": f"lid-driven cavity Re 400, {nx}x{ny}x{nz} hexes x 6 jittered tets "
@@ -349,6 +376,9 @@ def run_ours(args, r, w, lr):
         s.set_option("p.mixed", 0)
         s.set_option("p.maxit", 1000)
         forms["p_solve_to_1e-8_outer_iteration_1"] = to8
+
+    # standalone SpMV sweep on the assembled matrices after outer iterations 1, 10, 100
+    forms["spmv_sweep"] = spmv_sweep(s, n, nnz, hbm) if not args.p_maxit and not args.p_mixed else None
 
     out = {
         "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": w, "steps": args.steps,

@@ -96,6 +96,11 @@ long sysu_kernel_launches(void);
  * update, after the product + reduction and after the update + reduction --
  * 4 per iteration for the first 64 iterations (n <= 256). */
 int sysu_solver_cg_phases(sysu_solver *s, unsigned long long *out, int n);
+/* Standalone SpMV sweep on an assembled matrix ("mom", "p", "scalar", "solid"):
+ * *ms = mean device time of one y = A x (streaming SELL-32 kernel) over `reps`
+ * products on a fixed x, FP64 values or (fp32 != 0) their FP32 copy, with L2
+ * flushed before every product. */
+int sysu_solver_spmv_timing(sysu_solver *s, const char *which, int fp32, int reps, double *ms);
 /* Residual[0..9] of the last iteration (navier.h:65). */
 int sysu_solver_residuals(sysu_solver *s, double *out10);
 /* Per solve slot (mom u/v/w, p', k, eps, T, solid T): iterations, residual,

@@ -319,6 +319,14 @@ int sysu_solver_timer_stop(sysu_solver *s, double *ms) {
 
 long sysu_kernel_launches(void) { return sysu::g_launches.load(); }
 
+int sysu_solver_spmv_timing(sysu_solver *s, const char *which, int fp32, int reps, double *ms) {
+    if (!s || !which || !ms) return set_err(SYSU_ERR_INPUT, "null argument");
+    return guarded([&] {
+        *ms = s->impl->spmv_timing(which, fp32 != 0, reps);
+        return SYSU_OK;
+    });
+}
+
 int sysu_solver_cg_phases(sysu_solver *s, unsigned long long *out, int n) {
     if (!s || !out) return set_err(SYSU_ERR_INPUT, "null argument");
     return guarded([&] {

@@ -90,17 +90,52 @@ __device__ __forceinline__ void row_dot_scaled(const SellView &A, int i, const d
 }
 
 
-__global__ void k_spmv(SellView A, const double *__restrict__ x, double *__restrict__ y) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= A.n) return;
-    y[i] = row_dot(A, i, x);
-}
-
 __global__ void k_jacobi_apply(SellView A, double omega, const double *c, double *y) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= A.n) return;
     double d = A.val[A.sl_ptr[i >> 5] + (i & 31)];
     y[i] = omega * c[i] / d;
+}
+
+// Standalone SELL-32 product for the SpMV sweep: one row per thread, a warp per
+// slice; the matrix is streamed with evict-first loads (read once), all of a row's
+// entries are loaded before its FMAs, x is gathered through the read-only path.
+template <class V>
+__global__ void __launch_bounds__(256) k_spmv_stream(int n, const int *__restrict__ sl_ptr,
+                                                     const int *__restrict__ sl_w, const int *__restrict__ col,
+                                                     const V *__restrict__ val, const V *__restrict__ x,
+                                                     V *__restrict__ y) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int s = i >> 5;
+    int e = __ldg(sl_ptr + s) + (i & 31);
+    int w = __ldg(sl_w + s);
+    V acc = (V)0;
+    if (w <= 8) {
+        int c[8];
+        V a[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < w) {
+                c[k] = __ldcs(col + e + 32 * k);
+                a[k] = __ldcs(val + e + 32 * k);
+            }
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < w) acc = fma(a[k], __ldg(x + c[k]), acc);
+    } else {
+        for (int k = 0; k < w; ++k) acc = fma(__ldcs(val + e + 32 * k), __ldg(x + __ldcs(col + e + 32 * k)), acc);
+    }
+    y[i] = acc;
+}
+
+// A fixed, non-trivial x for the SpMV sweep: 1 + hash(i) / 2000.
+__global__ void k_fill_x(long n, double *x64, float *x32) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double v = 1.0 + 0.5 * (double)((i * 2654435761ull) % 1000) / 1000.0;
+    x64[i] = v;
+    x32[i] = (float)v;
 }
 
 __global__ void k_to_fp32(long n, const double *src, float *dst) {
@@ -339,9 +374,23 @@ void sell_to_fp32(const SellDev &A, const double *val, float *val32, cudaStream_
 }
 
 
-void spmv(const SellDev &A, const double *val, const double *x, double *y, cudaStream_t st) {
+void spmv(const SellDev &A, const double *val, const double *x, double *y, cudaStream_t st) { spmv_stream(A, val, x, y, st); }
+
+void fill_sweep_x(long n, double *x64, float *x32, cudaStream_t st) {
+    if (n == 0) return;
+    { k_fill_x<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, x64, x32); ++::sysu::g_launches; }
+    SYSU_CUDA(cudaGetLastError());
+}
+
+void spmv_stream(const SellDev &A, const double *val, const double *x, double *y, cudaStream_t st) {
     if (A.n == 0) return;
-    { k_spmv<<<(A.n + KB - 1) / KB, KB, 0, st>>>(view(A, val), x, y); ++::sysu::g_launches; }
+    { k_spmv_stream<double><<<(A.n + 255) / 256, 256, 0, st>>>(A.n, A.sl_ptr.get(), A.sl_w.get(), A.col.get(), val, x, y); ++::sysu::g_launches; }
+    SYSU_CUDA(cudaGetLastError());
+}
+
+void spmv_stream32(const SellDev &A, const float *val, const float *x, float *y, cudaStream_t st) {
+    if (A.n == 0) return;
+    { k_spmv_stream<float><<<(A.n + 255) / 256, 256, 0, st>>>(A.n, A.sl_ptr.get(), A.sl_w.get(), A.col.get(), val, x, y); ++::sysu::g_launches; }
     SYSU_CUDA(cudaGetLastError());
 }
 

@@ -99,6 +99,13 @@ void bicgstab_solve(const SellDev &A, const double *val, int nrhs, const double 
 // y = A x (standalone, for tests and the SpMV sweep).
 void spmv(const SellDev &A, const double *val, const double *x, double *y, cudaStream_t st);
 
+// y = A x with the matrix streamed once (evict-first loads), FP64 and FP32 values:
+// the standalone SpMV of the sweep.
+void spmv_stream(const SellDev &A, const double *val, const double *x, double *y, cudaStream_t st);
+void spmv_stream32(const SellDev &A, const float *val, const float *x, float *y, cudaStream_t st);
+// x of the sweep (FP64 and its FP32 copy).
+void fill_sweep_x(long n, double *x64, float *x32, cudaStream_t st);
+
 // y = omega D^-1 c (the Jacobi preconditioner applied once).
 void jacobi_apply(const SellDev &A, const double *val, double omega, const double *c, double *y, cudaStream_t st);
 

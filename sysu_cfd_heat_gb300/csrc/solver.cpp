@@ -605,6 +605,40 @@ double SimpleSolver::timer_stop() {
     return ms;
 }
 
+double SimpleSolver::spmv_timing(const std::string &which, bool fp32, int reps) {
+    const DomainDev *d = &fd;
+    const DevBuf<double> *v = nullptr;
+    if (which == "mom") v = &f.Amom;
+    else if (which == "p") v = &f.Ap;
+    else if (which == "scalar") v = &f.As;
+    else if (which == "solid" && cs.has_solid) { d = &sd; v = &s.As; }
+    else throw CaseError{"spmv_timing: unknown matrix " + which};
+    if (reps < 1) reps = 1;
+    const SellDev &A = d->A;
+    const size_t n = (size_t)A.n;
+    DevBuf<double> x64(n), y64(n);
+    DevBuf<float> x32(n), y32(n), v32;
+    DevBuf<unsigned char> flush((size_t)256 << 20);
+    fill_sweep_x((long)n, x64.get(), x32.get(), st);
+    if (fp32) {
+        v32.alloc((size_t)A.nnz);
+        sell_to_fp32(A, v->get(), v32.get(), st);
+    }
+    double total = 0.0;
+    for (int k = 0; k < reps + 1; ++k) {
+        SYSU_CUDA(cudaMemsetAsync(flush.get(), k & 0xff, flush.size(), st));
+        SYSU_CUDA(cudaEventRecord(ev[4], st));
+        if (fp32) spmv_stream32(A, v32.get(), x32.get(), y32.get(), st);
+        else spmv_stream(A, v->get(), x64.get(), y64.get(), st);
+        SYSU_CUDA(cudaEventRecord(ev[5], st));
+        SYSU_CUDA(cudaEventSynchronize(ev[5]));
+        float ms = 0.f;
+        SYSU_CUDA(cudaEventElapsedTime(&ms, ev[4], ev[5]));
+        if (k > 0) total += ms;  // the first product warms up
+    }
+    return total / reps;
+}
+
 // ---------------------------------------------------------------------------
 // Field access by the reference's member names.  kind: 0 cell, 1 cell gradient
 // (3 per cell, interleaved like double** rows), 2 face (reference face order),

@@ -120,6 +120,10 @@ class SimpleSolver {
     // CUDA events on the solver's stream around a region of work
     void timer_start();
     double timer_stop();  // ms; synchronises
+    // Standalone SpMV sweep on an assembled matrix ("mom", "p", "scalar", "solid"):
+    // mean device time (ms) of one y = A x over `reps` products, FP64 or FP32
+    // values, L2 flushed (256 MB write) before each product.
+    double spmv_timing(const std::string &which, bool fp32, int reps);
 
   private:
     void alloc_fields(FieldSet &fs, const DomainDev &d, bool solid);

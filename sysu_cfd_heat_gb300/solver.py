@@ -141,6 +141,12 @@ class NavierStokesSolver:
         check(lib().sysu_solver_timing(self._h, C.byref(p), C.byref(m)))
         return p.value, m.value
 
+    def spmv_timing(self, which: str = "p", fp32: bool = False, reps: int = 10) -> float:
+        """Mean device ms of one standalone y = A x on an assembled matrix (L2 flushed)."""
+        ms = C.c_double()
+        check(lib().sysu_solver_spmv_timing(self._h, which.encode(), int(fp32), int(reps), C.byref(ms)))
+        return ms.value
+
     def cg_phases(self) -> np.ndarray:
         """%globaltimer stamps (ns) of the last CG solve, shape (64, 4): iteration
         start, after the direction update, after the product, after the update
