@@ -24,10 +24,13 @@
  * GPU specifics: vectors stay in host memory (the caller reads and writes
  * Cmp[] directly); each iterator call uploads A (values only when the pattern
  * is unchanged), b and x, runs one persistent GPU solve and downloads x.
- * CGIter and BiCGSTABIter run those methods.  GMRESIter runs BiCGSTAB and
- * SSORPrecond / ILUPrecond apply the Jacobi preconditioner, unless
- * laspack_gpu_set_mode() selects otherwise; the substitution is reported once
- * on stderr.  The environment variable SYSU_LASPACK_RTC, when set, replaces
+ * CGIter, BiCGSTABIter and GMRESIter (restarted, SetGMRESRestart, default 10,
+ * at most 30) run those methods; JacobiPrecond, SSORPrecond and ILUPrecond
+ * (ILU(0)) run as given, the triangular sweeps level-scheduled in natural row
+ * order, except that BiCGSTABIter applies Jacobi in place of SSOR/ILU.
+ * laspack_gpu_set_mode() can substitute BiCGSTAB for GMRES and Jacobi for
+ * SSOR/ILU (faster, same solution to the tolerance); a substitution is reported
+ * once on stderr.  Any other preconditioner function is refused.  The environment variable SYSU_LASPACK_RTC, when set, replaces
  * the tolerance of every solve (for tight-tolerance comparisons).  Nothing here falls back to the CPU: without a GPU an iterator
  * leaves x unchanged and reports accuracy +inf, which the reference's own
  * checks treat as a failed solve.
@@ -103,7 +106,8 @@ Vector *SSORPrecond(QMatrix *A, Vector *y, Vector *c, double Omega);
 Vector *ILUPrecond(QMatrix *A, Vector *y, Vector *c, double Omega);
 
 /* ---- extensions (not LASPack) ------------------------------------------- */
-/* gmres_as: 1 = BiCGSTAB (default); ssor_as: 1 = Jacobi (default).  Returns 0. */
+/* gmres_as: 0 = GMRES (default), 1 = BiCGSTAB; ssor_as: 0 = SSOR/ILU as named
+ * (default), 1 = Jacobi.  Returns 0. */
 int laspack_gpu_set_mode(int gmres_as, int ssor_as);
 /* solves run through this ABI and the GPU iterations they took */
 long laspack_gpu_solves(void);

@@ -58,8 +58,13 @@ void sysu_solver_destroy(sysu_solver *s);
 /* out[0..5] = Ncel, Nfac, Nbnd, solid Ncel, matrix stored entries, matrix true entries */
 int sysu_solver_info(sysu_solver *s, long *out, int n);
 /* Options (defaults = the reference's call sites):
- *   "<eq>.eps" "<eq>.maxit" "<eq>.omega" "<eq>.kind" (0 CG, 1 BiCGSTAB)
- *     for eq in mom, p, ke, t, ts (solid T);
+ *   "<eq>.eps" "<eq>.maxit" "<eq>.omega" "<eq>.kind" (0 CG, 1 BiCGSTAB, 2 GMRES)
+ *     "<eq>.precond" (0 none, 1 Jacobi, 2 SSOR, 3 ILU(0); SSOR/ILU with CG and
+ *     GMRES) "<eq>.restart" (GMRES, 1..30) for eq in mom, p, ke, t, ts (solid T);
+ *   "reference_solvers" (1: the reference's own mode, GMRES(10) + SSOR for
+ *     momentum, k, eps, T and CG + SSOR for p' and solid T; the default mode
+ *     runs BiCGSTAB + Jacobi and CG + Jacobi, which reach the same solutions to
+ *     the tolerance and are faster on the GPU);
  *   "<eq>.mixed" (CG equations p, ts: FP32 inner CG in FP64 defect
  *     correction, stopping on the FP64 residual) and "<eq>.inner_tol";
  *   "rtc" sets every eq's eps; "mom_batched" (1: u,v,w as one 3-RHS solve);
@@ -127,9 +132,10 @@ long sysu_solver_matrix(sysu_solver *s, const char *which, int *rowptr, int *col
 
 /* ---- standalone sparse solves on the GPU ------------------------------------
  * The Krylov kernels of the SIMPLE path applied to a host CSR matrix (0-based,
- * any column order).  method: 0 CG, 1 BiCGSTAB, 2 CG with FP32 inner solves in
- * FP64 defect correction (Jacobi only; iters = inner iterations); precond: 0 none, 1 Jacobi
- * (y = omega D^-1 c).  Stopping test ||b - A x||_2 / ||b||_2 < eps, as the
+ * any column order).  method: 0 CG, 1 BiCGSTAB, 2 CG with FP32 recurrences and
+ * FP64 reliable updates (Jacobi only; iters = FP32 iterations), 3 GMRES(10)
+ * right preconditioned; precond: 0 none, 1 Jacobi (y = omega D^-1 c), 2 SSOR(omega),
+ * 3 ILU(0) (level-scheduled sweeps; not with BiCGSTAB).  Stopping test ||b - A x||_2 / ||b||_2 < eps, as the
  * reference's SolveLinearEqu (tools.cpp:56-64) expects.  x: x0 in, solution out.
  * status: 0 converged, 1 max iterations, 2 breakdown, 3 barrier timeout,
  * 4 non-finite. */

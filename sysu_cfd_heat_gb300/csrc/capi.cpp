@@ -163,6 +163,10 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
         return SYSU_OK;
     }
     if (k == "mom_batched") { o.mom_batched = value != 0.0; return SYSU_OK; }
+    if (k == "reference_solvers") {
+        if (value != 0.0) o.reference_solvers();
+        return SYSU_OK;
+    }
     if (k == "solid_source") { o.solid_source = value; return SYSU_OK; }
     if (k == "fatal_checks") { o.fatal_checks = value != 0.0; return SYSU_OK; }
     if (k == "timing") { o.timing = value != 0.0; return SYSU_OK; }
@@ -189,15 +193,38 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
             if (f == "mixed") {
                 if (value != 0.0 && e->kind != sysu::SK_CG)
                     return set_err(SYSU_ERR_INPUT, "mixed precision is available for CG solves (p, ts)");
+                if (value != 0.0 && e->precond != sysu::PK_JACOBI)
+                    return set_err(SYSU_ERR_INPUT, "the mixed-precision CG uses the Jacobi preconditioner");
                 e->mixed = value != 0.0;
                 return SYSU_OK;
             }
             if (f == "inner_tol") { e->inner_tol = value; return SYSU_OK; }
             if (f == "kind") {
                 int kind = (int)value;
-                if (kind != sysu::SK_CG && kind != sysu::SK_BICGSTAB) return set_err(SYSU_ERR_INPUT, "kind: 0 CG, 1 BiCGSTAB");
+                if (kind != sysu::SK_CG && kind != sysu::SK_BICGSTAB && kind != sysu::SK_GMRES)
+                    return set_err(SYSU_ERR_INPUT, "kind: 0 CG, 1 BiCGSTAB, 2 GMRES");
                 if (kind == sysu::SK_CG && e == &o.mom) return set_err(SYSU_ERR_INPUT, "momentum matrix is not symmetric");
+                if (kind == sysu::SK_BICGSTAB && e->precond > sysu::PK_JACOBI)
+                    return set_err(SYSU_ERR_INPUT, "BiCGSTAB runs with no or the Jacobi preconditioner");
+                if (kind != sysu::SK_CG) e->mixed = 0;
                 e->kind = kind;
+                return SYSU_OK;
+            }
+            if (f == "precond") {
+                int pc = (int)value;
+                if (pc < sysu::PK_NONE || pc > sysu::PK_ILU0)
+                    return set_err(SYSU_ERR_INPUT, "precond: 0 none, 1 Jacobi, 2 SSOR, 3 ILU(0)");
+                if (pc > sysu::PK_JACOBI && e->kind == sysu::SK_BICGSTAB)
+                    return set_err(SYSU_ERR_INPUT, "BiCGSTAB runs with no or the Jacobi preconditioner");
+                if (pc != sysu::PK_JACOBI && e->mixed)
+                    return set_err(SYSU_ERR_INPUT, "the mixed-precision CG uses the Jacobi preconditioner");
+                e->precond = pc;
+                return SYSU_OK;
+            }
+            if (f == "restart") {
+                int m = (int)value;
+                if (m < 1 || m > sysu::GMRES_MAX_RESTART) return set_err(SYSU_ERR_INPUT, "restart: 1..30");
+                e->restart = m;
                 return SYSU_OK;
             }
         }
@@ -224,6 +251,8 @@ int sysu_solver_get_option(sysu_solver *s, const char *key, double *value) {
             if (f == "omega") { *value = e->omega; return SYSU_OK; }
             if (f == "kind") { *value = e->kind; return SYSU_OK; }
             if (f == "mixed") { *value = e->mixed; return SYSU_OK; }
+            if (f == "precond") { *value = e->precond; return SYSU_OK; }
+            if (f == "restart") { *value = e->restart; return SYSU_OK; }
             if (f == "inner_tol") { *value = e->inner_tol; return SYSU_OK; }
         }
     }

@@ -61,7 +61,8 @@ thread_local std::string g_csr_err;
 
 extern "C" {
 
-// method: 0 CG, 1 BiCGSTAB; precond: 0 none, 1 Jacobi (omega D^-1).
+// method: 0 CG, 1 BiCGSTAB, 2 CG with FP32 recurrences (Jacobi), 3 GMRES(10);
+// precond: 0 none, 1 Jacobi (omega D^-1), 2 SSOR(omega), 3 ILU(0).
 // x holds x0 on entry and the solution on return.  Returns 0, or an error.
 int sysu_csr_solve(int method, int precond, int n, const int *rowptr, const int *col, const double *val,
                    const double *b, double *x, int maxit, double eps, double omega, int *iters, double *res,
@@ -82,17 +83,25 @@ int sysu_csr_solve(int method, int precond, int n, const int *rowptr, const int 
             o.eps = eps;
             o.omega = omega;
             o.jacobi = precond == 1;
-            if (method == 0) {
+            if (precond < 0 || precond > 3) throw sysu::CaseError{"precond: 0 none, 1 Jacobi, 2 SSOR, 3 ILU(0)"};
+            if (method == 1 && precond > 1) throw sysu::CaseError{"BiCGSTAB runs with no or the Jacobi preconditioner"};
+            if (method == 0 && precond > 1) {
+                sysu::pcg_solve(M.A, M.val.get(), db.get(), dx.get(), false, o, precond, w, info.get(), st);
+            } else if (method == 0) {
                 sysu::cg_solve(M.A, M.val.get(), db.get(), dx.get(), false, o, w, info.get(), st);
+            } else if (method == 3) {
+                sysu::gmres_solve(M.A, M.val.get(), db.get(), dx.get(), false, o, precond, 10, w, info.get(), st);
             } else if (method == 2) {
                 if (precond != 1) throw sysu::CaseError{"the mixed-precision CG uses the Jacobi preconditioner"};
                 sysu::DevBuf<float> v32(M.A.nnz);
                 sysu::sell_to_fp32(M.A, M.val.get(), v32.get(), st);
                 sysu::cg_solve_mixed(M.A, M.val.get(), v32.get(), db.get(), dx.get(), false, o, w, info.get(), st);
-            } else {
+            } else if (method == 1) {
                 const double *bb[1] = {db.get()};
                 double *xx[1] = {dx.get()};
                 sysu::bicgstab_solve(M.A, M.val.get(), 1, bb, xx, o, w, info.get(), st);
+            } else {
+                throw sysu::CaseError{"method: 0 CG, 1 BiCGSTAB, 2 CG-mixed, 3 GMRES"};
             }
             sysu::SolveInfo h;
             info.download(&h, 1, st);

@@ -65,6 +65,46 @@ void SellDev::upload(const SellPattern &p, cudaStream_t s) {
     sl_ptr.upload(p.sl_ptr, s);
     sl_w.upload(p.sl_w, s);
     col.upload(p.col, s);
+    // level schedule of the triangular sweeps (natural row order)
+    std::vector<int> lf(p.n, 0), lb(p.n, 0);
+    int nf = 0, nb = 0;
+    for (int i = 0; i < p.n; ++i) {
+        int l = 0;
+        for (int k = 1; k < p.row_len[i]; ++k) {
+            int j = p.col[p.pos(i, k)];
+            if (j < i) l = std::max(l, lf[j] + 1);
+        }
+        lf[i] = l;
+        nf = std::max(nf, l + 1);
+    }
+    for (int i = p.n - 1; i >= 0; --i) {
+        int l = 0;
+        for (int k = 1; k < p.row_len[i]; ++k) {
+            int j = p.col[p.pos(i, k)];
+            if (j > i) l = std::max(l, lb[j] + 1);
+        }
+        lb[i] = l;
+        nb = std::max(nb, l + 1);
+    }
+    auto group = [&](const std::vector<int> &lv, int nl, std::vector<int> &ptr, std::vector<int> &rows) {
+        ptr.assign(nl + 1, 0);
+        for (int i = 0; i < p.n; ++i) ptr[lv[i] + 1]++;
+        for (int l = 0; l < nl; ++l) ptr[l + 1] += ptr[l];
+        rows.assign(p.n, 0);
+        std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+        for (int i = 0; i < p.n; ++i) rows[fill[lv[i]]++] = i;
+    };
+    std::vector<int> fp, fr, bp, br;
+    if (p.n > 0) {
+        group(lf, nf, fp, fr);
+        group(lb, nb, bp, br);
+    }
+    lev.nf = p.n > 0 ? nf : 0;
+    lev.nb = p.n > 0 ? nb : 0;
+    lev.fptr.upload(fp, s);
+    lev.frows.upload(fr, s);
+    lev.bptr.upload(bp, s);
+    lev.brows.upload(br, s);
 }
 
 namespace {

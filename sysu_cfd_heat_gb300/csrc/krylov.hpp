@@ -33,11 +33,22 @@ struct SellPattern {
 // Build a SELL-32 pattern from per-row column lists (diagonal first).
 SellPattern make_sell(int n, const std::vector<int> &row_ptr, const std::vector<int> &cols);
 
+// Level schedule of a pattern in natural row order, for the triangular sweeps of
+// SSOR and ILU(0): forward level of row i = 1 + the largest forward level among
+// its columns j < i; backward level = 1 + the largest among its columns j > i.
+// Rows of one level do not depend on each other.  Rows are stored grouped by
+// level (ascending row number inside a level).
+struct LevelSchedule {
+    int nf = 0, nb = 0;  // number of forward / backward levels
+    DevBuf<int> fptr, frows, bptr, brows;
+};
+
 struct SellDev {
     int n = 0, nslices = 0;
     int wmax = 0;      // widest slice (entries per row incl. padding)
     long nnz = 0, nnz_true = 0;
     DevBuf<int> sl_ptr, sl_w, col;
+    LevelSchedule lev;
     void upload(const SellPattern &p, cudaStream_t s);
 };
 
@@ -61,6 +72,8 @@ struct KrylovWork {
     int n = 0, nrhs = 0, max_blocks = 0;
     DevBuf<double> r, rt, p, v, s, t, dinv, partials;
     DevBuf<float> r32, z32, p32, q32, e32, dinv32;  // mixed-precision inner solve
+    DevBuf<double> gV, gZ, gW, ilu;                  // GMRES basis, preconditioned basis, ILU(0) factors
+    DevBuf<long long> gpart;                         // exact multi-value partial sums
     DevBuf<GridBarrier> barrier;
     unsigned long long *phase_ts = nullptr;  // optional: 4 timestamps per CG iteration, first 64
     void ensure(int n, int nrhs, int max_blocks, cudaStream_t st);
@@ -74,6 +87,27 @@ struct KrylovOpts {
     bool jacobi = true;       // false: no preconditioner
     double inner_tol = 0.1;   // mixed precision: FP32 residual drop that triggers a reliable update
 };
+
+// Preconditioners of the general solvers (LASPack's JacobiPrecond, SSORPrecond,
+// ILUPrecond; none = identity).
+enum PrecondKind { PK_NONE = 0, PK_JACOBI = 1, PK_SSOR = 2, PK_ILU0 = 3 };
+constexpr int GMRES_MAX_RESTART = 30;
+
+// Restarted GMRES(m), right preconditioned (the oracle's LASPack restatement:
+// Saad Alg. 9.5 with Givens rotations), classical Gram-Schmidt applied twice with
+// exact deterministic grid sums; stopping test ||b - A x|| / ||b|| < eps, checked
+// on the true residual at the end of a cycle.  restart in 1..GMRES_MAX_RESTART.
+void gmres_solve(const SellDev &A, const double *val, const double *b, double *x, bool x0_zero,
+                 const KrylovOpts &o, int precond, int restart, KrylovWork &w, SolveInfo *info_dev,
+                 cudaStream_t st);
+
+// Preconditioned CG with any PrecondKind (Templates Fig. 2.5).
+void pcg_solve(const SellDev &A, const double *val, const double *b, double *x, bool x0_zero,
+               const KrylovOpts &o, int precond, KrylovWork &w, SolveInfo *info_dev, cudaStream_t st);
+
+// y = M^-1 c once (the LASPack preconditioner entry points).
+void precond_solve(const SellDev &A, const double *val, int precond, double omega, const double *c, double *y,
+                   KrylovWork &w, SolveInfo *info_dev, cudaStream_t st);
 
 // Copy FP64 SELL values to FP32 (same pattern).
 void sell_to_fp32(const SellDev &A, const double *val, float *val32, cudaStream_t st);

@@ -44,7 +44,8 @@ struct State {
     double eps = 1e-8;
     int last_iter = 0;
     double last_acc = 0.0;
-    int gmres_as = 1, ssor_as = 1;
+    int gmres_as = 0, ssor_as = 0;  // laspack_gpu_set_mode: 0 = the named method
+    int restart = 10;               // SetGMRESRestart
     long solves = 0, iters = 0;
     bool warned_gmres = false, warned_ssor = false, warned_err = false;
     cudaStream_t st = nullptr;
@@ -131,6 +132,16 @@ DevMatrix &matrix_for(State &s, const Pattern &p) {
 
 enum { M_CG = 0, M_BICGSTAB = 1, M_GMRES = 2 };
 
+// The preconditioner a LASPack iterator was given, by address: these three
+// (and none) run on the GPU; any other function is refused (no CPU fallback).
+int precond_kind(PrecondProcType pc) {
+    if (pc == nullptr) return PK_NONE;
+    if (pc == JacobiPrecond) return PK_JACOBI;
+    if (pc == SSORPrecond) return PK_SSOR;
+    if (pc == ILUPrecond) return PK_ILU0;
+    throw CaseError{"unknown preconditioner function: only JacobiPrecond, SSORPrecond, ILUPrecond run on the GPU"};
+}
+
 Vector *run_iter(int method, QMatrix *A, Vector *x, Vector *b, int MaxIter, PrecondProcType pc, double Omega) {
     State &s = S();
     std::lock_guard<std::mutex> lock(s.mu);
@@ -154,20 +165,36 @@ Vector *run_iter(int method, QMatrix *A, Vector *x, Vector *b, int MaxIter, Prec
         o.eps = s.eps;
         if (const char *ov = std::getenv("SYSU_LASPACK_RTC")) o.eps = std::atof(ov);
         o.omega = Omega;
-        o.jacobi = pc != nullptr;
-        if ((pc == SSORPrecond || pc == ILUPrecond) && s.ssor_as == 1 && !s.warned_ssor) {
-            std::fprintf(stderr, "laspack (GPU): SSOR/ILU preconditioners run as Jacobi on the GPU\n");
-            s.warned_ssor = true;
+        int kind = precond_kind(pc);
+        if ((kind == PK_SSOR || kind == PK_ILU0) && s.ssor_as == 1) {
+            if (!s.warned_ssor) {
+                std::fprintf(stderr, "laspack (GPU): SSOR/ILU preconditioners run as Jacobi (laspack_gpu_set_mode)\n");
+                s.warned_ssor = true;
+            }
+            kind = PK_JACOBI;
         }
-        if (method == M_GMRES) {
+        if (method == M_GMRES && s.gmres_as == 1) {
             if (!s.warned_gmres) {
-                std::fprintf(stderr, "laspack (GPU): GMRESIter runs BiCGSTAB on the GPU\n");
+                std::fprintf(stderr, "laspack (GPU): GMRESIter runs BiCGSTAB (laspack_gpu_set_mode)\n");
                 s.warned_gmres = true;
             }
             method = M_BICGSTAB;
         }
+        if (method == M_BICGSTAB && (kind == PK_SSOR || kind == PK_ILU0)) {
+            if (!s.warned_ssor) {
+                std::fprintf(stderr, "laspack (GPU): BiCGSTABIter applies the Jacobi preconditioner\n");
+                s.warned_ssor = true;
+            }
+            kind = PK_JACOBI;
+        }
+        o.jacobi = kind == PK_JACOBI;
         if (method == M_CG) {
-            cg_solve(m.A, m.val.get(), m.b.get(), m.x.get(), false, o, s.work, s.info.get(), s.st);
+            if (kind == PK_JACOBI || kind == PK_NONE)
+                cg_solve(m.A, m.val.get(), m.b.get(), m.x.get(), false, o, s.work, s.info.get(), s.st);
+            else
+                pcg_solve(m.A, m.val.get(), m.b.get(), m.x.get(), false, o, kind, s.work, s.info.get(), s.st);
+        } else if (method == M_GMRES) {
+            gmres_solve(m.A, m.val.get(), m.b.get(), m.x.get(), false, o, kind, s.restart, s.work, s.info.get(), s.st);
         } else {
             const double *bb[1] = {m.b.get()};
             double *xx[1] = {m.x.get()};
@@ -195,7 +222,7 @@ Vector *run_iter(int method, QMatrix *A, Vector *x, Vector *b, int MaxIter, Prec
     return x;
 }
 
-Vector *precond_apply(QMatrix *A, Vector *y, Vector *c, double Omega) {
+Vector *precond_apply(int kind, QMatrix *A, Vector *y, Vector *c, double Omega) {
     State &s = S();
     std::lock_guard<std::mutex> lock(s.mu);
     try {
@@ -211,9 +238,14 @@ Vector *precond_apply(QMatrix *A, Vector *y, Vector *c, double Omega) {
             for (int k = p.rowptr[i]; k < p.rowptr[i + 1]; ++k) m.hval[m.pat.pos(i, k - p.rowptr[i])] = vals[k];
         m.val.upload(m.hval.data(), m.hval.size(), s.st);
         m.b.upload(c->Cmp + 1, p.n, s.st);
-        jacobi_apply(m.A, m.val.get(), Omega, m.b.get(), m.y.get(), s.st);
+        if ((kind == PK_SSOR || kind == PK_ILU0) && s.ssor_as == 1) kind = PK_JACOBI;
+        precond_solve(m.A, m.val.get(), kind, Omega, m.b.get(), m.y.get(), s.work, s.info.get(), s.st);
+        SolveInfo h;
+        s.info.download(&h, 1, s.st);
         m.y.download(y->Cmp + 1, p.n, s.st);
         SYSU_CUDA(cudaStreamSynchronize(s.st));
+        if (h.err) throw CaseError{"preconditioner aborted: a grid barrier wait timed out"};
+        if (h.status[1]) throw CaseError{"ILU(0): zero pivot or row longer than 16 entries"};
     } catch (const CaseError &e) {
         std::fprintf(stderr, "laspack (GPU): preconditioner failed: %s\n", e.msg.c_str());
         for (size_t i = 1; i <= y->Dim; ++i) y->Cmp[i] = NAN;
@@ -285,7 +317,10 @@ void V_SetAllCmp(Vector *V, Real C) {
 void SetRTCAccuracy(double NewEps) { S().eps = NewEps; }
 int GetLastNoIter(void) { return S().last_iter; }
 double GetLastAccuracy(void) { return S().last_acc; }
-void SetGMRESRestart(int) {}
+void SetGMRESRestart(int MaxSteps) {
+    State &s = S();
+    s.restart = MaxSteps < 1 ? 10 : (MaxSteps > GMRES_MAX_RESTART ? GMRES_MAX_RESTART : MaxSteps);
+}
 
 Vector *CGIter(QMatrix *A, Vector *x, Vector *b, int MaxIter, PrecondProcType Precond, double Omega) {
     return run_iter(M_CG, A, x, b, MaxIter, Precond, Omega);
@@ -297,9 +332,11 @@ Vector *GMRESIter(QMatrix *A, Vector *x, Vector *b, int MaxIter, PrecondProcType
     return run_iter(M_GMRES, A, x, b, MaxIter, Precond, Omega);
 }
 
-Vector *JacobiPrecond(QMatrix *A, Vector *y, Vector *c, double Omega) { return precond_apply(A, y, c, Omega); }
-Vector *SSORPrecond(QMatrix *A, Vector *y, Vector *c, double Omega) { return precond_apply(A, y, c, Omega); }
-Vector *ILUPrecond(QMatrix *A, Vector *y, Vector *c, double Omega) { return precond_apply(A, y, c, Omega); }
+Vector *JacobiPrecond(QMatrix *A, Vector *y, Vector *c, double Omega) {
+    return precond_apply(PK_JACOBI, A, y, c, Omega);
+}
+Vector *SSORPrecond(QMatrix *A, Vector *y, Vector *c, double Omega) { return precond_apply(PK_SSOR, A, y, c, Omega); }
+Vector *ILUPrecond(QMatrix *A, Vector *y, Vector *c, double Omega) { return precond_apply(PK_ILU0, A, y, c, Omega); }
 
 int laspack_gpu_set_mode(int gmres_as, int ssor_as) {
     S().gmres_as = gmres_as;

@@ -326,10 +326,21 @@ void SimpleSolver::solve(int slot, const EqOpts &o, const SellDev &A, const doub
     ko.maxit = o.maxit;
     ko.eps = o.eps;
     ko.omega = o.omega;
-    ko.jacobi = true;
+    ko.jacobi = o.precond == PK_JACOBI;
     SolveInfo *info = infos.get() + slot;
+    if (o.kind == SK_GMRES) {
+        // one restarted GMRES per right-hand side (the reference solves u, v, w in turn)
+        for (int c = 0; c < nrhs; ++c)
+            gmres_solve(A, val, b[c], x[c], x0_zero, ko, o.precond, o.restart, kw,
+                        nrhs == 1 ? info : infos.get() + SLOT_N + c, st);
+        return;
+    }
     if (o.kind == SK_CG) {
         if (nrhs != 1) throw CaseError{"CG solves one right-hand side"};
+        if (o.precond == PK_SSOR || o.precond == PK_ILU0) {
+            pcg_solve(A, val, b[0], x[0], x0_zero, ko, o.precond, kw, info, st);
+            return;
+        }
         if (o.mixed) {
             // FP32 copy of this equation's matrix, then FP32 inner / FP64 outer CG
             DevBuf<float> &v32 = (&A == &sd.A) ? s.As32 : f.Ap32;
@@ -543,7 +554,7 @@ std::string SimpleSolver::check_iteration() {
     red_out.download(ro, RED_NSLOT, st);
     flags.download(&hf, 1, st);
     SYSU_CUDA(cudaStreamSynchronize(st));
-    if (!opt.mom_batched)
+    if (!opt.mom_batched || opt.mom.kind == SK_GMRES)
         for (int c = 0; c < 3; ++c) {
             h[SLOT_MOM].status[c] = h[SLOT_N + c].status[0];
             h[SLOT_MOM].iters[c] = h[SLOT_N + c].iters[0];

@@ -28,7 +28,7 @@ struct DomainDev {
 };
 
 // Solver choice per equation (the reference hard-codes them per call site).
-enum SolverKind { SK_CG = 0, SK_BICGSTAB = 1 };
+enum SolverKind { SK_CG = 0, SK_BICGSTAB = 1, SK_GMRES = 2 };
 
 struct EqOpts {
     int kind = SK_BICGSTAB;
@@ -37,6 +37,8 @@ struct EqOpts {
     double omega = 1.2;
     int mixed = 0;            // CG only: FP32 inner solves in FP64 defect correction
     double inner_tol = 0.1;   // FP32 residual drop between reliable updates
+    int precond = PK_JACOBI;  // PrecondKind (SSOR and ILU with CG and GMRES)
+    int restart = 10;         // GMRES restart length
 };
 
 struct SolverOptions {
@@ -49,6 +51,20 @@ struct SolverOptions {
     EqOpts ke{SK_BICGSTAB, 500, 1e-8, 1.3};
     EqOpts t{SK_BICGSTAB, 500, 1e-8, 1.3};
     EqOpts ts{SK_CG, 500, 1e-8, 1.3};
+    // the reference's own solver mode: GMRES(10) + SSOR for momentum and scalars,
+    // CG + SSOR for p' and solid conduction (option "reference_solvers")
+    void reference_solvers() {
+        for (EqOpts *e : {&mom, &ke, &t}) {
+            e->kind = SK_GMRES;
+            e->precond = PK_SSOR;
+        }
+        for (EqOpts *e : {&p, &ts}) {
+            e->kind = SK_CG;
+            e->precond = PK_SSOR;
+            e->mixed = 0;
+        }
+        mom_batched = false;
+    }
     bool mom_batched = true;      // u, v, w as one 3-RHS solve
     double solid_source = 0.0;    // W/m^3 (extension; the reference has none)
     bool fatal_checks = true;     // the reference's convergence checks
