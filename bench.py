@@ -377,6 +377,20 @@ def run_ours(args, r, w, lr):
         s.set_option("p.maxit", 1000)
         forms["p_solve_to_1e-8_outer_iteration_1"] = to8
 
+    # the reference's own solver mode (GMRES(10) + SSOR, CG + SSOR), outer iteration 1
+    if not args.p_maxit and not args.p_mixed:
+        s.set_option("reference_solvers", 1)
+        s.reset()
+        s.timer_start()
+        s.iterate(1)
+        ms_ref = s.timer_stop()
+        st = s.solve_stats()
+        forms["reference_solver_mode_outer_iteration_1"] = {
+            "ms": ms_ref, "solvers": "momentum GMRES(10)+SSOR(1.2) per component, p' CG+SSOR(1.3), level-scheduled",
+            "mom_gmres_iters": st["mom"]["iters"], "p_cg_ssor_iters": st["p"]["iters"][0],
+            "p_rel_residual": st["p"]["res"][0]}
+        s.set_option("reference_solvers", 0)
+
     # standalone SpMV sweep on the assembled matrices after outer iterations 1, 10, 100
     forms["spmv_sweep"] = spmv_sweep(s, n, nnz, hbm) if not args.p_maxit and not args.p_mixed else None
 

@@ -49,6 +49,11 @@ int sysu_case_info(const sysu_case *c, long *out, int n);
  * Returns the array's size in bytes (or -1 for an unknown name); copies
  * min(size, nbytes) bytes when out is non-null. */
 long sysu_case_array(const sysu_case *c, const char *name, void *out, long nbytes);
+/* The Tecplot writer on host arrays (no GPU): fields by name "P" "U" "V" "W" "R"
+ * "T" "VisLam" "VisTur" (required), "TE" "ED" (turbulence ke), "solid_T" (CHT),
+ * in reference cell order. */
+int sysu_case_write_tecplot(const sysu_case *c, const char *path, int nfields, const char *const *names,
+                            const double *const *arrays);
 
 /* ---- GPU solver ------------------------------------------------------------
  * create: main.cpp:14-28 (read, build, CellFaceInfo, CheckAndAllocate,
@@ -62,9 +67,9 @@ int sysu_solver_info(sysu_solver *s, long *out, int n);
  *     "<eq>.precond" (0 none, 1 Jacobi, 2 SSOR, 3 ILU(0); SSOR/ILU with CG and
  *     GMRES) "<eq>.restart" (GMRES, 1..30) for eq in mom, p, ke, t, ts (solid T);
  *   "reference_solvers" (1: the reference's own mode, GMRES(10) + SSOR for
- *     momentum, k, eps, T and CG + SSOR for p' and solid T; the default mode
- *     runs BiCGSTAB + Jacobi and CG + Jacobi, which reach the same solutions to
- *     the tolerance and are faster on the GPU);
+ *     momentum, k, eps, T and CG + SSOR for p' and solid T; 0: back to the
+ *     default mode, BiCGSTAB + Jacobi and CG + Jacobi, which reach the same
+ *     solutions to the tolerance and are faster on the GPU);
  *   "<eq>.mixed" (CG equations p, ts: FP32 inner CG in FP64 defect
  *     correction, stopping on the FP64 residual) and "<eq>.inner_tol";
  *   "rtc" sets every eq's eps; "mom_batched" (1: u,v,w as one 3-RHS solve);
@@ -75,8 +80,19 @@ int sysu_solver_get_option(sysu_solver *s, const char *key, double *value);
  * pressure, k-epsilon, energy and solid conduction as configured.  Stops
  * early when max(Residual) < ResidualSteady.  *done = iterations run. */
 int sysu_solver_iterate(sysu_solver *s, int n, int *done);
-/* NSSolve itself: MaxOuterStep-1 iterations with the steady break. */
+/* NSSolve itself: MaxOuterStep-1 iterations with the steady break.  With option
+ * "output" on it also writes what the reference writes next to param.in:
+ * tot.dat (header, then one VolumnAverage line), tec/res%04lu.dat every
+ * `output, N` iterations (navier.cpp:59-61,104-110) and once at the end. */
 int sysu_solver_nssolve(sysu_solver *s, int *done);
+/* NavierStokesSolver::Output (navier.cpp:264-337, plus the solid zone of
+ * HeatConductionSolver.cpp:330-361): <dir>/tec/res%04lu.dat, numbered per
+ * solver from 0, text identical to the reference's.  dir NULL = the directory
+ * of param.in. */
+int sysu_solver_output(sysu_solver *s, const char *dir);
+/* NavierStokesSolver::VolumnAverage (navier.cpp:243-261): one line appended to
+ * <dir>/tot.dat (created with the reference's header when missing). */
+int sysu_solver_volume_average(sysu_solver *s, const char *dir, double t, int out_iter);
 /* The individual methods, enqueued on the solver's stream (navier.h:103-116):
  * CalculateVelocity, CalculatePressure, UpdateTurKEpsilon, UpdateEnergy,
  * HeatConductionSolver::solve.  sysu_solver_check() then reads the residuals

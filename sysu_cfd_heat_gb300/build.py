@@ -18,7 +18,7 @@ LIB = os.path.join(PKG, "libsysucfd.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SRCS = ["krylov.cu", "cg.cu", "gmres.cu", "fv.cu", "noalloc.cu"]
-CPP_SRCS = ["case.cpp", "solver.cpp", "capi.cpp", "csr_api.cpp", "laspack_gpu.cpp"]
+CPP_SRCS = ["case.cpp", "solver.cpp", "capi.cpp", "csr_api.cpp", "laspack_gpu.cpp", "output.cpp"]
 
 
 def _cuda_home() -> str:

@@ -5,7 +5,10 @@
 #include <exception>
 #include <string>
 
+#include <fstream>
+#include <limits>
 #include "handles.hpp"
+#include "output.hpp"
 
 namespace {
 thread_local std::string g_err;
@@ -165,11 +168,13 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
     if (k == "mom_batched") { o.mom_batched = value != 0.0; return SYSU_OK; }
     if (k == "reference_solvers") {
         if (value != 0.0) o.reference_solvers();
+        else o.default_solvers();
         return SYSU_OK;
     }
     if (k == "solid_source") { o.solid_source = value; return SYSU_OK; }
     if (k == "fatal_checks") { o.fatal_checks = value != 0.0; return SYSU_OK; }
     if (k == "timing") { o.timing = value != 0.0; return SYSU_OK; }
+    if (k == "output") { o.output = value != 0.0; return SYSU_OK; }
     if (k == "profile_phases") {
         return guarded([&] {
             sysu::SimpleSolver &S = *s->impl;
@@ -240,6 +245,7 @@ int sysu_solver_get_option(sysu_solver *s, const char *key, double *value) {
     if (k == "solid_source") { *value = o.solid_source; return SYSU_OK; }
     if (k == "fatal_checks") { *value = o.fatal_checks; return SYSU_OK; }
     if (k == "timing") { *value = o.timing; return SYSU_OK; }
+    if (k == "output") { *value = o.output; return SYSU_OK; }
     if (k == "profile_phases") { *value = o.profile_phases; return SYSU_OK; }
     size_t dot = k.find('.');
     if (dot != std::string::npos) {
@@ -286,7 +292,78 @@ int sysu_solver_iterate(sysu_solver *s, int n, int *done) {
 
 int sysu_solver_nssolve(sysu_solver *s, int *done) {
     if (!s) return set_err(SYSU_ERR_INPUT, "null argument");
-    return guarded([&] { return run_iterations(s, s->impl->cs.params.max_outer_step - 1, done); });
+    sysu::SimpleSolver &S = *s->impl;
+    if (!S.opt.output) return guarded([&] { return run_iterations(s, S.cs.params.max_outer_step - 1, done); });
+    // navier.cpp:13-97 for a steady case, with its writers: tot.dat header
+    // (constructor), Output() every noutput iterations and at the end,
+    // VolumnAverage(cur_time = DBL_MAX, iter) after the loop.
+    return guarded([&] {
+        const std::string dir = S.case_dir;
+        sysu::write_tot_header(dir + "/tot.dat");
+        const int last = S.cs.params.max_outer_step;
+        const int nout = S.cs.params.noutput > 0 ? S.cs.params.noutput : 1;
+        int iter = 1;
+        for (; iter < last; ++iter) {
+            std::string msg = S.outer_iteration();
+            if (!msg.empty()) {
+                if (done) *done = iter;
+                return set_err(SYSU_ERR_SOLVE, msg);
+            }
+            if ((iter - 1) % nout == 0) S.output(dir);
+            double resmax = 0.0;
+            for (double r : S.Residual) resmax = resmax > r ? resmax : r;
+            if (S.cs.params.steady && resmax < S.cs.params.residual_steady) break;
+        }
+        if (done) *done = iter < last ? iter : last - 1;
+        S.volume_average(dir, std::numeric_limits<double>::max(), iter);
+        S.output(dir);
+        return SYSU_OK;
+    });
+}
+
+int sysu_solver_output(sysu_solver *s, const char *dir) {
+    if (!s) return set_err(SYSU_ERR_INPUT, "null argument");
+    return guarded([&] {
+        s->impl->output(dir ? std::string(dir) : s->impl->case_dir);
+        return SYSU_OK;
+    });
+}
+
+int sysu_solver_volume_average(sysu_solver *s, const char *dir, double t, int out_iter) {
+    if (!s) return set_err(SYSU_ERR_INPUT, "null argument");
+    return guarded([&] {
+        std::string d = dir ? std::string(dir) : s->impl->case_dir;
+        std::ifstream probe(d + "/tot.dat");
+        if (!probe.good()) sysu::write_tot_header(d + "/tot.dat");
+        s->impl->volume_average(d, t, out_iter);
+        return SYSU_OK;
+    });
+}
+
+int sysu_case_write_tecplot(const sysu_case *c, const char *path, int nfields, const char *const *names,
+                            const double *const *arrays) {
+    if (!c || !path || (nfields > 0 && (!names || !arrays))) return set_err(SYSU_ERR_INPUT, "null argument");
+    return guarded([&] {
+        sysu::TecFields f;
+        for (int k = 0; k < nfields; ++k) {
+            std::string nm(names[k]);
+            const double *a = arrays[k];
+            if (nm == "P") f.P = a;
+            else if (nm == "U") f.U = a;
+            else if (nm == "V") f.V = a;
+            else if (nm == "W") f.W = a;
+            else if (nm == "R") f.R = a;
+            else if (nm == "T") f.T = a;
+            else if (nm == "VisLam") f.VisLam = a;
+            else if (nm == "VisTur") f.VisTur = a;
+            else if (nm == "TE") f.TE = a;
+            else if (nm == "ED") f.ED = a;
+            else if (nm == "solid_T") f.solid_T = a;
+            else throw sysu::CaseError{"write_tecplot: unknown field " + nm};
+        }
+        sysu::write_tecplot(c->cs, path, f);
+        return SYSU_OK;
+    });
 }
 
 #define SYSU_METHOD(cname, call)                                                  \

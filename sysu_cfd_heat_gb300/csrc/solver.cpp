@@ -3,6 +3,10 @@
 // of the residual monitor and the solve status words in check_iteration().
 #include "solver.hpp"
 
+#include <sys/stat.h>
+
+#include "output.hpp"
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -169,6 +173,10 @@ void DomainDev::build(const Domain &d, const Params &p, cudaStream_t st) {
 
 // ---------------------------------------------------------------------------
 SimpleSolver::SimpleSolver(const std::string &param_path) {
+    {
+        size_t slash = param_path.find_last_of('/');
+        case_dir = slash == std::string::npos ? "." : param_path.substr(0, slash);
+    }
     cs.params = parse_params(param_path);
     std::string grid = cs.params.gridfile;
     RawMesh raw;
@@ -614,6 +622,36 @@ double SimpleSolver::timer_stop() {
     float ms = 0.f;
     SYSU_CUDA(cudaEventElapsedTime(&ms, ev[4], ev[5]));
     return ms;
+}
+
+void SimpleSolver::output(const std::string &dir) {
+    std::string tec = dir + "/tec";
+    ::mkdir(tec.c_str(), 0755);  // the reference expects tec/ to exist
+    char name[64];
+    std::snprintf(name, sizeof name, "/res%04lu.dat", output_counter++);
+    const long n = fd.nc;
+    std::vector<std::vector<double>> h(10, std::vector<double>((size_t)n));
+    const char *names[10] = {"P", "U", "V", "W", "R", "T", "VisLam", "VisTur", "TE", "ED"};
+    for (int k = 0; k < 10; ++k) get_field(names[k], h[k].data(), n);
+    TecFields f;
+    f.P = h[0].data(); f.U = h[1].data(); f.V = h[2].data(); f.W = h[3].data(); f.R = h[4].data();
+    f.T = h[5].data(); f.VisLam = h[6].data(); f.VisTur = h[7].data(); f.TE = h[8].data(); f.ED = h[9].data();
+    std::vector<double> ts;
+    if (cs.has_solid) {
+        ts.resize((size_t)sd.nc);
+        get_field("solid_T", ts.data(), sd.nc);
+        f.solid_T = ts.data();
+    }
+    write_tecplot(cs, tec + name, f);
+}
+
+void SimpleSolver::volume_average(const std::string &dir, double t, int out_iter) {
+    const long n = fd.nc;
+    std::vector<double> R((size_t)n), P((size_t)n), T((size_t)n);
+    get_field("R", R.data(), n);
+    get_field("P", P.data(), n);
+    get_field("T", T.data(), n);
+    append_tot_line(cs, dir + "/tot.dat", t, out_iter, R.data(), P.data(), T.data());
 }
 
 double SimpleSolver::spmv_timing(const std::string &which, bool fp32, int reps) {

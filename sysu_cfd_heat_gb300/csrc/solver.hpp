@@ -65,11 +65,24 @@ struct SolverOptions {
         }
         mom_batched = false;
     }
+    // back to the default (fast) mode: BiCGSTAB + Jacobi, CG + Jacobi, batched momentum
+    void default_solvers() {
+        for (EqOpts *e : {&mom, &ke, &t}) {
+            e->kind = SK_BICGSTAB;
+            e->precond = PK_JACOBI;
+        }
+        for (EqOpts *e : {&p, &ts}) {
+            e->kind = SK_CG;
+            e->precond = PK_JACOBI;
+        }
+        mom_batched = true;
+    }
     bool mom_batched = true;      // u, v, w as one 3-RHS solve
     double solid_source = 0.0;    // W/m^3 (extension; the reference has none)
     bool fatal_checks = true;     // the reference's convergence checks
     bool timing = false;          // CUDA events around the p' solve
     bool profile_phases = false;  // %globaltimer stamps at the CG phase boundaries
+    bool output = false;          // nssolve writes tec/res####.dat and tot.dat like the reference
 };
 
 enum SolveSlot { SLOT_MOM = 0, SLOT_P, SLOT_K, SLOT_EPS, SLOT_T, SLOT_TS, SLOT_N };
@@ -136,6 +149,12 @@ class SimpleSolver {
     // CUDA events on the solver's stream around a region of work
     void timer_start();
     double timer_stop();  // ms; synchronises
+    // Output(): tec/res%04lu.dat in `dir` (numbered by output_counter), and
+    // VolumnAverage(t, out_iter): one line of `dir`/tot.dat.
+    void output(const std::string &dir);
+    void volume_average(const std::string &dir, double t, int out_iter);
+    std::string case_dir;       // directory of param.in
+    unsigned long output_counter = 0;
     // Standalone SpMV sweep on an assembled matrix ("mom", "p", "scalar", "solid"):
     // mean device time (ms) of one y = A x over `reps` products, FP64 or FP32
     // values, L2 flushed (256 MB write) before each product.

@@ -80,6 +80,16 @@ class NavierStokesSolver:
         check(lib().sysu_solver_nssolve(self._h, C.byref(done)))
         return done.value
 
+    def Output(self, directory: str = None) -> None:
+        """NavierStokesSolver::Output: tec/res####.dat (numbered from 0) in `directory`
+        (default: the directory of param.in), text identical to the reference's."""
+        check(lib().sysu_solver_output(self._h, directory.encode() if directory else None))
+
+    def VolumnAverage(self, t: float, out_iter: int, directory: str = None) -> None:
+        """NavierStokesSolver::VolumnAverage: one line of tot.dat (header when new)."""
+        check(lib().sysu_solver_volume_average(self._h, directory.encode() if directory else None, float(t),
+                                               int(out_iter)))
+
     def iterate(self, n: int) -> int:
         """Run up to n steady outer iterations (stops at the steady convergence test)."""
         done = C.c_int()
