@@ -80,7 +80,10 @@ int sysu_solver_get_option(sysu_solver *s, const char *key, double *value);
  * pressure, k-epsilon, energy and solid conduction as configured.  Stops
  * early when max(Residual) < ResidualSteady.  *done = iterations run. */
 int sysu_solver_iterate(sysu_solver *s, int n, int *done);
-/* NSSolve itself: MaxOuterStep-1 iterations with the steady break.  With option
+/* NSSolve itself.  Steady: MaxOuterStep-1 iterations with the steady break.
+ * Transient ("transient, dt, total, Euler|Dual, MaxOuterStep"): time steps of
+ * outer iterations with the reference's break rule (navier.cpp:29-88);
+ * *done = outer iterations run in all steps.  With option
  * "output" on it also writes what the reference writes next to param.in:
  * tot.dat (header, then one VolumnAverage line), tec/res%04lu.dat every
  * `output, N` iterations (navier.cpp:59-61,104-110) and once at the end. */
@@ -102,6 +105,10 @@ int sysu_solver_calculate_pressure(sysu_solver *s);
 int sysu_solver_update_turkeps(sysu_solver *s);
 int sysu_solver_update_energy(sysu_solver *s);
 int sysu_solver_heat_conduction(sysu_solver *s);
+/* CycasSolver::SaveTransientOldData of the fluid and the solid module
+ * (navier.cpp:190-240, HeatConductionSolver.cpp:306-327): the current fields
+ * become the previous time level (a transient case; no-op when steady). */
+int sysu_solver_save_transient_old_data(sysu_solver *s);
 int sysu_solver_check(sysu_solver *s);
 /* Back to the state right after creation (InitFlowField); keeps the mesh,
  * matrices and options. */

@@ -319,5 +319,9 @@ int main(int argc, char **argv) {
     if (tf) std::fclose(tf);
     if (!g_dump.empty()) dump_fields(g_dump, ns);
     std::fprintf(stderr, "driver: %d outer iterations done\n", done);
+    // main.cpp ends without deleting the solver, which leaves the buffered tail
+    // of tot.dat unwritten; after NSSolve the driver deletes it so the file is
+    // complete (the destructor closes it, navier.cpp:420-432)
+    if (nssolve) delete ns;
     return 0;
 }

@@ -290,9 +290,45 @@ int sysu_solver_iterate(sysu_solver *s, int n, int *done) {
     return guarded([&] { return run_iterations(s, n, done); });
 }
 
+// The transient NSSolve (navier.cpp:20-90): per time step SaveTransientOldData,
+// then outer iterations until max(Residual) < 1e-4 or it fell 1000-fold since the
+// step's first iteration (at most MaxOuterStep-1), VolumnAverage, advance time.
+static int run_transient(sysu_solver *s, int *done) {
+    sysu::SimpleSolver &S = *s->impl;
+    const sysu::Params &p = S.cs.params;
+    const std::string dir = S.case_dir;
+    if (S.opt.output) sysu::write_tot_header(dir + "/tot.dat");
+    double cur_time = p.dt;
+    int total = 0;
+    for (int step = 1; step <= p.max_step; ++step) {
+        S.save_transient_old_data();
+        double resmax0 = 0.0;
+        int iter = 1;
+        for (; iter < p.max_outer_step; ++iter) {
+            std::string msg = S.outer_iteration();
+            ++total;
+            if (!msg.empty()) {
+                if (done) *done = total;
+                return set_err(SYSU_ERR_SOLVE, msg);
+            }
+            double resmax = 0.0;
+            for (double r : S.Residual) resmax = resmax > r ? resmax : r;
+            if (iter == 1) resmax0 = resmax;
+            if (resmax < 1.e-4 || resmax0 / (resmax + 1.e-16) > 1000.) break;
+        }
+        if (S.opt.output) S.volume_average(dir, cur_time, iter);
+        if (cur_time >= p.total_time) break;
+        cur_time += p.dt;
+    }
+    if (S.opt.output) S.output(dir);
+    if (done) *done = total;
+    return SYSU_OK;
+}
+
 int sysu_solver_nssolve(sysu_solver *s, int *done) {
     if (!s) return set_err(SYSU_ERR_INPUT, "null argument");
     sysu::SimpleSolver &S = *s->impl;
+    if (!S.cs.params.steady) return guarded([&] { return run_transient(s, done); });
     if (!S.opt.output) return guarded([&] { return run_iterations(s, S.cs.params.max_outer_step - 1, done); });
     // navier.cpp:13-97 for a steady case, with its writers: tot.dat header
     // (constructor), Output() every noutput iterations and at the end,
@@ -380,6 +416,7 @@ SYSU_METHOD(sysu_solver_calculate_pressure, calculate_pressure())
 SYSU_METHOD(sysu_solver_update_turkeps, update_ke())
 SYSU_METHOD(sysu_solver_update_energy, update_energy())
 SYSU_METHOD(sysu_solver_sync, sync())
+SYSU_METHOD(sysu_solver_save_transient_old_data, save_transient_old_data())
 
 int sysu_solver_heat_conduction(sysu_solver *s) {
     if (!s) return set_err(SYSU_ERR_INPUT, "null argument");

@@ -381,6 +381,20 @@ __global__ void k_mom_cell(DomView d, MomArgs a) {
     if (i >= d.nc) return;
     const int nc = d.nc;
     double app = 0., su = 0., sv = 0., sw = 0.;
+    if (a.tscheme) {  // unsteady terms first, navier_velocity.cpp:103-118
+        double coef = a.R[i] / a.dt * d.vol[i];
+        if (a.tscheme == 1) {
+            app += coef;
+            su += coef * a.Unp[i];
+            sv += coef * a.Vnp[i];
+            sw += coef * a.Wnp[i];
+        } else {
+            app += 1.5 * coef;
+            su += coef * (2 * a.Unp[i] - 0.5 * a.Unp[i]);
+            sv += coef * (2 * a.Vnp[i] - 0.5 * a.Vnp[i]);
+            sw += coef * (2 * a.Wnp[i] - 0.5 * a.Wnp[i]);
+        }
+    }
     for (int s = d.cs_ptr[i]; s < d.cs_ptr[i + 1]; ++s) {
         int f = d.cs_face[s];
         if (f < d.F) {
@@ -825,6 +839,20 @@ __global__ void k_cht_f2s(DomView fl, const double *gTf, const double *kcond, do
     Bq_s[s.ncb + k] = 0. - q;
 }
 
+__global__ void k_time_term(int n, const double *R, const double *vol, double dt, int scheme, const double *old,
+                            double *app, double *src) {
+    int i = blockIdx.x * NB + threadIdx.x;
+    if (i >= n) return;
+    double coef = R[i] / dt * vol[i];
+    if (scheme == 1) {
+        app[i] += coef;
+        src[i] += coef * old[i];
+    } else {
+        app[i] += 1.5 * coef;
+        src[i] += coef * (2 * old[i] - 0.5 * old[i]);
+    }
+}
+
 __global__ void k_fill(double *x, double v, int n) {
     int i = blockIdx.x * NB + threadIdx.x;
     if (i < n) x[i] = v;
@@ -987,6 +1015,13 @@ void launch_cht_fluid2solid(const DomView &f, const double *gTf, const double *k
     { k_cht_f2s<<<nblk(n), NB, 0, st>>>(f, gTf, kcond, Bq_f, s, Bq_s); ++::sysu::g_launches; }
     CHECK_LAUNCH();
 }
+void launch_time_term(int n, const double *R, const double *vol, double dt, int scheme, const double *old,
+                      double *app, double *src, cudaStream_t st) {
+    if (n <= 0 || scheme == 0) return;
+    { k_time_term<<<nblk(n), NB, 0, st>>>(n, R, vol, dt, scheme, old, app, src); ++::sysu::g_launches; }
+    CHECK_LAUNCH();
+}
+
 void launch_fill(double *x, double v, int n, cudaStream_t st) {
     if (n <= 0) return;
     { k_fill<<<nblk(n), NB, 0, st>>>(x, v, n); ++::sysu::g_launches; }

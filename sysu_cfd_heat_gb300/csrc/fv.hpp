@@ -87,8 +87,13 @@ struct MomArgs {
     double *bu, *bv, *bw;  // right-hand sides
     double *Apr;
     int *flags;            // error flags (e.g. unknown boundary type)
+    // transient terms (navier_velocity.cpp:103-118): tscheme 0 steady, 1 Euler,
+    // 2 "Dual" (BDF2 with the reference's old levels, both equal to the last step)
+    const double *Unp = nullptr, *Vnp = nullptr, *Wnp = nullptr;
+    double dt = 0.0;
+    int tscheme = 0;
 };
-// BuildVelocityMatrix, navier_velocity.cpp:77-357 (steady)
+// BuildVelocityMatrix, navier_velocity.cpp:77-357
 void launch_momentum(const DomView &d, const MomArgs &a, cudaStream_t st);
 
 // L1 change residual and commit: res += sum |old - new| * vol, old = new
@@ -165,6 +170,12 @@ void launch_cht_fluid2solid(const DomView &f, const double *gTf, const double *k
                             const DomView &s, double *Bq_s, cudaStream_t st);
 
 void launch_fill(double *x, double v, int n, cudaStream_t st);
+// Transient term of a cell equation (navier_scalar.cpp:72-89,350-366,
+// HeatConductionSolver.cpp:66-80): coef = R/dt * vol; Euler: app += coef,
+// src += coef phi_old; scheme 2: app += 1.5 coef, src += coef (2 phi_old - 0.5 phi_old2)
+// with phi_old2 = phi_old (SaveTransientOldData sets both levels to the last step).
+void launch_time_term(int n, const double *R, const double *vol, double dt, int scheme, const double *phi_old,
+                      double *app, double *src, cudaStream_t st);
 void launch_copy(double *dst, const double *src, int n, cudaStream_t st);
 void launch_scale_src(double *dst, const double *vol, double q, int n, cudaStream_t st);  // dst = q*vol
 

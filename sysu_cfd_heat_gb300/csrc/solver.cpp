@@ -191,7 +191,6 @@ SimpleSolver::SimpleSolver(const std::string &param_path) {
     }
     const Params &p = cs.params;
     if (p.density_model != 0) throw CaseError{"density model 1 (ideal gas) is not supported by the GPU path"};
-    if (!p.steady) throw CaseError{"transient runs are not supported by the GPU path yet"};
     if (p.heat_conduction && !p.solve_energy)
         throw CaseError{"must turn on SolveEnergy, if Solve3DHeatConduction is on"};
     build_case(raw, cs);
@@ -233,9 +232,16 @@ void SimpleSolver::alloc_fields(FieldSet &fs, const DomainDev &d, bool solid) {
     z(fs.T, nc); z(fs.R, nc); z(fs.dPhi, 3 * nc); z(fs.BTem, B); z(fs.Bq, B); z(fs.As, nnz);
     z(fs.bs, nc); z(fs.xs, nc); z(fs.fD, F); z(fs.fE, 3 * F); z(fs.bapp, B); z(fs.bsrc, 3 * B);
     z(fs.zeros, nc); z(fs.src, nc); z(fs.tmp3, 3 * nc); z(fs.tmpv, 2 * (size_t)std::max(d.nv, 1));
+    if (!cs.params.steady) {
+        z(fs.Tnp, nc);
+        z(fs.tapp, nc);
+    }
     if (solid) {
         z(fs.diff, nc);
         return;
+    }
+    if (!cs.params.steady) {
+        z(fs.Unp, nc); z(fs.Vnp, nc); z(fs.Wnp, nc); z(fs.TEp, nc); z(fs.EDp, nc);
     }
     z(fs.U, nc); z(fs.V, nc); z(fs.W, nc); z(fs.P, nc); z(fs.TE, nc); z(fs.ED, nc);
     z(fs.VisLam, nc); z(fs.VisTur, nc); z(fs.Apr, nc);
@@ -391,6 +397,11 @@ void SimpleSolver::calculate_velocity() {
     for (int k = 0; k < 3; ++k) a.g[k] = p.gravity[k];
     a.fD = f.fD.get(); a.fE = f.fE.get(); a.bapp = f.bapp.get(); a.bsrc = f.bsrc.get();
     a.val = f.Amom.get();
+    a.tscheme = tscheme();
+    if (a.tscheme) {
+        a.Unp = f.Unp.get(); a.Vnp = f.Vnp.get(); a.Wnp = f.Wnp.get();
+        a.dt = p.dt;
+    }
     a.bu = f.b3.get(); a.bv = f.b3.get() + nc; a.bw = f.b3.get() + 2 * (size_t)nc;
     a.Apr = f.Apr.get();
     a.flags = flags.get();
@@ -453,6 +464,10 @@ void SimpleSolver::update_ke() {
     k.VisED = f.VisED.get(); k.ApTE = f.ApTE.get(); k.ApED = f.ApED.get(); k.BTE = f.BTE.get(); k.BED = f.BED.get();
     launch_ke_sources(d, k, st);
     launch_ke_bnd_values(d, k, st);
+    // unsteady terms after the boundary treatment (navier_scalar.cpp:72-89); the
+    // eps source is recomputed after the k solve, so only its diagonal keeps it
+    launch_time_term(nc, f.R.get(), fd.vol.get(), p.dt, tscheme(), f.TEp.get(), f.ApTE.get(), f.TESrc.get(), st);
+    launch_time_term(nc, f.R.get(), fd.vol.get(), p.dt, tscheme(), f.EDp.get(), f.ApED.get(), f.EDSrc.get(), st);
     ScalarArgs sa{};
     sa.RUFace = f.RUFace.get(); sa.grad = f.dPhi.get(); sa.urf = p.urf[5]; sa.bc_mode = SC_FLUID_PLAIN;
     sa.fD = f.fD.get(); sa.fE = f.fE.get(); sa.bapp = f.bapp.get(); sa.bsrc = f.bsrc.get();
@@ -502,6 +517,13 @@ void SimpleSolver::update_energy() {
     grad_limited(fd, f, 1, phi, Bphi, grad);
     ScalarArgs sa{};
     sa.phi = f.T.get(); sa.Bphi = f.BTem.get(); sa.diff = f.kcond.get(); sa.src = f.zeros.get(); sa.app0 = f.zeros.get();
+    if (tscheme()) {  // navier_scalar.cpp:350-366
+        launch_fill(f.src.get(), 0.0, nc, st);
+        launch_fill(f.tapp.get(), 0.0, nc, st);
+        launch_time_term(nc, f.R.get(), fd.vol.get(), p.dt, tscheme(), f.Tnp.get(), f.tapp.get(), f.src.get(), st);
+        sa.src = f.src.get();
+        sa.app0 = f.tapp.get();
+    }
     sa.grad = f.dPhi.get(); sa.RUFace = f.RUFace.get(); sa.Bq = f.Bq.get(); sa.urf = p.urf[5];
     sa.bc_mode = SC_FLUID_ENERGY;
     sa.fD = f.fD.get(); sa.fE = f.fE.get(); sa.bapp = f.bapp.get(); sa.bsrc = f.bsrc.get();
@@ -529,6 +551,12 @@ void SimpleSolver::solid_solve() {
     grad_limited(sd, s, 1, phi, Bphi, grad);
     ScalarArgs sa{};
     sa.phi = s.T.get(); sa.Bphi = s.BTem.get(); sa.diff = s.diff.get(); sa.src = s.src.get(); sa.app0 = s.zeros.get();
+    if (tscheme()) {  // HeatConductionSolver.cpp:66-80 (solid density)
+        launch_fill(s.tapp.get(), 0.0, nc, st);
+        launch_time_term(nc, s.R.get(), sd.vol.get(), cs.params.dt, tscheme(), s.Tnp.get(), s.tapp.get(),
+                         s.src.get(), st);
+        sa.app0 = s.tapp.get();
+    }
     sa.grad = s.dPhi.get(); sa.RUFace = nullptr; sa.Bq = s.Bq.get(); sa.urf = 1.0;  // Preprocessor.cpp:506
     sa.bc_mode = SC_SOLID;
     sa.fD = s.fD.get(); sa.fE = s.fE.get(); sa.bapp = s.bapp.get(); sa.bsrc = s.bsrc.get();
@@ -539,6 +567,18 @@ void SimpleSolver::solid_solve() {
     double *x[1] = {s.xs.get()};
     solve(SLOT_TS, opt.ts, sd.A, s.As.get(), 1, b, x, false);
     launch_copy(s.T.get(), s.xs.get(), nc, st);
+}
+
+void SimpleSolver::save_transient_old_data() {
+    if (!tscheme()) return;
+    int nc = fd.nc;
+    launch_copy(f.Unp.get(), f.U.get(), nc, st);
+    launch_copy(f.Vnp.get(), f.V.get(), nc, st);
+    launch_copy(f.Wnp.get(), f.W.get(), nc, st);
+    launch_copy(f.Tnp.get(), f.T.get(), nc, st);
+    launch_copy(f.TEp.get(), f.TE.get(), nc, st);
+    launch_copy(f.EDp.get(), f.ED.get(), nc, st);
+    if (cs.has_solid) launch_copy(s.Tnp.get(), s.T.get(), sd.nc, st);
 }
 
 std::string SimpleSolver::outer_iteration() {

@@ -98,6 +98,7 @@ struct FieldSet {
     DevBuf<double> Prod, TESrc, EDSrc, VisTE, VisED, ApTE, ApED, kcond, zeros, src;
     DevBuf<double> tmp3, tmpv;
     DevBuf<double> diff;  // solid conductivity
+    DevBuf<double> Unp, Vnp, Wnp, Tnp, TEp, EDp, tapp;  // transient: last step's fields, time-term diagonal
     DevBuf<float> Ap32, As32;  // FP32 copies for mixed-precision solves
 };
 
@@ -135,6 +136,9 @@ class SimpleSolver {
     void update_ke();
     void update_energy();
     void solid_solve();
+    // SaveTransientOldData (navier.cpp:190-240, HeatConductionSolver.cpp:306-327)
+    void save_transient_old_data();
+    int tscheme() const { return cs.params.steady ? 0 : cs.params.time_scheme; }
     // one NSSolve loop body; syncs once, updates Residual and the solve infos,
     // returns a non-empty message when a reference convergence check fails
     std::string outer_iteration();

@@ -105,6 +105,9 @@ class NavierStokesSolver:
     def UpdateTurKEpsilon(self) -> None:
         check(lib().sysu_solver_update_turkeps(self._h))
 
+    def SaveTransientOldData(self) -> None:
+        check(lib().sysu_solver_save_transient_old_data(self._h))
+
     def UpdateEnergy(self) -> None:
         check(lib().sysu_solver_update_energy(self._h))
 
