@@ -320,8 +320,8 @@ int main(int argc, char **argv) {
     if (!g_dump.empty()) dump_fields(g_dump, ns);
     std::fprintf(stderr, "driver: %d outer iterations done\n", done);
     // main.cpp ends without deleting the solver, which leaves the buffered tail
-    // of tot.dat unwritten; after NSSolve the driver deletes it so the file is
-    // complete (the destructor closes it, navier.cpp:420-432)
-    if (nssolve) delete ns;
+    // of tot.dat unwritten; after NSSolve the driver flushes the (public) stream
+    // the destructor would close (navier.cpp:420-432)
+    if (nssolve) ns->totFile.flush();
     return 0;
 }

@@ -552,8 +552,12 @@ void SimpleSolver::solid_solve() {
     ScalarArgs sa{};
     sa.phi = s.T.get(); sa.Bphi = s.BTem.get(); sa.diff = s.diff.get(); sa.src = s.src.get(); sa.app0 = s.zeros.get();
     if (tscheme()) {  // HeatConductionSolver.cpp:66-80 (solid density)
+        // Always Euler: NavierStokesSolver declares its own TimeScheme (navier.h:29),
+        // so the copy that seeds the solid (Preprocessor.cpp:466-468) carries the
+        // base-class default 1 (BasicSolver.cpp:10) while IfSteady and dt come
+        // across; a "Dual" case steps the solid with the Euler term.
         launch_fill(s.tapp.get(), 0.0, nc, st);
-        launch_time_term(nc, s.R.get(), sd.vol.get(), cs.params.dt, tscheme(), s.Tnp.get(), s.tapp.get(),
+        launch_time_term(nc, s.R.get(), sd.vol.get(), cs.params.dt, 1, s.Tnp.get(), s.tapp.get(),
                          s.src.get(), st);
         sa.app0 = s.tapp.get();
     }
