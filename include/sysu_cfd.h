@@ -190,6 +190,47 @@ int sysu_csr_cg_noalloc(int n, const int *d_rowptr, const int *d_col, const doub
                         int *status);
 const char *sysu_noalloc_last_error(void);
 
+/* ---- learned preconditioner (message-passing network) -----------------------
+ * No counterpart in the reference: a 4-layer, width-32 message-passing network
+ * over the graph of a symmetric matrix (for the p' systems: the cell-face
+ * graph), BF16 weights with FP32 accumulation on the tensor cores, used as the
+ * preconditioner of flexible CG.  z = s (u + w_d . h4 + b_d) with u = D^-1 r / s
+ * and s = rms(D^-1 r); with zero decoder weights it is the Jacobi
+ * preconditioner.  Parameters: a flat FP32 vector of sysu_gnn_num_params()
+ * values, layout [e(32) c(32)] [W_l (64 x 32, input-major) b_l (32)] x 4
+ * [w_d(32) b_d].  The handle owns a stream and the matrix on the device.
+ * Training pairs (r, e = A^-1 r) go into a ring of `capacity` pairs; each
+ * training step is one Adam step (beta 0.9 / 0.999) on one pair, in the
+ * order the pairs were added; loss_kind 0 = energy norm of the error,
+ * 1 = residual norm.  All calls return 0 or an error code (message in
+ * sysu_gnn_last_error()). */
+typedef struct sysu_gnn sysu_gnn;
+int sysu_gnn_num_params(void);
+int sysu_gnn_create(int n, const int *rowptr, const int *col, const double *val, int capacity, sysu_gnn **out);
+void sysu_gnn_free(sysu_gnn *g);
+int sysu_gnn_init_params(sysu_gnn *g, unsigned long long seed);
+int sysu_gnn_set_params(sysu_gnn *g, const float *p, int np);
+int sysu_gnn_get_params(sysu_gnn *g, float *p, int np);
+/* z = M(r), host vectors of n values. */
+int sysu_gnn_apply(sysu_gnn *g, const double *r, double *z);
+int sysu_gnn_add_pair(sysu_gnn *g, const double *r, const double *e);
+/* loss and gradient (np values) of pair k, no update */
+int sysu_gnn_loss_grad(sysu_gnn *g, int k, int loss_kind, double *loss, float *grad, int np);
+/* `steps` Adam steps cycling over the stored pairs; losses[steps] (may be NULL) */
+int sysu_gnn_train(sysu_gnn *g, int steps, double lr, int loss_kind, double *losses);
+/* Flexible CG (FP32 recurrences, FP64 reliable updates every inner_tol drop of
+ * the residual) with the network (use_gnn = 1) or Jacobi as preconditioner.
+ * Jacobi takes over when the network stalls for stall_max iterations or a
+ * direction loses positivity (fallback_at = iteration, else -1).  Stops on
+ * ||b - A x||_2 / ||b||_2 < eps.  x: x0 in (ignored if x0_zero), solution out.
+ * seconds: device time of the solve (CUDA events). */
+int sysu_gnn_fcg(sysu_gnn *g, const double *b, double *x, int x0_zero, int maxit, double eps, double inner_tol,
+                 int use_gnn, int stall_max, int *iters, double *res, int *status, int *fallback_at,
+                 int *refinements, double *seconds);
+/* hidden state h^layer (layer 1..4) of the network on r, FP32 [n][32] */
+int sysu_gnn_hidden(sysu_gnn *g, const double *r, int layer, float *h);
+const char *sysu_gnn_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -30,6 +30,7 @@ def lib() -> C.CDLL:
             raise ImportError(f"{LIB_PATH} is missing: build it with python -m sysu_cfd_heat_gb300.build")
         L = C.CDLL(LIB_PATH)
         vp, cp, ip, dp, lp = C.c_void_p, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_long)
+        fp = C.POINTER(C.c_float)
         sig = {
             "sysu_last_error": (cp, []),
             "sysu_version": (C.c_int, []),
@@ -71,6 +72,20 @@ def lib() -> C.CDLL:
                                          C.c_double, ip, dp, ip]),
             "sysu_csr_spmv": (C.c_int, [C.c_int, ip, ip, dp, dp, dp]),
             "sysu_csr_last_error": (cp, []),
+            "sysu_gnn_num_params": (C.c_int, []),
+            "sysu_gnn_create": (C.c_int, [C.c_int, ip, ip, dp, C.c_int, C.POINTER(vp)]),
+            "sysu_gnn_free": (None, [vp]),
+            "sysu_gnn_init_params": (C.c_int, [vp, C.c_ulonglong]),
+            "sysu_gnn_set_params": (C.c_int, [vp, fp, C.c_int]),
+            "sysu_gnn_get_params": (C.c_int, [vp, fp, C.c_int]),
+            "sysu_gnn_apply": (C.c_int, [vp, dp, dp]),
+            "sysu_gnn_add_pair": (C.c_int, [vp, dp, dp]),
+            "sysu_gnn_loss_grad": (C.c_int, [vp, C.c_int, C.c_int, dp, fp, C.c_int]),
+            "sysu_gnn_train": (C.c_int, [vp, C.c_int, C.c_double, C.c_int, dp]),
+            "sysu_gnn_fcg": (C.c_int, [vp, dp, dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int,
+                                       ip, dp, ip, ip, ip, dp]),
+            "sysu_gnn_hidden": (C.c_int, [vp, dp, C.c_int, fp]),
+            "sysu_gnn_last_error": (cp, []),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
