@@ -72,6 +72,12 @@ int sysu_solver_info(sysu_solver *s, long *out, int n);
  *     solutions to the tolerance and are faster on the GPU);
  *   "<eq>.mixed" (CG equations p, ts: FP32 inner CG in FP64 defect
  *     correction, stopping on the FP64 residual) and "<eq>.inner_tol";
+ *   "p.learned" (1: the p' CG with the learned preconditioner -- the first
+ *     "p.learn_iters" solves run the plain method and train the network on
+ *     their residual/correction pairs, "p.learn_steps" Adam steps each at rate
+ *     "p.learn_lr" with loss "p.learn_kind" (0 energy norm, 1 residual norm);
+ *     later solves run flexible CG with the network, see sysu_gnn_fcg; the
+ *     network survives sysu_solver_reset; read-only "p.learned_solves");
  *   "rtc" sets every eq's eps; "mom_batched" (1: u,v,w as one 3-RHS solve);
  *   "solid_source" (W/m^3, an extension); "fatal_checks"; "timing". */
 int sysu_solver_set_option(sysu_solver *s, const char *key, double value);
@@ -208,6 +214,8 @@ typedef struct sysu_gnn sysu_gnn;
 int sysu_gnn_num_params(void);
 int sysu_gnn_create(int n, const int *rowptr, const int *col, const double *val, int capacity, sysu_gnn **out);
 void sysu_gnn_free(sysu_gnn *g);
+/* new matrix values with the pattern given to sysu_gnn_create (same rowptr, col) */
+int sysu_gnn_set_values(sysu_gnn *g, const int *rowptr, const int *col, const double *val);
 int sysu_gnn_init_params(sysu_gnn *g, unsigned long long seed);
 int sysu_gnn_set_params(sysu_gnn *g, const float *p, int np);
 int sysu_gnn_get_params(sysu_gnn *g, float *p, int np);

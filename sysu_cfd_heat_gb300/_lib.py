@@ -75,6 +75,7 @@ def lib() -> C.CDLL:
             "sysu_gnn_num_params": (C.c_int, []),
             "sysu_gnn_create": (C.c_int, [C.c_int, ip, ip, dp, C.c_int, C.POINTER(vp)]),
             "sysu_gnn_free": (None, [vp]),
+            "sysu_gnn_set_values": (C.c_int, [vp, ip, ip, dp]),
             "sysu_gnn_init_params": (C.c_int, [vp, C.c_ulonglong]),
             "sysu_gnn_set_params": (C.c_int, [vp, fp, C.c_int]),
             "sysu_gnn_get_params": (C.c_int, [vp, fp, C.c_int]),

@@ -1,6 +1,7 @@
 // C ABI of libsysucfd.so (declared in include/sysu_cfd.h).
 #include "../../include/sysu_cfd.h"
 
+#include <algorithm>
 #include <cstring>
 #include <exception>
 #include <string>
@@ -232,6 +233,21 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
                 e->restart = m;
                 return SYSU_OK;
             }
+            if (f == "learned") {
+                if (value != 0.0 && (e != &o.p || e->kind != sysu::SK_CG || e->precond != sysu::PK_JACOBI))
+                    return set_err(SYSU_ERR_INPUT, "the learned preconditioner is for the p' CG (Jacobi mode)");
+                e->learned = value != 0.0;
+                return SYSU_OK;
+            }
+            if (f == "learn_iters") { e->learn_iters = std::max(0, (int)value); return SYSU_OK; }
+            if (f == "learn_steps") { e->learn_steps = std::max(0, (int)value); return SYSU_OK; }
+            if (f == "learn_lr") { e->learn_lr = value; return SYSU_OK; }
+            if (f == "learn_kind") {
+                if (value != 0.0 && value != 1.0) return set_err(SYSU_ERR_INPUT, "learn_kind: 0 energy norm, 1 residual norm");
+                e->learn_kind = (int)value;
+                s->impl->gnn.loss_kind = e->learn_kind;
+                return SYSU_OK;
+            }
         }
     }
     return set_err(SYSU_ERR_INPUT, "unknown option " + k);
@@ -260,8 +276,14 @@ int sysu_solver_get_option(sysu_solver *s, const char *key, double *value) {
             if (f == "precond") { *value = e->precond; return SYSU_OK; }
             if (f == "restart") { *value = e->restart; return SYSU_OK; }
             if (f == "inner_tol") { *value = e->inner_tol; return SYSU_OK; }
+            if (f == "learned") { *value = e->learned; return SYSU_OK; }
+            if (f == "learn_iters") { *value = e->learn_iters; return SYSU_OK; }
+            if (f == "learn_steps") { *value = e->learn_steps; return SYSU_OK; }
+            if (f == "learn_lr") { *value = e->learn_lr; return SYSU_OK; }
+            if (f == "learn_kind") { *value = e->learn_kind; return SYSU_OK; }
         }
     }
+    if (k == "p.learned_solves") { *value = s->impl->p_solves; return SYSU_OK; }
     return set_err(SYSU_ERR_INPUT, "unknown option " + k);
 }
 

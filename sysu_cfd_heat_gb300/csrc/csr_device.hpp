@@ -36,16 +36,28 @@ struct CsrDevice {
     SellPattern pat;
     SellDev A;
     DevBuf<double> val;
+    std::vector<int> rp, cl;  // diagonal-first row lists of the pattern
     void load(int n, const int *rowptr, const int *col, const double *v, cudaStream_t st) {
-        std::vector<int> rp, cl;
         std::vector<double> vl;
         csr_rows_diag_first(n, rowptr, col, v, rp, cl, vl);
         pat = make_sell(n, rp, cl);
         A.upload(pat, st);
+        upload_values(vl, st);
+    }
+    // new values for the same pattern (same rowptr and col as load)
+    void reload_values(int n, const int *rowptr, const int *col, const double *v, cudaStream_t st) {
+        std::vector<int> rp2, cl2;
+        std::vector<double> vl;
+        csr_rows_diag_first(n, rowptr, col, v, rp2, cl2, vl);
+        if (n != pat.n || rp2 != rp || cl2 != cl) throw CaseError{"matrix pattern differs from the loaded one"};
+        upload_values(vl, st);
+    }
+    void upload_values(const std::vector<double> &vl, cudaStream_t st) {
         std::vector<double> sv(pat.nnz, 0.0);
-        for (int i = 0; i < n; ++i)
+        for (int i = 0; i < pat.n; ++i)
             for (int k = rp[i]; k < rp[i + 1]; ++k) sv[pat.pos(i, k - rp[i])] = vl[k];
         val.upload(sv, st);
+        SYSU_CUDA(cudaStreamSynchronize(st));
     }
 };
 

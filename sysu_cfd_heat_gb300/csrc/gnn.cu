@@ -55,8 +55,9 @@ __device__ __forceinline__ uint32_t bf_pack(float a, float b) {
 __device__ __forceinline__ float bf_round(float a) { return __bfloat162float(__float2bfloat16_rn(a)); }
 
 // Block partial sums of NV values -> part[block][NV]; the last block to arrive
-// adds them in block order.  Returns true in exactly one thread (lane 0 of the
-// last block), which then holds the totals.
+// adds them up (every thread of that block loads a strided share, then a block
+// reduction in a fixed order).  Returns true in exactly one thread (thread 0 of
+// the last block), which then holds the totals in v.
 template <int NV>
 __device__ bool grid_sums(double (&v)[NV], double *part, unsigned *cnt) {
     __shared__ double sm[NV * 8];
@@ -70,18 +71,31 @@ __device__ bool grid_sums(double (&v)[NV], double *part, unsigned *cnt) {
         s_last = prev == gridDim.x - 1;
     }
     __syncthreads();
-    if (!s_last || threadIdx.x >= 32) return false;
+    if (!s_last) return false;
     __threadfence();
-    int lane = threadIdx.x;
+    double t[NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-        double t = 0.0;
-        for (int b = lane; b < (int)gridDim.x; b += 32) t += __ldcg(part + (size_t)b * NV + k);
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(FULL_MASK, t, o);
-        v[k] = t;
+    for (int k = 0; k < NV; ++k) t[k] = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) t[k] += __ldcg(part + (size_t)b * NV + k);
+    block_sum_t0<NV>(t, sm);
+    if (threadIdx.x != 0) return false;
+    *cnt = 0;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = t[k];
+    return true;
+}
+
+// Wait for the MMA commit of this tile (bounded by COPY_WAIT_NS).
+__device__ __forceinline__ bool mma_wait(uint64_t *bar, unsigned parity, int mode) {
+    if (mode == 0) return mbar_wait(bar, parity);
+    unsigned long long t0 = global_timer_ns();
+    for (;;) {
+        bool ok = mode == 1 ? mbar_try_wait(bar, parity) : mbar_test_wait(bar, parity);
+        if (ok) return true;
+        if (global_timer_ns() - t0 > COPY_WAIT_NS) return false;
     }
-    if (lane == 0) *cnt = 0;
-    return lane == 0;
 }
 
 // ---------------------------------------------------------------- forward --
@@ -102,6 +116,7 @@ struct NetArgs {
     FcgState *fs;
     double *part;
     int *err;
+    int wait_mode;
 };
 
 template <bool L1, bool TRAIN, bool DEC>
@@ -180,33 +195,46 @@ __global__ void __launch_bounds__(GT) k_gnn_fwd(NetArgs a) {
                     a.aw[2 * (size_t)row + 1] = wi;
                 }
             } else {
-                for (int k = 1; k < w; ++k) {
-                    int pos = base + k * 32 + lane;
-                    int j = a.g.col[pos];
-                    float v = a.g.val[pos];
-                    const uint4 *hp = reinterpret_cast<const uint4 *>(a.hin + (size_t)j * 32);
+                {
+                    const uint4 *hp = reinterpret_cast<const uint4 *>(a.hin + (size_t)row * 32);
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
-                        uint4 h4 = hp[q];
-                        uint32_t hw[4] = {h4.x, h4.y, h4.z, h4.w};
+                        uint4 h4 = __ldg(hp + q);
+                        hs[4 * q] = h4.x;
+                        hs[4 * q + 1] = h4.y;
+                        hs[4 * q + 2] = h4.z;
+                        hs[4 * q + 3] = h4.w;
+                    }
+                }
+                // two neighbours per step: eight 16-byte loads in flight per thread
+                for (int k = 1; k < w; k += 2) {
+                    const int pos = base + k * 32 + lane;
+                    const bool two = k + 1 < w;
+                    const int j0 = a.g.col[pos];
+                    const float v0 = a.g.val[pos];
+                    const int j1 = two ? a.g.col[pos + 32] : j0;
+                    const float v1 = two ? a.g.val[pos + 32] : 0.f;
+                    const uint4 *p0 = reinterpret_cast<const uint4 *>(a.hin + (size_t)j0 * 32);
+                    const uint4 *p1 = reinterpret_cast<const uint4 *>(a.hin + (size_t)j1 * 32);
+                    uint4 x[4], y[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        x[q] = __ldg(p0 + q);
+                        y[q] = __ldg(p1 + q);
+                    }
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        uint32_t xw[4] = {x[q].x, x[q].y, x[q].z, x[q].w};
+                        uint32_t yw[4] = {y[q].x, y[q].y, y[q].z, y[q].w};
 #pragma unroll
                         for (int e = 0; e < 4; ++e) {
-                            mv[8 * q + 2 * e] += v * bf_lo(hw[e]);
-                            mv[8 * q + 2 * e + 1] += v * bf_hi(hw[e]);
+                            mv[8 * q + 2 * e] += v0 * bf_lo(xw[e]) + v1 * bf_lo(yw[e]);
+                            mv[8 * q + 2 * e + 1] += v0 * bf_hi(xw[e]) + v1 * bf_hi(yw[e]);
                         }
                     }
                 }
 #pragma unroll
                 for (int c = 0; c < 32; ++c) mv[c] *= di;
-                const uint4 *hp = reinterpret_cast<const uint4 *>(a.hin + (size_t)row * 32);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    uint4 h4 = hp[q];
-                    hs[4 * q] = h4.x;
-                    hs[4 * q + 1] = h4.y;
-                    hs[4 * q + 2] = h4.z;
-                    hs[4 * q + 3] = h4.w;
-                }
             }
         }
         uint32_t mp[16];
@@ -236,7 +264,7 @@ __global__ void __launch_bounds__(GT) k_gnn_fwd(NetArgs a) {
             umma::commit(bar);
         }
         __syncwarp();
-        bool fail = !mbar_wait(bar, it & 1);
+        bool fail = !mma_wait(bar, it & 1, a.wait_mode);
         if (__syncthreads_or(fail)) {
             if (tid == 0) atomicExch(a.err, (int)DEV_BARRIER_TIMEOUT);
             break;
@@ -677,6 +705,27 @@ __global__ void k_gnn_dinv(int n, const int *sl_ptr, const double *val, float *d
     dinv[i] = d != 0.0 ? (float)(1.0 / d) : 0.f;
 }
 
+// training pair from a partial solve: r = b - A x1, e = xs - x1 (x1 == nullptr: 0)
+__global__ void k_pair_from(GView g, const double *val64, const double *b, const double *x1, const double *xs,
+                            float *r, float *e) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.n) return;
+    double ri = b[i], ei = xs[i];
+    if (x1) {
+        const int sl = i >> 5, lane = i & 31;
+        const int base = g.sl_ptr[sl], w = g.sl_w[sl];
+        double ax = 0.0;
+        for (int k = 0; k < w; ++k) {
+            int pos = base + k * 32 + lane;
+            ax += val64[pos] * x1[g.col[pos]];
+        }
+        ri -= ax;
+        ei -= x1[i];
+    }
+    r[i] = (float)ri;
+    e[i] = (float)ei;
+}
+
 __global__ void k_to_f32(int n, const double *a, float *b) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) b[i] = (float)a[i];
@@ -903,6 +952,10 @@ int blocks_flat(int n) { return std::max(1, std::min((n + FB - 1) / FB, num_sms(
 }  // namespace
 
 void GnnPrecond::bind(const SellDev &A, const double *val64, const float *val32, cudaStream_t st) {
+    for (ChunkGraph &g : graphs_) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = ChunkGraph{};
+    }
     A_ = &A;
     val64_ = val64;
     val32_ = val32;
@@ -915,17 +968,22 @@ void GnnPrecond::bind(const SellDev &A, const double *val64, const float *val32,
         SYSU_CUDA(cudaFuncSetAttribute(k_gnn_bwd<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, BWD_SMEM_REQ));
         attr = true;
     }
+    // forward: as many co-resident CTAs as registers and shared memory allow
+    // (the gather is latency-bound).  Computed from the kernel's attributes:
+    // the runtime's occupancy query reports one CTA per SM for kernels that
+    // allocate tensor memory.
+    cudaFuncAttributes fa{};
+    SYSU_CUDA(cudaFuncGetAttributes(&fa, k_gnn_fwd<false, true, true>));
+    int by_regs = 65536 / std::max(1, fa.numRegs * GT);
+    int by_smem = (227 * 1024) / (FWD_SMEM + (int)fa.sharedSizeBytes + 1024);
+    int occ = std::max(1, std::min(std::min(by_regs, by_smem), 8));
+    if (fwd_per_sm > 0) occ = fwd_per_sm;
+    gfwd_ = std::max(1, std::min(ntiles_, num_sms() * occ));
     gtiles_ = std::max(1, std::min(ntiles_, num_sms() * 3));
     gflat_ = blocks_flat(n_);
     const size_t n = (size_t)n_;
     dinv_.alloc(n);
-    k_gnn_dinv<<<(n_ + FB - 1) / FB, FB, 0, st>>>(n_, A.sl_ptr.get(), val64, dinv_.get());
-    ++g_launches;
-    SYSU_CUDA(cudaGetLastError());
-    double d0 = 0.0;
-    SYSU_CUDA(cudaMemcpyAsync(&d0, val64, sizeof(double), cudaMemcpyDeviceToHost, st));
-    SYSU_CUDA(cudaStreamSynchronize(st));
-    sgn_ = d0 < 0.0 ? -1.0f : 1.0f;
+    refresh(st);
     if (p_.size() == 0) {
         p_.alloc(GNN_NPARAM_PAD);
         m_.alloc(GNN_NPARAM_PAD);
@@ -944,7 +1002,7 @@ void GnnPrecond::bind(const SellDev &A, const double *val64, const float *val32,
         err_.zero(st);
     }
     rec_.alloc((size_t)gtiles_ * GNN_NPARAM_PAD);
-    part_.alloc((size_t)std::max(gtiles_, gflat_) * 4);
+    part_.alloc((size_t)std::max(std::max(gtiles_, gfwd_), gflat_) * 4);
     H_.alloc(5 * n * 32);
     M_.alloc(4 * n * 32);
     mask_.alloc(4 * n);
@@ -958,6 +1016,16 @@ void GnnPrecond::bind(const SellDev &A, const double *val64, const float *val32,
     pe_.alloc((size_t)capacity_ * n);
     r64_.alloc(n);
     count_ = next_ = 0;
+}
+
+void GnnPrecond::refresh(cudaStream_t st) {
+    k_gnn_dinv<<<(n_ + FB - 1) / FB, FB, 0, st>>>(n_, A_->sl_ptr.get(), val64_, dinv_.get());
+    ++g_launches;
+    SYSU_CUDA(cudaGetLastError());
+    double d0 = 0.0;
+    SYSU_CUDA(cudaMemcpyAsync(&d0, val64_, sizeof(double), cudaMemcpyDeviceToHost, st));
+    SYSU_CUDA(cudaStreamSynchronize(st));
+    sgn_ = d0 < 0.0 ? -1.0f : 1.0f;
 }
 
 void GnnPrecond::refresh_bf16(cudaStream_t st) {
@@ -1019,6 +1087,7 @@ void GnnPrecond::forward(const float *r32, float *z32, bool train, FcgState *fs,
     a.fs = fs;
     a.part = part_.get();
     a.err = err_.get();
+    a.wait_mode = wait_mode;
     const size_t nn = (size_t)n_ * 32;
     for (int l = 0; l < GNN_LAYERS; ++l) {
         a.layer = l;
@@ -1034,7 +1103,7 @@ void GnnPrecond::forward(const float *r32, float *z32, bool train, FcgState *fs,
             a.mout = nullptr;
             a.mask = nullptr;
         }
-        dim3 grid(gtiles_), blk(GT);
+        dim3 grid(gfwd_), blk(GT);
         if (l == 0) {
             if (train) k_gnn_fwd<true, true, false><<<grid, blk, FWD_SMEM, st>>>(a);
             else k_gnn_fwd<true, false, false><<<grid, blk, FWD_SMEM, st>>>(a);
@@ -1100,6 +1169,27 @@ void GnnPrecond::apply(const double *r, double *z, cudaStream_t st) {
     check_err(st);
 }
 
+double GnnPrecond::time_apply(const double *r, int reps, cudaStream_t st) {
+    int nb = (n_ + FB - 1) / FB;
+    k_to_f32<<<nb, FB, 0, st>>>(n_, r, r32_.get());
+    ++g_launches;
+    scale_of(r32_.get(), st);
+    forward(r32_.get(), z32_.get(), false, nullptr, nullptr, st);
+    cudaEvent_t e0, e1;
+    SYSU_CUDA(cudaEventCreate(&e0));
+    SYSU_CUDA(cudaEventCreate(&e1));
+    SYSU_CUDA(cudaEventRecord(e0, st));
+    for (int i = 0; i < reps; ++i) forward(r32_.get(), z32_.get(), false, nullptr, nullptr, st);
+    SYSU_CUDA(cudaEventRecord(e1, st));
+    SYSU_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    check_err(st);
+    return ms / std::max(reps, 1);
+}
+
 void GnnPrecond::check_err(cudaStream_t st) {
     int e = 0;
     SYSU_CUDA(cudaMemcpyAsync(&e, err_.get(), sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -1117,6 +1207,17 @@ void GnnPrecond::add_pair(const double *r, const double *e, cudaStream_t st) {
     k_to_f32<<<nb, FB, 0, st>>>(n_, r, pr_.get() + off);
     k_to_f32<<<nb, FB, 0, st>>>(n_, e, pe_.get() + off);
     g_launches += 2;
+    SYSU_CUDA(cudaGetLastError());
+    next_ = (next_ + 1) % capacity_;
+    count_ = std::min(count_ + 1, capacity_);
+}
+
+void GnnPrecond::add_pair_from(const double *b, const double *x1, const double *xs, cudaStream_t st) {
+    if (!bound()) throw CaseError{"learned preconditioner: no matrix bound"};
+    size_t off = (size_t)next_ * n_;
+    k_pair_from<<<(n_ + FB - 1) / FB, FB, 0, st>>>(gview(*A_, val32_, dinv_.get()), val64_, b, x1, xs,
+                                                  pr_.get() + off, pe_.get() + off);
+    ++g_launches;
     SYSU_CUDA(cudaGetLastError());
     next_ = (next_ + 1) % capacity_;
     count_ = std::min(count_ + 1, capacity_);
@@ -1172,15 +1273,36 @@ void GnnPrecond::last_losses(std::vector<double> &out, int count, cudaStream_t s
     SYSU_CUDA(cudaStreamSynchronize(st));
 }
 
+// One flexible-CG iteration (network or Jacobi preconditioner, direction,
+// update, conditional reliable update) enqueued on st.
+void GnnPrecond::fcg_iteration(const void *args, bool use_gnn, cudaStream_t st) {
+    const FcgArgs &a = *static_cast<const FcgArgs *>(args);
+    if (use_gnn) forward(a.r, a.z, false, a.fs, a.q, st);
+    k_fcg_jacobi<<<gflat_, FB, 0, st>>>(a);
+    k_fcg_dir<<<gflat_, FB, 0, st>>>(a);
+    k_fcg_upd<<<gflat_, FB, 0, st>>>(a);
+    k_fcg_rel1<<<gflat_, FB, 0, st>>>(a);
+    k_fcg_rel2<<<gflat_, FB, 0, st>>>(a);
+    g_launches += 5;
+    SYSU_CUDA(cudaGetLastError());
+}
+
 void GnnPrecond::fcg(const double *b, double *x, bool x0_zero, const KrylovOpts &o, bool use_gnn, SolveInfo *info_dev,
                      cudaStream_t st) {
     if (!bound()) throw CaseError{"learned preconditioner: no matrix bound"};
+    // the iterations run from a CUDA graph over fixed buffers: b and x are copied in and out
+    if (b64_.size() < (size_t)n_) {
+        b64_.alloc(n_);
+        x64_.alloc(n_);
+    }
+    SYSU_CUDA(cudaMemcpyAsync(b64_.get(), b, sizeof(double) * n_, cudaMemcpyDeviceToDevice, st));
+    if (!x0_zero) SYSU_CUDA(cudaMemcpyAsync(x64_.get(), x, sizeof(double) * n_, cudaMemcpyDeviceToDevice, st));
     FcgArgs a{};
     a.g = gview(*A_, val32_, dinv_.get());
     a.val64 = val64_;
     a.sgn = sgn_;
-    a.b = b;
-    a.x = x;
+    a.b = b64_.get();
+    a.x = x64_.get();
     a.r = r32_.get();
     a.z = z32_.get();
     a.p = p32_.get();
@@ -1191,33 +1313,50 @@ void GnnPrecond::fcg(const double *b, double *x, bool x0_zero, const KrylovOpts 
     a.inner_tol2 = o.inner_tol * o.inner_tol;
     a.stall_max = stall_max;
     if (x0_zero) {
-        k_fcg_zero<<<(n_ + FB - 1) / FB, FB, 0, st>>>(n_, x);
+        k_fcg_zero<<<(n_ + FB - 1) / FB, FB, 0, st>>>(n_, a.x);
         ++g_launches;
     }
     k_fcg_init<<<gflat_, FB, 0, st>>>(a, x0_zero ? 1 : 0, o.eps, o.maxit, use_gnn ? 1 : 0);
     ++g_launches;
     SYSU_CUDA(cudaGetLastError());
+    // (re)capture the chunk graph when its arguments changed
+    ChunkGraph &cg = graphs_[use_gnn ? 1 : 0];
+    if (!cg.exec || cg.inner_tol != o.inner_tol || cg.stall_max != stall_max || cg.chunk != check_every ||
+        cg.val32 != val32_ || cg.dinv != dinv_.get()) {
+        if (cg.exec) cudaGraphExecDestroy(cg.exec);
+        cg.exec = nullptr;
+        long before = g_launches.load();
+        cudaGraph_t g;
+        SYSU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        for (int c = 0; c < check_every; ++c) fcg_iteration(&a, use_gnn, st);
+        SYSU_CUDA(cudaStreamEndCapture(st, &g));
+        cg.launches = g_launches.load() - before;
+        g_launches -= cg.launches;
+        SYSU_CUDA(cudaGraphInstantiate(&cg.exec, g, 0));
+        cudaGraphDestroy(g);
+        cg.inner_tol = o.inner_tol;
+        cg.stall_max = stall_max;
+        cg.chunk = check_every;
+        cg.val32 = val32_;
+        cg.dinv = dinv_.get();
+    }
     int done = 0;
-    for (int it = 0; it < o.maxit && !done;) {
-        int chunk = std::min(check_every, o.maxit - it);
-        for (int c = 0; c < chunk; ++c) {
-            if (use_gnn) forward(a.r, a.z, false, a.fs, a.q, st);
-            k_fcg_jacobi<<<gflat_, FB, 0, st>>>(a);
-            k_fcg_dir<<<gflat_, FB, 0, st>>>(a);
-            k_fcg_upd<<<gflat_, FB, 0, st>>>(a);
-            k_fcg_rel1<<<gflat_, FB, 0, st>>>(a);
-            k_fcg_rel2<<<gflat_, FB, 0, st>>>(a);
-            g_launches += 5;
-        }
-        SYSU_CUDA(cudaGetLastError());
-        it += chunk;
+    for (int it = 0; it < o.maxit && !done; it += check_every) {
+        SYSU_CUDA(cudaGraphLaunch(cg.exec, st));
+        g_launches += cg.launches;
         SYSU_CUDA(cudaMemcpyAsync(&done, &fs_.get()->done, sizeof(int), cudaMemcpyDeviceToHost, st));
         SYSU_CUDA(cudaStreamSynchronize(st));
     }
+    SYSU_CUDA(cudaMemcpyAsync(x, x64_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, st));
     k_fcg_info<<<1, 1, 0, st>>>(fs_.get(), info_dev);
     ++g_launches;
     SYSU_CUDA(cudaGetLastError());
     check_err(st);
+}
+
+GnnPrecond::~GnnPrecond() {
+    for (ChunkGraph &g : graphs_)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
 }
 
 __global__ void k_bf16_to_f32(long n, const uint16_t *a, float *b) {

@@ -55,10 +55,17 @@ struct GnnScalars {  // training / apply scalars (device memory)
 
 class GnnPrecond {
   public:
+    GnnPrecond() = default;
+    GnnPrecond(const GnnPrecond &) = delete;
+    GnnPrecond &operator=(const GnnPrecond &) = delete;
+    ~GnnPrecond();
     // Attach to a symmetric SELL matrix (FP64 values and their FP32 copy, both
     // owned by the caller and kept alive); sizes the work buffers for it.
     void bind(const SellDev &A, const double *val64, const float *val32, cudaStream_t st);
     bool bound() const { return A_ != nullptr; }
+    // The bound matrix's values changed (same pattern, same buffers): recompute
+    // the diagonal inverse the network and the solver use.
+    void refresh(cudaStream_t st);
     int n() const { return n_; }
 
     void init_params(unsigned long long seed, cudaStream_t st);
@@ -69,9 +76,18 @@ class GnnPrecond {
     // z = M(r) (FP64 device vectors, converted to FP32 inside).
     void apply(const double *r, double *z, cudaStream_t st);
 
+    // device time of one network application (ms), averaged over reps
+    double time_apply(const double *r, int reps, cudaStream_t st);
+    int wait_mode = 0;    // MMA completion wait: 0 try_wait with sleep hint, 1 try_wait, 2 test_wait spin
+    int fwd_per_sm = 0;   // forward CTAs per SM (0: occupancy limit); applied at bind
+
     // Training pairs: a ring of `capacity` FP32 pairs.
     void set_capacity(int pairs) { capacity_ = pairs; }
     void add_pair(const double *r, const double *e, cudaStream_t st);
+    // pair of a partial solve x1 of A x = b with solution xs: (b - A x1, xs - x1);
+    // x1 == nullptr gives (b, xs)
+    void add_pair_from(const double *b, const double *x1, const double *xs, cudaStream_t st);
+    int newest_pair() const { return (next_ + capacity_ - 1) % capacity_; }
     int pairs() const { return count_; }
     void clear_pairs() { count_ = 0; next_ = 0; }
     // One Adam step on pair k; the loss lands in losses()[step index] (device).
@@ -102,11 +118,22 @@ class GnnPrecond {
     void refresh_bf16(cudaStream_t st);
     void scale_of(const float *r32, cudaStream_t st);
     void check_err(cudaStream_t st);
+    void fcg_iteration(const void *args, bool use_gnn, cudaStream_t st);
+
+    // a captured chunk of check_every flexible-CG iterations
+    struct ChunkGraph {
+        cudaGraphExec_t exec = nullptr;
+        double inner_tol = 0.0;
+        int stall_max = 0, chunk = 0;
+        long launches = 0;
+        const float *val32 = nullptr, *dinv = nullptr;
+    };
+    ChunkGraph graphs_[2];
 
     const SellDev *A_ = nullptr;
     const double *val64_ = nullptr;
     const float *val32_ = nullptr;
-    int n_ = 0, ntiles_ = 0, gtiles_ = 0, gflat_ = 0;
+    int n_ = 0, ntiles_ = 0, gtiles_ = 0, gfwd_ = 0, gflat_ = 0;
     float sgn_ = 1.0f;
     int capacity_ = 32, count_ = 0, next_ = 0, adam_t_ = 0;
 
@@ -120,7 +147,7 @@ class GnnPrecond {
     DevBuf<float> dA_, gA_, dB_, gB_;  // backward ping-pong [n][32]
     DevBuf<float> z32_, y32_, r32_, e32_, p32_, q32_, x32_;
     DevBuf<float> pr_, pe_;     // pair ring [capacity][n]
-    DevBuf<double> part_, r64_;
+    DevBuf<double> part_, r64_, b64_, x64_;
     DevBuf<double> losses_;
     DevBuf<GnnScalars> sc_;
     DevBuf<FcgState> fs_;

@@ -71,6 +71,15 @@ void sysu_gnn_free(sysu_gnn *g) {
     if (st) cudaStreamDestroy(st);
 }
 
+int sysu_gnn_set_values(sysu_gnn *g, const int *rowptr, const int *col, const double *val) {
+    if (!g || !rowptr || !col || !val) return SYSU_ERR_INPUT;
+    return guarded([&] {
+        g->M.reload_values(g->net.n(), rowptr, col, val, g->st);
+        sysu::sell_to_fp32(g->M.A, g->M.val.get(), g->val32.get(), g->st);
+        g->net.refresh(g->st);
+    });
+}
+
 int sysu_gnn_init_params(sysu_gnn *g, unsigned long long seed) {
     if (!g) return SYSU_ERR_INPUT;
     return guarded([&] {
@@ -184,6 +193,19 @@ int sysu_gnn_hidden(sysu_gnn *g, const double *r, int layer, float *h) {
     return guarded([&] {
         g->v0.upload(r, g->net.n(), g->st);
         g->net.hidden(g->v0.get(), layer, h, g->st);
+    });
+}
+
+int sysu_gnn_time_apply(sysu_gnn *g, const double *r, int reps, int wait_mode, int fwd_per_sm, double *ms) {
+    if (!g || !r || !ms) return SYSU_ERR_INPUT;
+    return guarded([&] {
+        g->v0.upload(r, g->net.n(), g->st);
+        g->net.wait_mode = wait_mode;
+        if (fwd_per_sm != g->net.fwd_per_sm) {
+            g->net.fwd_per_sm = fwd_per_sm;
+            g->net.bind(g->M.A, g->M.val.get(), g->val32.get(), g->st);
+        }
+        *ms = g->net.time_apply(g->v0.get(), reps, g->st);
     });
 }
 

@@ -349,6 +349,11 @@ void SimpleSolver::solve(int slot, const EqOpts &o, const SellDev &A, const doub
                         nrhs == 1 ? info : infos.get() + SLOT_N + c, st);
         return;
     }
+    if (o.kind == SK_CG && o.learned && &A == &fd.A) {
+        if (nrhs != 1) throw CaseError{"CG solves one right-hand side"};
+        solve_learned(o, val, b[0], x[0], x0_zero, info);
+        return;
+    }
     if (o.kind == SK_CG) {
         if (nrhs != 1) throw CaseError{"CG solves one right-hand side"};
         if (o.precond == PK_SSOR || o.precond == PK_ILU0) {
@@ -374,6 +379,48 @@ void SimpleSolver::solve(int slot, const EqOpts &o, const SellDev &A, const doub
         return;
     }
     bicgstab_solve(A, val, nrhs, b, x, ko, kw, info, st);
+}
+
+// p' solve of the learned form.  Training window: a loose plain solve (1e-2)
+// from zero, then the solve to eps from there; the pairs (b, x*) and
+// (b - A x1, x* - x1) go into the network's ring and learn_steps Adam steps
+// follow.  After the window: flexible CG with the network.
+void SimpleSolver::solve_learned(const EqOpts &o, const double *val, const double *b, double *x, bool x0_zero,
+                                 SolveInfo *info) {
+    const SellDev &A = fd.A;
+    if (f.Ap32.size() < (size_t)A.nnz) f.Ap32.alloc(A.nnz);
+    sell_to_fp32(A, val, f.Ap32.get(), st);
+    if (!gnn.bound()) {
+        gnn.set_capacity(std::max(8, 2 * std::min(o.learn_iters, 32)));
+        gnn.bind(A, val, f.Ap32.get(), st);
+        gnn.init_params(20261203ULL, st);
+        gnn.loss_kind = o.learn_kind;
+    } else {
+        gnn.refresh(st);
+    }
+    KrylovOpts ko;
+    ko.maxit = o.maxit;
+    ko.eps = o.eps;
+    ko.omega = o.omega;
+    ko.jacobi = true;
+    ko.inner_tol = o.inner_tol;
+    if (p_solves++ >= o.learn_iters) {
+        gnn.fcg(b, x, x0_zero, ko, true, info, st);
+        return;
+    }
+    auto plain = [&](double eps, bool zero) {
+        KrylovOpts k = ko;
+        k.eps = eps;
+        if (o.mixed) cg_solve_mixed(A, val, f.Ap32.get(), b, x, zero, k, kw, info, st);
+        else cg_solve(A, val, b, x, zero, k, kw, info, st);
+    };
+    if (gnn_x1.size() < (size_t)A.n) gnn_x1.alloc(A.n);
+    plain(std::max(o.eps, 1e-2), x0_zero);
+    SYSU_CUDA(cudaMemcpyAsync(gnn_x1.get(), x, sizeof(double) * A.n, cudaMemcpyDeviceToDevice, st));
+    plain(o.eps, false);
+    gnn.add_pair_from(b, nullptr, x, st);
+    gnn.add_pair_from(b, gnn_x1.get(), x, st);
+    for (int k = 0; k < o.learn_steps; ++k) gnn.train_step(k % gnn.pairs(), o.learn_lr, st);
 }
 
 // CalculateVelocity + BuildVelocityMatrix, navier_velocity.cpp:12-357

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "fv.hpp"
+#include "gnn.hpp"
 
 namespace sysu {
 
@@ -39,6 +40,16 @@ struct EqOpts {
     double inner_tol = 0.1;   // FP32 residual drop between reliable updates
     int precond = PK_JACOBI;  // PrecondKind (SSOR and ILU with CG and GMRES)
     int restart = 10;         // GMRES restart length
+    // CG only (the p' equation): learned preconditioner.  The first learn_iters
+    // solves run the plain method and train the network on their
+    // residual/correction pairs (learn_steps Adam steps each, rate learn_lr);
+    // later solves run flexible CG preconditioned by the network (FP32
+    // recurrences, FP64 reliable updates, Jacobi fallback).
+    int learned = 0;
+    int learn_iters = 20;
+    int learn_steps = 64;
+    double learn_lr = 1e-3;
+    int learn_kind = 1;       // loss: 0 energy norm of the error, 1 residual norm
 };
 
 struct SolverOptions {
@@ -113,6 +124,9 @@ class SimpleSolver {
     DomainDev fd, sd;
     FieldSet f, s;
     KrylovWork kw;
+    GnnPrecond gnn;             // learned p' preconditioner (option p.learned)
+    int p_solves = 0;           // p' solves so far (training window of the learned form)
+    DevBuf<double> gnn_x1;      // partial solution of a training solve
     DevBuf<SolveInfo> infos;
     DevBuf<double> red_partials, red_out;
     DevBuf<unsigned int> red_ticket;
@@ -166,6 +180,7 @@ class SimpleSolver {
 
   private:
     void alloc_fields(FieldSet &fs, const DomainDev &d, bool solid);
+    void solve_learned(const EqOpts &o, const double *val, const double *b, double *x, bool x0_zero, SolveInfo *info);
     void solve(int slot, const EqOpts &o, const SellDev &A, const double *val, int nrhs, const double *const *b,
                double *const *x, bool x0_zero);
     void grad_limited(DomainDev &d, FieldSet &fs, int nfield, const double *const *phi, const double *const *Bphi,

@@ -63,6 +63,11 @@ class LearnedPreconditioner:
     def __exit__(self, *a):
         self.close()
 
+    def set_values(self, val):
+        """New values for the same pattern (rowptr, col of the constructor)."""
+        self.val = np.ascontiguousarray(val, dtype=np.float64)
+        self._check(_lib.lib().sysu_gnn_set_values(self.h, _ip(self.rowptr), _ip(self.col), _dp(self.val)))
+
     def init_params(self, seed: int = 0):
         self._check(_lib.lib().sysu_gnn_init_params(self.h, seed))
 

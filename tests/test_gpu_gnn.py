@@ -158,3 +158,32 @@ def test_fcg_jacobi_matches_cg():
     assert info["status"] == 0 and info["res"] < 1e-10
     assert abs(info["iters"] - it.value) <= 0.1 * it.value + 5, (info, it.value)
     assert _rel(x, xc) < 1e-8
+
+
+def test_simple_learned_form_matches_fp64():
+    """The SIMPLE loop with the learned p' form (option p.learned): fields after
+    30 outer iterations within 1e-6 of the plain FP64 form, every p' solve to
+    its tolerance, fewer p' iterations once trained."""
+    import tempfile
+    from sysu_cfd_heat_gb300 import meshgen as mg
+    from sysu_cfd_heat_gb300.solver import NavierStokesSolver
+
+    with tempfile.TemporaryDirectory() as d:
+        p = mg.write_case(d, mg.lid_cavity_tet(12, 12, 8, jitter=0.2, seed=7), mg.cavity_param("x", 100, mu=0.0025))
+        out = {}
+        for name, opts in (("fp64", {}), ("learned", {"p.learned": 1, "p.learn_iters": 8, "p.learn_steps": 48})):
+            o = {"rtc": 1e-10, "p.maxit": 20000}
+            o.update(opts)
+            with NavierStokesSolver(p, o) as s:
+                its = []
+                for k in range(30):
+                    assert s.iterate(1) == 1
+                    st = s.solve_stats()["p"]
+                    assert st["status"][0] == 0 and st["res"][0] < 1e-10, (name, k, st)
+                    its.append(st["iters"][0])
+                out[name] = ({f: s.get(f) for f in ("U", "V", "W", "P")}, its)
+                if name == "learned":
+                    assert s.get_option("p.learned_solves") == 30
+    for f, a in out["fp64"][0].items():
+        assert _rel(out["learned"][0][f], a) < 1e-6, f
+    assert np.mean(out["learned"][1][-10:]) < 0.8 * np.mean(out["fp64"][1][-10:]), (out["learned"][1], out["fp64"][1])
