@@ -78,6 +78,9 @@ int sysu_solver_info(sysu_solver *s, long *out, int n);
  *     "p.learn_lr" with loss "p.learn_kind" (0 energy norm, 1 residual norm);
  *     later solves run flexible CG with the network, see sysu_gnn_fcg; the
  *     network survives sysu_solver_reset; read-only "p.learned_solves");
+ *   "scalars_batched" (1: k, eps and T assembled together and solved by one
+ *     batched BiCGSTAB launch; eps's source and T's conductivity then lag by
+ *     one outer iteration, the steady solution is the same; needs ke + energy);
  *   "rtc" sets every eq's eps; "mom_batched" (1: u,v,w as one 3-RHS solve);
  *   "solid_source" (W/m^3, an extension); "fatal_checks"; "timing". */
 int sysu_solver_set_option(sysu_solver *s, const char *key, double value);
@@ -172,6 +175,12 @@ int sysu_csr_solve(int method, int precond, int n, const int *rowptr, const int 
                    const double *b, double *x, int maxit, double eps, double omega, int *iters, double *res,
                    int *status);
 int sysu_csr_spmv(int n, const int *rowptr, const int *col, const double *val, const double *x, double *y);
+/* Three systems sharing one sparsity pattern (rowptr, col), values vals[c],
+ * right-hand sides b[c], x[c] (x0 in, solution out), solved by one batched
+ * BiCGSTAB + Jacobi launch (the k, eps, T form of option "scalars_batched"). */
+int sysu_csr_bicgstab_batched3(int n, const int *rowptr, const int *col, const double *const *vals,
+                               const double *const *b, double *const *x, int maxit, double eps, int *iters,
+                               double *res, int *status);
 const char *sysu_csr_last_error(void);
 
 /* ---- Jacobi-CG that allocates nothing ----------------------------------------

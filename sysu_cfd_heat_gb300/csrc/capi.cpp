@@ -167,6 +167,16 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
         return SYSU_OK;
     }
     if (k == "mom_batched") { o.mom_batched = value != 0.0; return SYSU_OK; }
+    if (k == "scalars_batched") {
+        const sysu::Params &pp = s->impl->cs.params;
+        if (value != 0.0 && (pp.tur_model != 1 || !pp.solve_energy))
+            return set_err(SYSU_ERR_INPUT, "scalars_batched needs turbulence ke and energy on");
+        if (value != 0.0 && (o.ke.kind != sysu::SK_BICGSTAB || o.t.kind != sysu::SK_BICGSTAB ||
+                             o.ke.precond > sysu::PK_JACOBI || o.t.precond > sysu::PK_JACOBI))
+            return set_err(SYSU_ERR_INPUT, "scalars_batched runs k, eps and T with BiCGSTAB + Jacobi");
+        o.scalars_batched = value != 0.0;
+        return SYSU_OK;
+    }
     if (k == "reference_solvers") {
         if (value != 0.0) o.reference_solvers();
         else o.default_solvers();
@@ -258,6 +268,7 @@ int sysu_solver_get_option(sysu_solver *s, const char *key, double *value) {
     sysu::SolverOptions &o = s->impl->opt;
     std::string k(key);
     if (k == "mom_batched") { *value = o.mom_batched; return SYSU_OK; }
+    if (k == "scalars_batched") { *value = o.scalars_batched; return SYSU_OK; }
     if (k == "solid_source") { *value = o.solid_source; return SYSU_OK; }
     if (k == "fatal_checks") { *value = o.fatal_checks; return SYSU_OK; }
     if (k == "timing") { *value = o.timing; return SYSU_OK; }

@@ -98,6 +98,63 @@ int sysu_csr_spmv(int n, const int *rowptr, const int *col, const double *val, c
     }
 }
 
+// Three systems with one sparsity pattern (rowptr, col) and their own values,
+// solved by one batched BiCGSTAB + Jacobi launch.
+int sysu_csr_bicgstab_batched3(int n, const int *rowptr, const int *col, const double *const *vals,
+                               const double *const *b, double *const *x, int maxit, double eps, int *iters,
+                               double *res, int *status) {
+    try {
+        if (!vals || !b || !x) throw sysu::CaseError{"null argument"};
+        cudaStream_t st;
+        SYSU_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        {
+            sysu::CsrDevice M;
+            M.load(n, rowptr, col, vals[0], st);
+            sysu::CsrDevice M1, M2;
+            M1.pat = M.pat;
+            M1.rp = M.rp;
+            M1.cl = M.cl;
+            M2.pat = M.pat;
+            M2.rp = M.rp;
+            M2.cl = M.cl;
+            M1.reload_values(n, rowptr, col, vals[1], st);
+            M2.reload_values(n, rowptr, col, vals[2], st);
+            sysu::DevBuf<double> db[3], dx[3];
+            for (int c = 0; c < 3; ++c) {
+                db[c].alloc(n);
+                dx[c].alloc(n);
+                db[c].upload(b[c], n, st);
+                dx[c].upload(x[c], n, st);
+            }
+            sysu::KrylovWork w;
+            sysu::DevBuf<sysu::SolveInfo> info(1);
+            sysu::KrylovOpts o;
+            o.maxit = maxit;
+            o.eps = eps;
+            o.omega = 1.0;
+            o.jacobi = true;
+            const double *vv[3] = {M.val.get(), M1.val.get(), M2.val.get()};
+            const double *bb[3] = {db[0].get(), db[1].get(), db[2].get()};
+            double *xx[3] = {dx[0].get(), dx[1].get(), dx[2].get()};
+            sysu::bicgstab_solve_multi(M.A, vv, bb, xx, o, w, info.get(), st);
+            sysu::SolveInfo h;
+            info.download(&h, 1, st);
+            for (int c = 0; c < 3; ++c) dx[c].download(x[c], n, st);
+            SYSU_CUDA(cudaStreamSynchronize(st));
+            for (int c = 0; c < 3; ++c) {
+                if (iters) iters[c] = h.iters[c];
+                if (res) res[c] = h.res[c];
+                if (status) status[c] = h.err ? sysu::DEV_BARRIER_TIMEOUT : h.status[c];
+            }
+        }
+        cudaStreamDestroy(st);
+        return SYSU_OK;
+    } catch (const sysu::CaseError &e) {
+        g_csr_err = e.msg;
+        return SYSU_ERR_CUDA;
+    }
+}
+
 const char *sysu_csr_last_error(void) { return g_csr_err.c_str(); }
 
 // Assembled matrix of a solver ("mom", "p", "scalar", "solid") as CSR with the

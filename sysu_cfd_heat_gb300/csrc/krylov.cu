@@ -110,22 +110,30 @@ void SellDev::upload(const SellPattern &p, cudaStream_t s) {
 namespace {
 
 // y_c = A (dinv .* x_c) for NR right-hand sides, skipping inactive ones.
-template <int NR>
-__device__ __forceinline__ void row_dot_scaled(const SellView &A, int i, const double *__restrict__ dinv,
-                                               const double *__restrict__ x, int n, const bool (&act)[3],
-                                               double (&y)[NR]) {
+// MULTI: right-hand side c has its own matrix values vals[c] (same pattern) and
+// its own diagonal inverse dinv + c n; the column indices are read once.
+template <int NR, bool MULTI>
+__device__ __forceinline__ void row_dot_scaled(const SellView &A, const double *const *vals, int i,
+                                               const double *__restrict__ dinv, const double *__restrict__ x, int n,
+                                               const bool (&act)[3], double (&y)[NR]) {
     int s = i >> 5;
     int e = A.sl_ptr[s] + (i & 31);
     int w = A.sl_w[s];
 #pragma unroll
     for (int c = 0; c < NR; ++c) y[c] = 0.0;
     for (int k = 0; k < w; ++k, e += 32) {
-        double a = A.val[e];
         int j = A.col[e];
-        double d = dinv[j];
+        if (MULTI) {
 #pragma unroll
-        for (int c = 0; c < NR; ++c)
-            if (act[c]) y[c] += a * (d * x[(size_t)c * n + j]);
+            for (int c = 0; c < NR; ++c)
+                if (act[c]) y[c] += vals[c][e] * (dinv[(size_t)c * n + j] * x[(size_t)c * n + j]);
+        } else {
+            double a = A.val[e];
+            double d = dinv[j];
+#pragma unroll
+            for (int c = 0; c < NR; ++c)
+                if (act[c]) y[c] += a * (d * x[(size_t)c * n + j]);
+        }
     }
 }
 
@@ -186,6 +194,7 @@ __global__ void k_to_fp32(long n, const double *src, float *dst) {
 
 struct BicgArgs {
     SellView A;
+    const double *vals[3];  // per right-hand-side matrix values (MULTI)
     const double *b[3];
     double *x[3];
     double *r, *rt, *p, *v, *s, *t;
@@ -197,7 +206,7 @@ struct BicgArgs {
     double eps;
 };
 
-template <int NR>
+template <int NR, bool MULTI>
 __global__ void __launch_bounds__(KB) k_bicgstab(BicgArgs a) {
     const int n = a.A.n;
     const int T = gridDim.x * KB;
@@ -218,7 +227,9 @@ __global__ void __launch_bounds__(KB) k_bicgstab(BicgArgs a) {
 #pragma unroll
             for (int c = 0; c < NR; ++c) {
                 double bi = a.b[c][i];
-                double ri = bi - row_dot(a.A, i, a.x[c]);
+                SellView Ac = a.A;
+                if (MULTI) Ac.val = a.vals[c];
+                double ri = bi - row_dot(Ac, i, a.x[c]);
                 a.r[c * N + i] = ri;
                 a.rt[c * N + i] = ri;
                 v[c] += bi * bi;
@@ -269,7 +280,7 @@ __global__ void __launch_bounds__(KB) k_bicgstab(BicgArgs a) {
             for (int c = 0; c < NR; ++c) red[c] = 0.0;
             for (int i = t0; i < n; i += T) {
                 double y[NR];
-                row_dot_scaled<NR>(a.A, i, dinv, a.p, n, act, y);
+                row_dot_scaled<NR, MULTI>(a.A, a.vals, i, dinv, a.p, n, act, y);
 #pragma unroll
                 for (int c = 0; c < NR; ++c) {
                     if (!act[c]) continue;
@@ -319,7 +330,7 @@ __global__ void __launch_bounds__(KB) k_bicgstab(BicgArgs a) {
             for (int c = 0; c < 2 * NR; ++c) red[c] = 0.0;
             for (int i = t0; i < n; i += T) {
                 double y[NR];
-                row_dot_scaled<NR>(a.A, i, dinv, a.s, n, act2, y);
+                row_dot_scaled<NR, MULTI>(a.A, a.vals, i, dinv, a.s, n, act2, y);
 #pragma unroll
                 for (int c = 0; c < NR; ++c) {
                     if (!act2[c]) continue;
@@ -340,11 +351,11 @@ __global__ void __launch_bounds__(KB) k_bicgstab(BicgArgs a) {
 #pragma unroll
             for (int c = 0; c < 2 * NR; ++c) red[c] = 0.0;
             for (int i = t0; i < n; i += T) {
-                double di = dinv[i];
 #pragma unroll
                 for (int c = 0; c < NR; ++c) {
                     if (!act[c]) continue;
                     size_t k = c * N + i;
+                    double di = MULTI ? dinv[k] : dinv[i];
                     double ph = di * a.p[k];
                     if (early[c]) {
                         a.x[c][i] += alpha[c] * ph;
@@ -395,7 +406,7 @@ void KrylovWork::ensure(int n_, int nrhs_, int max_blocks_, cudaStream_t st) {
     max_blocks = std::max(max_blocks, max_blocks_);
     size_t m = (size_t)n * nrhs;
     r.alloc(m); rt.alloc(m); p.alloc(m); v.alloc(m); s.alloc(m); t.alloc(m);
-    dinv.alloc(n);
+    dinv.alloc(m);
     partials.alloc((size_t)8 * NVMAX * max_blocks);  // also the 4-word exact-sum partials
     barrier.alloc(1);
     barrier.zero(st);
@@ -441,24 +452,33 @@ void jacobi_apply(const SellDev &A, const double *val, double omega, const doubl
 }
 
 
-void bicgstab_solve(const SellDev &A, const double *val, int nrhs, const double *const *b, double *const *x,
-                    const KrylovOpts &o, KrylovWork &w, SolveInfo *info, cudaStream_t st) {
-    int n = A.n;
-    if (n == 0) return;
-    if (nrhs < 1 || nrhs > 3) throw CaseError{"bicgstab_solve: 1..3 right-hand sides"};
-    static int maxb1 = 0, maxb3 = 0;
-    if (!maxb1) {
-        maxb1 = coresident_blocks(k_bicgstab<1>);
-        maxb3 = coresident_blocks(k_bicgstab<3>);
+static int bicg_max_blocks(int nrhs, bool multi) {
+    static int mb[4] = {0, 0, 0, 0};
+    if (!mb[0]) {
+        mb[0] = coresident_blocks(k_bicgstab<1, false>);
+        mb[1] = coresident_blocks(k_bicgstab<3, false>);
+        mb[2] = coresident_blocks(k_bicgstab<3, true>);
+        mb[3] = std::max(std::max(mb[0], mb[1]), mb[2]);
     }
-    int maxb = (nrhs == 1) ? maxb1 : maxb3;
-    w.ensure(n, nrhs == 1 ? 1 : 3, std::max(maxb1, maxb3), st);
-    SellView V = view(A, val);
-    { k_jacobi_dinv<<<(n + KB - 1) / KB, KB, 0, st>>>(V, o.omega, o.jacobi ? 1 : 0, w.dinv.get()); ++::sysu::g_launches; }
+    if (nrhs < 0) return mb[3];
+    return nrhs == 1 ? mb[0] : (multi ? mb[2] : mb[1]);
+}
+
+static void bicg_launch(const SellDev &A, const double *const *vals, bool multi, int nrhs, const double *const *b,
+                        double *const *x, const KrylovOpts &o, KrylovWork &w, SolveInfo *info, cudaStream_t st) {
+    int n = A.n;
+    int maxb = bicg_max_blocks(nrhs, multi);
+    if (w.block_cap > 0) maxb = std::min(maxb, w.block_cap);
+    w.ensure(n, nrhs == 1 ? 1 : 3, bicg_max_blocks(-1, false), st);
+    for (int c = 0; c < (multi ? nrhs : 1); ++c) {
+        SellView Vc = view(A, vals[c]);
+        { k_jacobi_dinv<<<(n + KB - 1) / KB, KB, 0, st>>>(Vc, o.omega, o.jacobi ? 1 : 0, w.dinv.get() + (size_t)c * n); ++::sysu::g_launches; }
+    }
     SYSU_CUDA(cudaMemsetAsync(info, 0, sizeof(SolveInfo), st));
     BicgArgs a{};
-    a.A = V;
+    a.A = view(A, vals[0]);
     for (int c = 0; c < 3; ++c) {
+        a.vals[c] = vals[multi ? std::min(c, nrhs - 1) : 0];
         a.b[c] = b[std::min(c, nrhs - 1)];
         a.x[c] = x[std::min(c, nrhs - 1)];
     }
@@ -471,12 +491,24 @@ void bicgstab_solve(const SellDev &A, const double *val, int nrhs, const double 
     a.eps = o.eps;
     void *args[] = {&a};
     int G = grid_for(n, maxb);
-    if (nrhs == 1)
-        { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_bicgstab<1>, dim3(G), dim3(KB), args, 0, st)); ++::sysu::g_launches; }
-    else if (nrhs == 2)
-        throw CaseError{"bicgstab_solve: use 1 or 3 right-hand sides"};
-    else
-        { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_bicgstab<3>, dim3(G), dim3(KB), args, 0, st)); ++::sysu::g_launches; }
+    const void *k = nrhs == 1 ? (const void *)k_bicgstab<1, false>
+                              : (multi ? (const void *)k_bicgstab<3, true> : (const void *)k_bicgstab<3, false>);
+    SYSU_CUDA(cudaLaunchCooperativeKernel(k, dim3(G), dim3(KB), args, 0, st));
+    ++::sysu::g_launches;
+}
+
+void bicgstab_solve(const SellDev &A, const double *val, int nrhs, const double *const *b, double *const *x,
+                    const KrylovOpts &o, KrylovWork &w, SolveInfo *info, cudaStream_t st) {
+    if (A.n == 0) return;
+    if (nrhs != 1 && nrhs != 3) throw CaseError{"bicgstab_solve: use 1 or 3 right-hand sides"};
+    const double *vals[1] = {val};
+    bicg_launch(A, vals, false, nrhs, b, x, o, w, info, st);
+}
+
+void bicgstab_solve_multi(const SellDev &A, const double *const *vals, const double *const *b, double *const *x,
+                          const KrylovOpts &o, KrylovWork &w, SolveInfo *info, cudaStream_t st) {
+    if (A.n == 0) return;
+    bicg_launch(A, vals, true, 3, b, x, o, w, info, st);
 }
 
 }  // namespace sysu

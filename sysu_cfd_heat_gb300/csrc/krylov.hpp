@@ -76,6 +76,7 @@ struct KrylovWork {
     DevBuf<long long> gpart;                         // exact multi-value partial sums
     DevBuf<GridBarrier> barrier;
     unsigned long long *phase_ts = nullptr;  // optional: 4 timestamps per CG iteration, first 64
+    int block_cap = 0;  // > 0: at most this many blocks per persistent solve (cases sharing the GPU)
     void ensure(int n, int nrhs, int max_blocks, cudaStream_t st);
     void ensure32(int n, cudaStream_t st);
 };
@@ -129,6 +130,12 @@ void cg_solve(const SellDev &A, const double *val, const double *b, double *x, b
 // BiCGSTAB on nrhs (1..3) right-hand sides sharing one matrix; b[c], x[c].
 void bicgstab_solve(const SellDev &A, const double *val, int nrhs, const double *const *b, double *const *x,
                     const KrylovOpts &o, KrylovWork &w, SolveInfo *info_dev, cudaStream_t st);
+
+// BiCGSTAB on three systems with one sparsity pattern and their own values
+// vals[c] (and Jacobi diagonals), in one launch: the column indices are read
+// once per product for the three (k, eps and T of one outer iteration).
+void bicgstab_solve_multi(const SellDev &A, const double *const *vals, const double *const *b, double *const *x,
+                          const KrylovOpts &o, KrylovWork &w, SolveInfo *info, cudaStream_t st);
 
 // y = A x (standalone, for tests and the SpMV sweep).
 void spmv(const SellDev &A, const double *val, const double *x, double *y, cudaStream_t st);

@@ -253,6 +253,9 @@ void SimpleSolver::alloc_fields(FieldSet &fs, const DomainDev &d, bool solid) {
     z(fs.fcoef, F);
     z(fs.Prod, nc); z(fs.TESrc, nc); z(fs.EDSrc, nc); z(fs.VisTE, nc); z(fs.VisED, nc);
     z(fs.ApTE, nc); z(fs.ApED, nc); z(fs.kcond, nc);
+    if (cs.params.tur_model == 1 && cs.params.solve_energy) {
+        z(fs.As2, nnz); z(fs.As3, nnz); z(fs.bs2, nc); z(fs.bs3, nc); z(fs.xs2, nc); z(fs.xs3, nc);
+    }
 }
 
 // navier.cpp:113-188 and HeatConductionSolver.cpp:334-369
@@ -550,6 +553,92 @@ void SimpleSolver::update_ke() {
     launch_visc_tur(nc, f.R.get(), f.TE.get(), f.ED.get(), f.VisTur.get(), st);
 }
 
+// Batched scalar form: UpdateTurKEpsilon and UpdateEnergy (navier_scalar.cpp:14-172,
+// 257-397) assembled from the fields as they stand after the pressure
+// correction, then one three-system BiCGSTAB launch.  Differences from the
+// sequential form: eps's production/dissipation terms use k of the previous
+// outer iteration (the reference recomputes them after the k solve) and T's
+// conductivity uses the previous mu_t; a steady solution satisfies both forms.
+void SimpleSolver::update_scalars_batched() {
+    const Params &p = cs.params;
+    const DomView &d = fd.view;
+    int nc = fd.nc;
+    KeArgs k{};
+    k.dU = f.dU.get(); k.dV = f.dV.get(); k.dW = f.dW.get(); k.R = f.R.get(); k.VisLam = f.VisLam.get();
+    k.U = f.U.get(); k.V = f.V.get(); k.W = f.W.get();
+    k.TE = f.TE.get(); k.ED = f.ED.get(); k.VisTur = f.VisTur.get();
+    k.Prod = f.Prod.get(); k.TESrc = f.TESrc.get(); k.EDSrc = f.EDSrc.get(); k.VisTE = f.VisTE.get();
+    k.VisED = f.VisED.get(); k.ApTE = f.ApTE.get(); k.ApED = f.ApED.get(); k.BTE = f.BTE.get(); k.BED = f.BED.get();
+    launch_ke_sources(d, k, st);
+    launch_ke_bnd_values(d, k, st);
+    launch_time_term(nc, f.R.get(), fd.vol.get(), p.dt, tscheme(), f.TEp.get(), f.ApTE.get(), f.TESrc.get(), st);
+    launch_time_term(nc, f.R.get(), fd.vol.get(), p.dt, tscheme(), f.EDp.get(), f.ApED.get(), f.EDSrc.get(), st);
+    launch_ke_eps_sources(d, k, st);
+    ScalarArgs sa{};
+    sa.RUFace = f.RUFace.get(); sa.grad = f.dPhi.get(); sa.urf = p.urf[5]; sa.bc_mode = SC_FLUID_PLAIN;
+    sa.fD = f.fD.get(); sa.fE = f.fE.get(); sa.bapp = f.bapp.get(); sa.bsrc = f.bsrc.get();
+    sa.flags = flags.get();
+    {
+        const double *phi[1] = {f.TE.get()};
+        const double *Bphi[1] = {f.BTE.get()};
+        double *grad[1] = {f.dPhi.get()};
+        grad_limited(fd, f, 1, phi, Bphi, grad);
+        sa.phi = f.TE.get(); sa.Bphi = f.BTE.get(); sa.diff = f.VisTE.get(); sa.src = f.TESrc.get(); sa.app0 = f.ApTE.get();
+        sa.val = f.As.get(); sa.b = f.bs.get();
+        launch_scalar(d, sa, st);
+        launch_copy(f.xs.get(), f.TE.get(), nc, st);
+    }
+    {
+        const double *phi[1] = {f.ED.get()};
+        const double *Bphi[1] = {f.BED.get()};
+        double *grad[1] = {f.dPhi.get()};
+        grad_limited(fd, f, 1, phi, Bphi, grad);
+        sa.phi = f.ED.get(); sa.Bphi = f.BED.get(); sa.diff = f.VisED.get(); sa.src = f.EDSrc.get(); sa.app0 = f.ApED.get();
+        sa.val = f.As2.get(); sa.b = f.bs2.get();
+        launch_scalar(d, sa, st);
+        launch_ke_eps_wall_rows(d, f.ED.get(), f.As2.get(), f.bs2.get(), st);
+        launch_copy(f.xs2.get(), f.ED.get(), nc, st);
+    }
+    launch_kcond(nc, f.VisLam.get(), f.VisTur.get(), p.cp, p.prl, p.prte, f.kcond.get(), st);
+    launch_bc_temperature_fluid(d, f.T.get(), f.BTem.get(), st);
+    if (cs.has_solid) launch_cht_solid2fluid(sd.view, s.T.get(), s.dPhi.get(), d, f.BTem.get(), st);
+    {
+        const double *phi[1] = {f.T.get()};
+        const double *Bphi[1] = {f.BTem.get()};
+        double *grad[1] = {f.dPhi.get()};
+        grad_limited(fd, f, 1, phi, Bphi, grad);
+        ScalarArgs ta = sa;
+        ta.phi = f.T.get(); ta.Bphi = f.BTem.get(); ta.diff = f.kcond.get(); ta.src = f.zeros.get(); ta.app0 = f.zeros.get();
+        if (tscheme()) {
+            launch_fill(f.src.get(), 0.0, nc, st);
+            launch_fill(f.tapp.get(), 0.0, nc, st);
+            launch_time_term(nc, f.R.get(), fd.vol.get(), p.dt, tscheme(), f.Tnp.get(), f.tapp.get(), f.src.get(), st);
+            ta.src = f.src.get();
+            ta.app0 = f.tapp.get();
+        }
+        ta.Bq = f.Bq.get();
+        ta.bc_mode = SC_FLUID_ENERGY;
+        ta.val = f.As3.get(); ta.b = f.bs3.get();
+        launch_scalar(d, ta, st);
+        launch_copy(f.xs3.get(), f.T.get(), nc, st);
+    }
+    KrylovOpts ko;
+    ko.maxit = opt.ke.maxit;
+    ko.eps = opt.ke.eps;
+    ko.omega = opt.ke.omega;
+    ko.jacobi = opt.ke.precond == PK_JACOBI;
+    const double *vals[3] = {f.As.get(), f.As2.get(), f.As3.get()};
+    const double *bb[3] = {f.bs.get(), f.bs2.get(), f.bs3.get()};
+    double *xx[3] = {f.xs.get(), f.xs2.get(), f.xs3.get()};
+    bicgstab_solve_multi(fd.A, vals, bb, xx, ko, kw, infos.get() + SLOT_K, st);
+    launch_clip_max(f.TE.get(), f.xs.get(), 1.e-9, nc, st);
+    launch_clip_max(f.ED.get(), f.xs2.get(), 1.e-12, nc, st);
+    launch_visc_tur(nc, f.R.get(), f.TE.get(), f.ED.get(), f.VisTur.get(), st);
+    launch_copy(f.T.get(), f.xs3.get(), nc, st);
+    if (cs.has_solid)
+        launch_cht_fluid2solid(d, f.dPhi.get(), f.kcond.get(), f.Bq.get(), sd.view, s.Bq.get(), st);
+}
+
 // NavierStokesSolver::UpdateEnergy, navier_scalar.cpp:257-397
 void SimpleSolver::update_energy() {
     const Params &p = cs.params;
@@ -636,10 +725,15 @@ std::string SimpleSolver::outer_iteration() {
     SYSU_CUDA(cudaMemsetAsync(infos.get(), 0, sizeof(SolveInfo) * (SLOT_N + 3), st));
     calculate_velocity();
     calculate_pressure();
-    if (cs.params.tur_model == 1) update_ke();
-    if (cs.params.solve_energy) {
-        update_energy();
+    if (opt.scalars_batched && cs.params.tur_model == 1 && cs.params.solve_energy) {
+        update_scalars_batched();
         if (cs.has_solid) solid_solve();
+    } else {
+        if (cs.params.tur_model == 1) update_ke();
+        if (cs.params.solve_energy) {
+            update_energy();
+            if (cs.has_solid) solid_solve();
+        }
     }
     ++iter_done;
     return check_iteration();
@@ -660,6 +754,18 @@ std::string SimpleSolver::check_iteration() {
             h[SLOT_MOM].res[c] = h[SLOT_N + c].res[0];
             h[SLOT_MOM].err |= h[SLOT_N + c].err;
         }
+    if (opt.scalars_batched && cs.params.tur_model == 1 && cs.params.solve_energy) {
+        // one batched solve: k, eps, T in the slots of SLOT_K
+        int sl[3] = {SLOT_K, SLOT_EPS, SLOT_T};
+        SolveInfo b = h[SLOT_K];
+        for (int c = 0; c < 3; ++c) {
+            h[sl[c]] = SolveInfo{};
+            h[sl[c]].status[0] = b.status[c];
+            h[sl[c]].iters[0] = b.iters[c];
+            h[sl[c]].res[0] = b.res[c];
+            h[sl[c]].err = b.err;
+        }
+    }
     std::memcpy(last_info, h, sizeof(last_info));
     for (int k = 0; k < 10; ++k) Residual[k] = 0.0;
     Residual[0] = ro[RED_RES0];

@@ -75,6 +75,7 @@ struct SolverOptions {
             e->mixed = 0;
         }
         mom_batched = false;
+        scalars_batched = false;
     }
     // back to the default (fast) mode: BiCGSTAB + Jacobi, CG + Jacobi, batched momentum
     void default_solvers() {
@@ -94,6 +95,11 @@ struct SolverOptions {
     bool timing = false;          // CUDA events around the p' solve
     bool profile_phases = false;  // %globaltimer stamps at the CG phase boundaries
     bool output = false;          // nssolve writes tec/res####.dat and tot.dat like the reference
+    // k, eps and T assembled from the fields at the start of the scalar stage and
+    // solved as one batched BiCGSTAB launch (eps's source and T's conductivity lag
+    // the k and eps of this iteration by one outer iteration); needs k-epsilon and
+    // energy on, BiCGSTAB for ke and t
+    bool scalars_batched = false;
 };
 
 enum SolveSlot { SLOT_MOM = 0, SLOT_P, SLOT_K, SLOT_EPS, SLOT_T, SLOT_TS, SLOT_N };
@@ -111,6 +117,7 @@ struct FieldSet {
     DevBuf<double> diff;  // solid conductivity
     DevBuf<double> Unp, Vnp, Wnp, Tnp, TEp, EDp, tapp;  // transient: last step's fields, time-term diagonal
     DevBuf<float> Ap32, As32;  // FP32 copies for mixed-precision solves
+    DevBuf<double> As2, As3, bs2, bs3, xs2, xs3;  // eps and T systems of the batched scalar form
 };
 
 class SimpleSolver {
@@ -149,6 +156,7 @@ class SimpleSolver {
     void calculate_pressure();
     void update_ke();
     void update_energy();
+    void update_scalars_batched();
     void solid_solve();
     // SaveTransientOldData (navier.cpp:190-240, HeatConductionSolver.cpp:306-327)
     void save_transient_old_data();
