@@ -81,6 +81,8 @@ int sysu_solver_info(sysu_solver *s, long *out, int n);
  *   "scalars_batched" (1: k, eps and T assembled together and solved by one
  *     batched BiCGSTAB launch; eps's source and T's conductivity then lag by
  *     one outer iteration, the steady solution is the same; needs ke + energy);
+ *   "sm_cap" (SMs' worth of blocks the persistent Krylov solves may use, 0 = all;
+ *     set per case by the batch autotuner);
  *   "rtc" sets every eq's eps; "mom_batched" (1: u,v,w as one 3-RHS solve);
  *   "solid_source" (W/m^3, an extension); "fatal_checks"; "timing". */
 int sysu_solver_set_option(sysu_solver *s, const char *key, double value);
@@ -204,6 +206,34 @@ int sysu_csr_cg_noalloc(int n, const int *d_rowptr, const int *d_col, const doub
                         double *d_x, int maxit, double eps, double omega, void *stream, int *iters, double *res,
                         int *status);
 const char *sysu_noalloc_last_error(void);
+
+/* ---- batches of independent cases -----------------------------------------
+ * Many cases (each its own param.in) advanced together: sysu_batch_capture
+ * records one outer iteration of every case into one CUDA graph (each case on
+ * its own branch, so the cases run concurrently; the host is not involved
+ * inside a replay); sysu_batch_replay(n) replays it n times.  The autotuner
+ * (sysu_batch_tune) times one outer iteration of each case alone for every
+ * candidate SM cap (the SMs' worth of blocks its persistent Krylov solves may
+ * use -- the rows per warp of those kernels), then gives SMs to the slowest
+ * case while the caps add up to at most the GPU's SM count; it resets the
+ * cases afterwards.  Cases are reached with sysu_batch_case (borrowed handles:
+ * options, fields, solve statistics; do not destroy them).  Capture after every
+ * option change.  sysu_batch_run_sequential times the cases one after another
+ * with ordinary launches, for comparison. */
+typedef struct sysu_batch sysu_batch;
+int sysu_batch_create(int n, const char *const *params, sysu_batch **out);
+void sysu_batch_free(sysu_batch *b);
+int sysu_batch_size(sysu_batch *b);
+sysu_solver *sysu_batch_case(sysu_batch *b, int k);
+/* caps/ms_alone/ms_full: one value per case (may be NULL) */
+int sysu_batch_tune(sysu_batch *b, const int *cand, int ncand, int *caps, double *ms_alone, double *ms_full,
+                    double *makespan);
+int sysu_batch_set_caps(sysu_batch *b, const int *caps);
+int sysu_batch_capture(sysu_batch *b);
+int sysu_batch_replay(sysu_batch *b, int n, double *ms);
+/* the reference's convergence checks on every case's last iteration */
+int sysu_batch_check(sysu_batch *b);
+int sysu_batch_run_sequential(sysu_batch *b, int n, double *ms);
 
 /* ---- learned preconditioner (message-passing network) -----------------------
  * No counterpart in the reference: a 4-layer, width-32 message-passing network

@@ -74,6 +74,16 @@ def lib() -> C.CDLL:
             "sysu_csr_last_error": (cp, []),
             "sysu_csr_bicgstab_batched3": (C.c_int, [C.c_int, ip, ip, C.POINTER(dp), C.POINTER(dp), C.POINTER(dp),
                                                      C.c_int, C.c_double, ip, dp, ip]),
+            "sysu_batch_create": (C.c_int, [C.c_int, C.POINTER(cp), C.POINTER(vp)]),
+            "sysu_batch_free": (None, [vp]),
+            "sysu_batch_size": (C.c_int, [vp]),
+            "sysu_batch_case": (vp, [vp, C.c_int]),
+            "sysu_batch_tune": (C.c_int, [vp, ip, C.c_int, ip, dp, dp, dp]),
+            "sysu_batch_set_caps": (C.c_int, [vp, ip]),
+            "sysu_batch_capture": (C.c_int, [vp]),
+            "sysu_batch_replay": (C.c_int, [vp, C.c_int, dp]),
+            "sysu_batch_check": (C.c_int, [vp]),
+            "sysu_batch_run_sequential": (C.c_int, [vp, C.c_int, dp]),
             "sysu_gnn_num_params": (C.c_int, []),
             "sysu_gnn_create": (C.c_int, [C.c_int, ip, ip, dp, C.c_int, C.POINTER(vp)]),
             "sysu_gnn_free": (None, [vp]),

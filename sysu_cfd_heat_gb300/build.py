@@ -19,7 +19,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SRCS = ["krylov.cu", "cg.cu", "gmres.cu", "fv.cu", "noalloc.cu", "gnn.cu"]
 CPP_SRCS = ["case.cpp", "solver.cpp", "capi.cpp", "csr_api.cpp", "laspack_gpu.cpp", "output.cpp",
-            "gnn_api.cpp"]
+            "gnn_api.cpp", "batch.cpp"]
 
 
 def _cuda_home() -> str:

@@ -8,6 +8,7 @@
 
 #include <fstream>
 #include <limits>
+#include "batch.hpp"
 #include "handles.hpp"
 #include "output.hpp"
 
@@ -167,6 +168,7 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
         return SYSU_OK;
     }
     if (k == "mom_batched") { o.mom_batched = value != 0.0; return SYSU_OK; }
+    if (k == "sm_cap") { s->impl->kw.sm_cap = std::max(0, (int)value); return SYSU_OK; }
     if (k == "scalars_batched") {
         const sysu::Params &pp = s->impl->cs.params;
         if (value != 0.0 && (pp.tur_model != 1 || !pp.solve_energy))
@@ -269,6 +271,7 @@ int sysu_solver_get_option(sysu_solver *s, const char *key, double *value) {
     std::string k(key);
     if (k == "mom_batched") { *value = o.mom_batched; return SYSU_OK; }
     if (k == "scalars_batched") { *value = o.scalars_batched; return SYSU_OK; }
+    if (k == "sm_cap") { *value = s->impl->kw.sm_cap; return SYSU_OK; }
     if (k == "solid_source") { *value = o.solid_source; return SYSU_OK; }
     if (k == "fatal_checks") { *value = o.fatal_checks; return SYSU_OK; }
     if (k == "timing") { *value = o.timing; return SYSU_OK; }
@@ -557,6 +560,100 @@ int sysu_solver_set_field(sysu_solver *s, const char *name, const double *in, lo
     if (!s || !name || !in) return set_err(SYSU_ERR_INPUT, "null argument");
     return guarded([&] {
         s->impl->set_field(name, in, n);
+        return SYSU_OK;
+    });
+}
+
+// ---- batches of cases (batch.hpp) --------------------------------------------
+
+struct sysu_batch {
+    sysu::CaseBatch *impl;
+};
+
+int sysu_batch_create(int n, const char *const *params, sysu_batch **out) {
+    if (!params || !out || n <= 0) return set_err(SYSU_ERR_INPUT, "sysu_batch_create: bad arguments");
+    *out = nullptr;
+    return guarded([&] {
+        std::vector<std::string> ps;
+        for (int k = 0; k < n; ++k) {
+            if (!params[k]) throw sysu::CaseError{"sysu_batch_create: null param path"};
+            ps.emplace_back(params[k]);
+        }
+        *out = new sysu_batch{new sysu::CaseBatch(ps)};
+        return SYSU_OK;
+    });
+}
+
+void sysu_batch_free(sysu_batch *b) {
+    if (!b) return;
+    try {
+        delete b->impl;
+    } catch (...) {
+    }
+    delete b;
+}
+
+int sysu_batch_size(sysu_batch *b) { return b ? b->impl->size() : 0; }
+
+sysu_solver *sysu_batch_case(sysu_batch *b, int k) {
+    if (!b || k < 0 || k >= b->impl->size()) return nullptr;
+    return b->impl->handle(k);
+}
+
+int sysu_batch_tune(sysu_batch *b, const int *cand, int ncand, int *caps, double *ms_alone, double *ms_full,
+                    double *makespan) {
+    if (!b || !cand || ncand <= 0) return set_err(SYSU_ERR_INPUT, "sysu_batch_tune: bad arguments");
+    return guarded([&] {
+        sysu::TuneResult r = b->impl->tune(std::vector<int>(cand, cand + ncand));
+        for (int k = 0; k < b->impl->size(); ++k) {
+            if (caps) caps[k] = r.sm_cap[k];
+            if (ms_alone) ms_alone[k] = r.ms_alone[k];
+            if (ms_full) ms_full[k] = r.ms_full[k];
+        }
+        if (makespan) *makespan = r.makespan_ms;
+        return SYSU_OK;
+    });
+}
+
+int sysu_batch_set_caps(sysu_batch *b, const int *caps) {
+    if (!b || !caps) return set_err(SYSU_ERR_INPUT, "null argument");
+    return guarded([&] {
+        b->impl->set_caps(std::vector<int>(caps, caps + b->impl->size()));
+        return SYSU_OK;
+    });
+}
+
+int sysu_batch_capture(sysu_batch *b) {
+    if (!b) return set_err(SYSU_ERR_INPUT, "null argument");
+    return guarded([&] {
+        b->impl->capture();
+        return SYSU_OK;
+    });
+}
+
+int sysu_batch_replay(sysu_batch *b, int n, double *ms) {
+    if (!b || n < 0) return set_err(SYSU_ERR_INPUT, "bad arguments");
+    return guarded([&] {
+        double t = b->impl->replay(n);
+        if (ms) *ms = t;
+        return SYSU_OK;
+    });
+}
+
+int sysu_batch_check(sysu_batch *b) {
+    if (!b) return set_err(SYSU_ERR_INPUT, "null argument");
+    return guarded([&] {
+        std::string m = b->impl->check();
+        if (!m.empty()) return set_err(SYSU_ERR_SOLVE, m);
+        return SYSU_OK;
+    });
+}
+
+int sysu_batch_run_sequential(sysu_batch *b, int n, double *ms) {
+    if (!b || n < 0) return set_err(SYSU_ERR_INPUT, "bad arguments");
+    return guarded([&] {
+        double t = b->impl->run_sequential(n);
+        if (ms) *ms = t;
         return SYSU_OK;
     });
 }

@@ -655,7 +655,8 @@ int cg_max_blocks(K kernel) {
     return per_sm * num_sms();
 }
 
-int cg_grid(const SellDev &A, const CgPlan &pl, int maxb) {
+int cg_grid(const SellDev &A, const CgPlan &pl, int maxb, int sm_cap) {
+    if (sm_cap > 0) maxb = std::min(maxb, sm_cap * std::max(1, maxb / num_sms()));
     int tiles = (A.nslices + pl.ts - 1) / pl.ts;
     return std::max(1, std::min(tiles, maxb));
 }
@@ -691,7 +692,7 @@ void cg_solve(const SellDev &A, const double *val, const double *b, double *x, b
     a.ts = w.phase_ts;
     a.plan = plan_cg(A.wmax, 8);
     void *args[] = {&a};
-    int G = cg_grid(A, a.plan, maxb);
+    int G = cg_grid(A, a.plan, maxb, w.sm_cap);
     { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_cg_pipe, dim3(G), dim3(KBC), args, a.plan.smem, st)); ++::sysu::g_launches; }
 }
 
@@ -728,7 +729,7 @@ void cg_solve_mixed(const SellDev &A, const double *val, const float *val32, con
     a.ts = w.phase_ts;
     a.plan = plan_cg(A.wmax, 4);
     void *args[] = {&a};
-    int G = cg_grid(A, a.plan, maxb);
+    int G = cg_grid(A, a.plan, maxb, w.sm_cap);
     { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_cg_mixed_pipe, dim3(G), dim3(KBC), args, a.plan.smem, st)); ++::sysu::g_launches; }
 }
 

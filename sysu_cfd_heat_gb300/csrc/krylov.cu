@@ -468,7 +468,7 @@ static void bicg_launch(const SellDev &A, const double *const *vals, bool multi,
                         double *const *x, const KrylovOpts &o, KrylovWork &w, SolveInfo *info, cudaStream_t st) {
     int n = A.n;
     int maxb = bicg_max_blocks(nrhs, multi);
-    if (w.block_cap > 0) maxb = std::min(maxb, w.block_cap);
+    if (w.sm_cap > 0) maxb = std::min(maxb, w.sm_cap * std::max(1, maxb / num_sms()));
     w.ensure(n, nrhs == 1 ? 1 : 3, bicg_max_blocks(-1, false), st);
     for (int c = 0; c < (multi ? nrhs : 1); ++c) {
         SellView Vc = view(A, vals[c]);

@@ -76,7 +76,9 @@ struct KrylovWork {
     DevBuf<long long> gpart;                         // exact multi-value partial sums
     DevBuf<GridBarrier> barrier;
     unsigned long long *phase_ts = nullptr;  // optional: 4 timestamps per CG iteration, first 64
-    int block_cap = 0;  // > 0: at most this many blocks per persistent solve (cases sharing the GPU)
+    // > 0: the persistent solves of this work use at most this many SMs' worth of
+    // blocks (cases that share the GPU; the batch autotuner sets it)
+    int sm_cap = 0;
     void ensure(int n, int nrhs, int max_blocks, cudaStream_t st);
     void ensure32(int n, cudaStream_t st);
 };

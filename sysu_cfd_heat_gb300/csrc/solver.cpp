@@ -722,6 +722,12 @@ void SimpleSolver::save_transient_old_data() {
 }
 
 std::string SimpleSolver::outer_iteration() {
+    enqueue_iteration();
+    ++iter_done;
+    return check_iteration();
+}
+
+void SimpleSolver::enqueue_iteration() {
     SYSU_CUDA(cudaMemsetAsync(infos.get(), 0, sizeof(SolveInfo) * (SLOT_N + 3), st));
     calculate_velocity();
     calculate_pressure();
@@ -735,8 +741,6 @@ std::string SimpleSolver::outer_iteration() {
             if (cs.has_solid) solid_solve();
         }
     }
-    ++iter_done;
-    return check_iteration();
 }
 
 std::string SimpleSolver::check_iteration() {

@@ -157,6 +157,10 @@ class SimpleSolver {
     void update_ke();
     void update_energy();
     void update_scalars_batched();
+    // the device work of one outer iteration, enqueued on st without any host
+    // synchronisation (capturable into a CUDA graph); outer_iteration() is this
+    // plus check_iteration()
+    void enqueue_iteration();
     void solid_solve();
     // SaveTransientOldData (navier.cpp:190-240, HeatConductionSolver.cpp:306-327)
     void save_transient_old_data();

@@ -329,6 +329,19 @@ def cavity_param(gridfile: str, iters: int, mu: float, rho: float = 1.0, urf=(0.
     ]
 
 
+def batch_cavities(n_cases: int = 48, lmin: int = 12, lmax: int = 64, re_min: float = 50.0,
+                   re_max: float = 1000.0, seed: int = DEFAULT_SEED) -> List[tuple]:
+    """(edge cells L, Reynolds number) of the many-cavity batch: L uniform on
+    {lmin..lmax}, Re uniform on [re_min, re_max], from the counter-based generator
+    (draw 2k for L, 2k+1 for Re of case k)."""
+    u = splitmix64_uniform(seed, np.arange(2 * n_cases))
+    out = []
+    for k in range(n_cases):
+        L = lmin + min(int(u[2 * k] * (lmax - lmin + 1)), lmax - lmin)
+        out.append((L, float(re_min + u[2 * k + 1] * (re_max - re_min))))
+    return out
+
+
 def cht_param(gridfile: str, iters: int, u_in: float = 1.0, nu: float = 1e-5, rho: float = 1.0,
               t_in: float = 300.0, t_wall: float = 400.0, k_solid: float = 15.0, rho_solid: float = 1.0,
               turb: bool = True, urf=(0.7, 0.3, 0.8), limiter: str = "no", intensity: float = 0.05,

@@ -43,10 +43,21 @@ class NavierStokesSolver:
         if self.info()["solid_Ncel"] > 0:
             self.physicalModule["3dHeatConduction"] = HeatConductionSolver(self)
 
+    @classmethod
+    def _borrow(cls, handle: int) -> "NavierStokesSolver":
+        """A view of a solver owned elsewhere (a case of a batch): close() does not free it."""
+        self = cls.__new__(cls)
+        self._h = C.c_void_p(handle)
+        self._borrowed = True
+        self.physicalModule = {}
+        if self.info()["solid_Ncel"] > 0:
+            self.physicalModule["3dHeatConduction"] = HeatConductionSolver(self)
+        return self
+
     def close(self) -> None:
-        if self._h:
+        if self._h and not getattr(self, "_borrowed", False):
             lib().sysu_solver_destroy(self._h)
-            self._h = C.c_void_p()
+        self._h = C.c_void_p()
 
     def __del__(self):
         try:

@@ -1,0 +1,47 @@
+"""Many cases in one CUDA graph (sysu_batch_*): the graph replays give exactly the
+fields of each case run alone with the same SM cap, the autotuner's caps fit the
+GPU, and the reference's convergence checks pass on every case."""
+import tempfile
+
+import numpy as np
+import pytest
+
+from sysu_cfd_heat_gb300 import meshgen as mg
+from sysu_cfd_heat_gb300.batch import CaseBatch
+from sysu_cfd_heat_gb300.solver import NavierStokesSolver
+
+pytestmark = pytest.mark.gpu
+OPTS = {"rtc": 1e-8, "p.mixed": 1, "p.maxit": 5000}
+
+
+def _cases(d, spec):
+    out = []
+    for k, (L, re) in enumerate(spec):
+        sub = f"{d}/c{k}"
+        out.append(mg.write_case(sub, mg.lid_cavity_hex(L), mg.cavity_param("x", 1000, mu=1.0 / re)))
+    return out
+
+
+def test_graph_replay_equals_cases_alone():
+    spec = [(6, 100.0), (11, 400.0), (14, 900.0), (9, 50.0)]
+    iters = 12
+    with tempfile.TemporaryDirectory() as d:
+        params = _cases(d, spec)
+        with CaseBatch(params, OPTS) as b:
+            t = b.tune((1, 2, 4, 8))
+            assert sum(t["sm_cap"]) <= 152 and all(c >= 1 for c in t["sm_cap"])
+            b.capture()
+            b.replay(iters)
+            b.check()
+            got = [{f: s.get(f) for f in ("U", "V", "W", "P")} for s in b.cases]
+            caps = t["sm_cap"]
+        for k, p in enumerate(params):
+            with NavierStokesSolver(p, dict(OPTS, sm_cap=caps[k])) as s:
+                assert s.iterate(iters) == iters
+                for f in ("U", "V", "W", "P"):
+                    assert np.array_equal(s.get(f), got[k][f]), (k, f)
+            with NavierStokesSolver(p, OPTS) as s:  # no cap: other grids, same solution
+                s.iterate(iters)
+                for f in ("U", "V", "W", "P"):
+                    a = s.get(f)
+                    assert np.linalg.norm(a - got[k][f]) <= 1e-7 * np.linalg.norm(a) + 1e-14, (k, f)
