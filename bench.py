@@ -242,6 +242,68 @@ def config_of(args):
             "parallelism": "replicas"}
 
 
+def batch_case_dirs():
+    """The 48 lid-driven hex cavities of the batch form (edge 12..64 cells, Re 50..1000)."""
+    from sysu_cfd_heat_gb300 import meshgen as mg
+
+    out = []
+    for k, (L, re) in enumerate(mg.batch_cavities()):
+        d = os.path.join(tempfile.gettempdir(), f"sysu_bench_batch_s{SEED}_{k}_{L}")
+        p = os.path.join(d, "param.in")
+        if not os.path.exists(p):
+            tmp = d + ".tmp%d" % os.getpid()
+            mg.write_case(tmp, mg.lid_cavity_hex(L), mg.cavity_param("x", 100000, mu=1.0 / re))
+            try:
+                os.rename(tmp, d)
+            except OSError:
+                pass
+        out.append((p, L, re))
+    return out
+
+
+def batch_form(args):
+    """48 independent cavities advanced together: one CUDA graph replay = one outer
+    iteration of every case (each case on its own graph branch), p' in FP32 CG with
+    FP64 reliable updates, each case's persistent-solver grid (SMs, i.e. rows per
+    warp) chosen by the autotuner; against the same cases run one after another
+    with ordinary launches and full-GPU grids."""
+    from sysu_cfd_heat_gb300.batch import CaseBatch, DEFAULT_CAPS
+
+    t0 = time.perf_counter()
+    cases = batch_case_dirs()
+    gen_s = time.perf_counter() - t0
+    cells = sum(L ** 3 for _, L, _ in cases)
+    with CaseBatch([p for p, _, _ in cases], {"rtc": RTC, "p.mixed": 1}) as b:
+        t0 = time.perf_counter()
+        tune = b.tune(DEFAULT_CAPS)
+        tune_s = time.perf_counter() - t0
+        b.capture()
+        b.replay(args.warmup)
+        for c in b.cases:
+            c.reset()
+        ms = b.replay(args.steps)
+        b.check()
+        b.set_caps([0] * len(cases))
+        for c in b.cases:
+            c.reset()
+        b.run_sequential(1)
+        for c in b.cases:
+            c.reset()
+        seq_ms = b.run_sequential(args.steps)
+    return {"cases": len(cases), "cells_total": cells, "edge_cells": [L for _, L, _ in cases],
+            "reynolds": [round(re, 1) for _, _, re in cases],
+            "batch_iters_per_s": args.steps / (ms / 1000.0),
+            "case_iters_per_s": len(cases) * args.steps / (ms / 1000.0),
+            "cell_iters_per_s": cells * args.steps / (ms / 1000.0),
+            "ms_per_batch_iteration": ms / args.steps,
+            "sequential_ms_per_batch_iteration": seq_ms / args.steps,
+            "speedup_vs_sequential": seq_ms / ms if ms > 0 else None,
+            "precision": "momentum BiCGSTAB FP64, p' CG FP32 recurrences + FP64 reliable updates, eps 1e-8",
+            "autotuner": {"candidates_sms": list(DEFAULT_CAPS), "sm_cap": tune["sm_cap"],
+                          "model_makespan_ms": tune["makespan_ms"], "seconds": tune_s},
+            "mesh_generation_seconds": gen_s}
+
+
 def learned_form(s, args, to8, field_err):
     """The learned + FP32 form: p' by flexible CG preconditioned by the message-passing
     network (FP32 recurrences, FP64 reliable updates, Jacobi fallback).  The network
@@ -459,6 +521,9 @@ def run_ours(args, r, w, lr):
 
     # standalone SpMV sweep on the assembled matrices after outer iterations 1, 10, 100
     forms["spmv_sweep"] = spmv_sweep(s, n, nnz, hbm) if not args.p_maxit and not args.p_mixed else None
+    # the batched k, eps, T form needs a k-epsilon + energy case: not this cavity
+    forms["batch_48_cavities"] = (batch_form(args) if args.workload == "c3" and not args.p_maxit
+                                  and not args.p_mixed and not args.no_batch else None)
 
     out = {
         "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": w, "steps": args.steps,
@@ -503,6 +568,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c3", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 48-cavity batch form")
     ap.add_argument("--cpu-budget", type=float, default=240.0)
     ap.add_argument("--ref-budget", type=float, default=150.0)
     ap.add_argument("--p-maxit", type=int, default=0,

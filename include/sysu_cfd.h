@@ -214,9 +214,10 @@ const char *sysu_noalloc_last_error(void);
  * inside a replay); sysu_batch_replay(n) replays it n times.  The autotuner
  * (sysu_batch_tune) times one outer iteration of each case alone for every
  * candidate SM cap (the SMs' worth of blocks its persistent Krylov solves may
- * use -- the rows per warp of those kernels), then gives SMs to the slowest
- * case while the caps add up to at most the GPU's SM count; it resets the
- * cases afterwards.  Cases are reached with sysu_batch_case (borrowed handles:
+ * use -- the rows per warp of those kernels), then raises caps one step at a
+ * time where that lowers the model makespan max(slowest case, SM-time / SMs),
+ * while the caps add up to at most the GPU's SM count; the graph then issues
+ * the longest cases first.  It resets the cases afterwards.  Cases are reached with sysu_batch_case (borrowed handles:
  * options, fields, solve statistics; do not destroy them).  Capture after every
  * option change.  sysu_batch_run_sequential times the cases one after another
  * with ordinary launches, for comparison. */

@@ -92,36 +92,53 @@ TuneResult CaseBatch::tune(const std::vector<int> &candidates) {
         c.kw.sm_cap = 0;
         c.reset();
     }
-    // greedy: start every case at the smallest cap; repeatedly move the slowest
-    // case to its next cap while the caps add up to at most the SM count and the
-    // move makes it faster
+    // greedy on the model makespan J = max(slowest case alone, SM-time / SMs):
+    // start every case at the smallest cap and keep applying the single
+    // one-step cap increase that lowers J most, while the caps fit the GPU
     std::vector<size_t> pick(nc, 0);
-    auto used = [&]() {
+    auto model = [&](const std::vector<size_t> &pk, long *used) {
+        double tmax = 0.0, area = 0.0;
         long u = 0;
-        for (int k = 0; k < nc; ++k) u += cand[pick[k]];
-        return u;
+        for (int k = 0; k < nc; ++k) {
+            double tk = t[k][pk[k]];
+            tmax = std::max(tmax, tk);
+            area += tk * cand[pk[k]];
+            u += cand[pk[k]];
+        }
+        if (used) *used = u;
+        return std::max(tmax, area / S);
     };
+    double J = model(pick, nullptr);
     for (;;) {
-        int worst = -1;
-        double tw = -1.0;
-        for (int k = 0; k < nc; ++k)
-            if (t[k][pick[k]] > tw) {
-                tw = t[k][pick[k]];
-                worst = k;
+        int best = -1;
+        double bestJ = J;
+        for (int k = 0; k < nc; ++k) {
+            if (pick[k] + 1 >= cand.size()) continue;
+            std::vector<size_t> trial(pick);
+            ++trial[k];
+            long u = 0;
+            double j = model(trial, &u);
+            if (u <= S && j < bestJ - 1e-9) {
+                bestJ = j;
+                best = k;
             }
-        size_t nx = pick[worst] + 1;
-        if (nx >= cand.size() || t[worst][nx] >= tw || used() - cand[pick[worst]] + cand[nx] > S) break;
-        pick[worst] = nx;
+        }
+        if (best < 0) break;
+        ++pick[best];
+        J = bestJ;
     }
     r.sm_cap.resize(nc);
     r.ms_alone.resize(nc);
-    r.makespan_ms = 0.0;
+    r.makespan_ms = J;
     for (int k = 0; k < nc; ++k) {
         r.sm_cap[k] = cand[pick[k]];
         r.ms_alone[k] = t[k][pick[k]];
-        r.makespan_ms = std::max(r.makespan_ms, r.ms_alone[k]);
     }
     set_caps(r.sm_cap);
+    // the graph issues the longest cases first
+    order_.resize(nc);
+    for (int k = 0; k < nc; ++k) order_[k] = k;
+    std::stable_sort(order_.begin(), order_.end(), [&](int a, int b) { return r.ms_alone[a] > r.ms_alone[b]; });
     return r;
 }
 
@@ -141,7 +158,11 @@ void CaseBatch::capture() {
     SYSU_CUDA(cudaStreamBeginCapture(main_, cudaStreamCaptureModeThreadLocal));
     try {
         SYSU_CUDA(cudaEventRecord(fork_, main_));
-        for (int k = 0; k < size(); ++k) {
+        if ((int)order_.size() != size()) {
+            order_.resize(size());
+            for (int k = 0; k < size(); ++k) order_[k] = k;
+        }
+        for (int k : order_) {
             SimpleSolver &c = at(k);
             SYSU_CUDA(cudaStreamWaitEvent(c.st, fork_, 0));
             c.enqueue_iteration();

@@ -15,7 +15,7 @@ struct TuneResult {
     std::vector<int> sm_cap;        // chosen SMs per case
     std::vector<double> ms_alone;   // one outer iteration at that cap, case alone
     std::vector<double> ms_full;    // one outer iteration with no cap, case alone
-    double makespan_ms = 0.0;       // max over cases of ms_alone (the model's estimate)
+    double makespan_ms = 0.0;       // the model's makespan: max(slowest case, SM-time / SMs)
 };
 
 class CaseBatch {
@@ -30,8 +30,9 @@ class CaseBatch {
     SimpleSolver &at(int k) { return *cases[k]->impl; }
 
     // Time one outer iteration of every case alone for each candidate SM cap,
-    // then give SMs greedily to the slowest case while the caps fit the GPU.
-    // The cases are reset to their initial state afterwards.
+    // then choose caps greedily against the makespan model max(slowest case,
+    // SM-time / SMs) while the caps fit the GPU; the graph issues the longest
+    // cases first.  The cases are reset to their initial state afterwards.
     TuneResult tune(const std::vector<int> &candidates);
     void set_caps(const std::vector<int> &caps);
     // One eager iteration per case (allocates every buffer), a reset, then the
@@ -49,6 +50,7 @@ class CaseBatch {
     cudaStream_t main_ = nullptr;
     cudaEvent_t fork_ = nullptr, t0_ = nullptr, t1_ = nullptr;
     std::vector<cudaEvent_t> join_;
+    std::vector<int> order_;  // capture order of the cases (longest first after tune)
     cudaGraphExec_t exec_ = nullptr;
     long graph_launches_ = 0;
 };
