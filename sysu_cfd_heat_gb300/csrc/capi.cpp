@@ -182,6 +182,9 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
     if (k == "reference_solvers") {
         if (value != 0.0) o.reference_solvers();
         else o.default_solvers();
+        // perfect gas: p' is not symmetric, the reference solves it with GMRES
+        // (navier_pressure.cpp:28-31)
+        if (s->impl->cs.params.density_model == 1) o.p.kind = value != 0.0 ? sysu::SK_GMRES : sysu::SK_BICGSTAB;
         return SYSU_OK;
     }
     if (k == "solid_source") { o.solid_source = value; return SYSU_OK; }
@@ -222,6 +225,8 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
                 if (kind != sysu::SK_CG && kind != sysu::SK_BICGSTAB && kind != sysu::SK_GMRES)
                     return set_err(SYSU_ERR_INPUT, "kind: 0 CG, 1 BiCGSTAB, 2 GMRES");
                 if (kind == sysu::SK_CG && e == &o.mom) return set_err(SYSU_ERR_INPUT, "momentum matrix is not symmetric");
+                if (kind == sysu::SK_CG && e == &o.p && s->impl->cs.params.density_model == 1)
+                    return set_err(SYSU_ERR_INPUT, "the perfect-gas p' matrix is not symmetric");
                 if (kind == sysu::SK_BICGSTAB && e->precond > sysu::PK_JACOBI)
                     return set_err(SYSU_ERR_INPUT, "BiCGSTAB runs with no or the Jacobi preconditioner");
                 if (kind != sysu::SK_CG) e->mixed = 0;

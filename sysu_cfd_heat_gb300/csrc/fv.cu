@@ -496,7 +496,9 @@ __global__ void k_rhie_chow(DomView d, PresArgs a) {
 __global__ void k_pressure_cell(DomView d, PresArgs a) {
     int i = blockIdx.x * NB + threadIdx.x;
     if (i >= d.nc) return;
+    const bool gas = a.density_model == 1;
     double valcen = 0., bpv = 0.;
+    if (gas && a.transient) valcen += -d.vol[i] / (a.dt * a.rcpcv * a.T[i]);
     for (int s = d.cs_ptr[i]; s < d.cs_ptr[i + 1]; ++s) {
         int f = d.cs_face[s];
         bool first = d.fc1[f] == i;
@@ -506,11 +508,78 @@ __global__ void k_pressure_cell(DomView d, PresArgs a) {
         if (f < d.F) {
             double tmp = a.fcoef[f];
             valcen += -tmp;
-            a.val[sell_pos(d.A, i, d.cs_k[s])] = tmp;
+            double aij = tmp;
+            if (gas) {  // navier_pressure.cpp:165-181
+                int in = first ? d.fc2[f] : d.fc1[f];
+                double lambda = first ? d.flam[f] : 1. - d.flam[f];
+                double lambda2 = 1. - lambda;
+                double RUn = first ? RU : -RU;
+                double rof = lambda * a.R[i] + lambda2 * a.R[in];
+                if (RUn > 0.) valcen += -RUn / (rof * a.rcpcv * a.T[i]);
+                if (RUn < 0.) aij += -RUn / (rof * a.rcpcv * a.T[in]);
+            }
+            a.val[sell_pos(d.A, i, d.cs_k[s])] = aij;
+        } else if (gas) {  // navier_pressure.cpp:118-133
+            int b = f - d.F;
+            int type = d.btype1[b];
+            if (type == 2) valcen += fmin(RU, 0.) / (a.BRo[b] * a.rcpcv * a.T[i]);
+            else if (type == 3) valcen += fmax(RU, 0.) / (a.R[i] * a.rcpcv * a.T[i]);
         }
     }
     a.val[sell_pos(d.A, i, 0)] = valcen;
     a.bp[i] = bpv;
+}
+
+// navier_scalar.cpp:277-338, gathered per cell (+ for the face's cell1, - for cell2)
+__global__ void k_energy_viscous(DomView d, const double *VisLam, const double *VisTur, const double *dU,
+                                 const double *dV, const double *dW, const double *U, const double *V,
+                                 const double *W, double cp, double *src) {
+    int i = blockIdx.x * NB + threadIdx.x;
+    if (i >= d.nc) return;
+    const int nc = d.nc, nf = d.nf;
+    double acc = src[i];
+    for (int s = d.cs_ptr[i]; s < d.cs_ptr[i + 1]; ++s) {
+        int f = d.cs_face[s];
+        int c1 = d.fc1[f], c2 = d.fc2[f];
+        double VisL, VisT, g[9], vx, vy, vz;
+        const double *gr[3] = {dU, dV, dW};
+        if (c2 < 0) {
+            VisL = VisLam[c1];
+            VisT = VisTur[c1];
+            for (int q = 0; q < 3; ++q)
+                for (int k = 0; k < 3; ++k) g[3 * q + k] = gr[q][(size_t)k * nc + c1];
+            vx = U[c1];
+            vy = V[c1];
+            vz = W[c1];
+        } else {
+            double lambda = d.flam[f], lambda2 = 1. - lambda;
+            VisL = lambda * VisLam[c1] + lambda2 * VisLam[c2];
+            VisT = lambda * VisTur[c1] + lambda2 * VisTur[c2];
+            for (int q = 0; q < 3; ++q)
+                for (int k = 0; k < 3; ++k)
+                    g[3 * q + k] = lambda * gr[q][(size_t)k * nc + c1] + lambda2 * gr[q][(size_t)k * nc + c2];
+            vx = lambda * U[c1] + lambda2 * U[c2];
+            vy = lambda * V[c1] + lambda2 * V[c2];
+            vz = lambda * W[c1] + lambda2 * W[c2];
+        }
+        double dudx = g[0], dudy = g[1], dudz = g[2], dvdx = g[3], dvdy = g[4], dvdz = g[5];
+        double dwdx = g[6], dwdy = g[7], dwdz = g[8];
+        double vmul = VisL + VisT;
+        double vlac = -2. / 3. * vmul;
+        double div = dudx + dvdy + dwdz;
+        double txx = 2. * vmul * dudx + vlac * div;
+        double tyy = 2. * vmul * dvdy + vlac * div;
+        double tzz = 2. * vmul * dwdz + vlac * div;
+        double txy = vmul * (dudy + dvdx);
+        double txz = vmul * (dudz + dwdx);
+        double tyz = vmul * (dvdz + dwdy);
+        double btx = vx * txx + vy * txy + vz * txz;
+        double bty = vx * txy + vy * tyy + vz * tyz;
+        double btz = vx * txz + vy * tyz + vz * tzz;
+        double fvis = (btx * d.fn[f] + bty * d.fn[nf + f] + btz * d.fn[2 * nf + f]) / cp;
+        acc += (c1 == i) ? fvis : -fvis;
+    }
+    src[i] = acc;
 }
 
 // navier_pressure.cpp:38-56
@@ -522,7 +591,12 @@ __global__ void k_correct_cells(DomView d, CorrArgs a, RedScratch rs) {
         double dpi = a.dp[i];
         double vol = d.vol[i];
         v[0] += fabs(dpi - dpref) * vol;
-        a.P[i] = a.P[i] + a.urf_p * (dpi - dpref);
+        if (a.density_model == 1) {  // navier_pressure.cpp:45-48
+            a.P[i] = a.P[i] + a.urf_p * dpi;
+            a.R[i] += dpi / (a.rcpcv * a.T[i]);
+        } else {
+            a.P[i] = a.P[i] + a.urf_p * (dpi - dpref);
+        }
         double coef = vol * a.Apr[i];
         a.U[i] = a.U[i] - coef * a.dPdp[i];
         a.V[i] = a.V[i] - coef * a.dPdp[n + i];
@@ -535,7 +609,8 @@ __global__ void k_correct_cells(DomView d, CorrArgs a, RedScratch rs) {
 // CorrectRUFace2, navier_pressure.cpp:200-242
 __global__ void k_correct_faces(DomView d, const double *dp, const double *dPdp, const double *R,
                                 const double *Apr, const double *BRo, const double *BU, const double *BV,
-                                const double *BW, double urf_p, double *RUFace, const double *fcoef) {
+                                const double *BW, double urf_p, double *RUFace, const double *fcoef,
+                                int density_model, const double *T, double rcpcv) {
     int f = blockIdx.x * NB + threadIdx.x;
     if (f >= d.nf) return;
     const int nc = d.nc, nf = d.nf, F = d.F;
@@ -551,6 +626,15 @@ __global__ void k_correct_faces(DomView d, const double *dp, const double *dPdp,
     double dx20 = d.fxnac[f] - d.cx[c2], dx21 = d.fxnac[F + f] - d.cx[nc + c2],
            dx22 = d.fxnac[2 * F + f] - d.cx[2 * nc + c2];
     double coef = fcoef[f];
+    if (density_model == 1) {  // rho' u, and rho Apr from the corrected density
+        double lambda = d.flam[f], lambda2 = 1. - lambda;
+        double rop = dp[c1] / (rcpcv * T[c1]) * lambda + dp[c2] / (rcpcv * T[c2]) * lambda2;
+        double rof = R[c1] * lambda + R[c2] * lambda2;
+        RUFace[f] += RUFace[f] * rop / rof;
+        double roapf = R[c1] * Apr[c1] * lambda + R[c2] * Apr[c2] * lambda2;
+        double vol = d.vol[c1] * lambda + d.vol[c2] * lambda2;
+        coef = roapf * vol * d.frl[f];
+    }
     double dp1 = dp[c1] + urf_p * (dPdp[c1] * dx10 + dPdp[nc + c1] * dx11 + dPdp[2 * nc + c1] * dx12);
     double dp2 = dp[c2] + urf_p * (dPdp[c2] * dx20 + dPdp[nc + c2] * dx21 + dPdp[2 * nc + c2] * dx22);
     RUFace[f] += -coef * (dp2 - dp1);
@@ -935,6 +1019,14 @@ void launch_commit3(const DomView &d, double *U, double *V, double *W, const dou
     CHECK_LAUNCH();
 }
 
+void launch_energy_viscous(const DomView &d, const double *VisLam, const double *VisTur, const double *dU,
+                           const double *dV, const double *dW, const double *U, const double *V, const double *W,
+                           double cp, double *src, cudaStream_t st) {
+    if (d.nc == 0) return;
+    { k_energy_viscous<<<nblk(d.nc), NB, 0, st>>>(d, VisLam, VisTur, dU, dV, dW, U, V, W, cp, src); ++::sysu::g_launches; }
+    CHECK_LAUNCH();
+}
+
 void launch_pressure_assembly(const DomView &d, const PresArgs &a, cudaStream_t st) {
     { k_rhie_chow<<<nblk(d.nf), NB, 0, st>>>(d, a); ++::sysu::g_launches; }
     { k_pressure_cell<<<nblk(d.nc), NB, 0, st>>>(d, a); ++::sysu::g_launches; }
@@ -948,8 +1040,9 @@ void launch_correct_cells(const DomView &d, const CorrArgs &a, RedScratch rs, cu
 
 void launch_correct_faces(const DomView &d, const double *dp, const double *dPdp, const double *R,
                           const double *Apr, const double *BRo, const double *BU, const double *BV,
-                          const double *BW, double urf_p, double *RUFace, const double *fcoef, cudaStream_t st) {
-    { k_correct_faces<<<nblk(d.nf), NB, 0, st>>>(d, dp, dPdp, R, Apr, BRo, BU, BV, BW, urf_p, RUFace, fcoef); ++::sysu::g_launches; }
+                          const double *BW, double urf_p, double *RUFace, const double *fcoef, int density_model,
+                          const double *T, double rcpcv, cudaStream_t st) {
+    { k_correct_faces<<<nblk(d.nf), NB, 0, st>>>(d, dp, dPdp, R, Apr, BRo, BU, BV, BW, urf_p, RUFace, fcoef, density_model, T, rcpcv); ++::sysu::g_launches; }
     CHECK_LAUNCH();
 }
 

@@ -106,25 +106,44 @@ struct PresArgs {
     const double *BRo, *BU, *BV, *BW;
     double *RUFace;        // out: Rhie-Chow flux (internal face order)
     double *fcoef;         // out: (rho Apr)_f vol_f rlencos per interior face
-    double *val, *bp;      // p' matrix (full symmetric storage) and right-hand side
+    double *val, *bp;      // p' matrix (full storage) and right-hand side
+    // density model 1 (perfect gas, navier_pressure.cpp:96-100,118-133,165-181):
+    // compressibility terms; the matrix is then not symmetric
+    int density_model;
+    const double *T;
+    double rcpcv;
+    int transient;
+    double dt;
 };
 // CalRUFace2 (navier_velocity.cpp:389-442) + BuildPressureMatrix (navier_pressure.cpp:78-198)
 void launch_pressure_assembly(const DomView &d, const PresArgs &a, cudaStream_t st);
 
 struct CorrArgs {
     const double *dp, *dPdp;   // p' and its gradient
-    const double *Apr, *R;
+    const double *Apr;
+    double *R;                 // corrected for density model 1 (navier_pressure.cpp:45-48)
     double *P, *U, *V, *W;
     double urf_p;
     int cell_ref;
+    int density_model;
+    const double *T;
+    double rcpcv;
 };
 // navier_pressure.cpp:38-56: Residual[3], pressure and velocity correction
 void launch_correct_cells(const DomView &d, const CorrArgs &a, RedScratch rs, cudaStream_t st);
 // CorrectRUFace2, navier_pressure.cpp:200-242 (density model 0)
 // (the face coefficient of the p' assembly, fcoef, is reused: Apr and rho are unchanged)
+// Density model 1: the face coefficient is recomputed from the corrected density
+// and the flux gains the rho' u term (navier_pressure.cpp:225-234).
 void launch_correct_faces(const DomView &d, const double *dp, const double *dPdp, const double *R,
                           const double *Apr, const double *BRo, const double *BU, const double *BV,
-                          const double *BW, double urf_p, double *RUFace, const double *fcoef, cudaStream_t st);
+                          const double *BW, double urf_p, double *RUFace, const double *fcoef, int density_model,
+                          const double *T, double rcpcv, cudaStream_t st);
+// Viscous work source of the energy equation for density model 1
+// (navier_scalar.cpp:277-338): src[i] += sum over i's faces of +-fvis_f.
+void launch_energy_viscous(const DomView &d, const double *VisLam, const double *VisTur, const double *dU,
+                           const double *dV, const double *dW, const double *U, const double *V, const double *W,
+                           double cp, double *src, cudaStream_t st);
 // Bphi[b] = phi(cell of b) for every record: SetBCPressure / SetBCDeltaP (navier_bc.cpp:110-162)
 void launch_bnd_from_cell(const DomView &d, const double *phi, double *Bphi, cudaStream_t st);
 

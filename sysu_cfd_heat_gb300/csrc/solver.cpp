@@ -190,7 +190,10 @@ SimpleSolver::SimpleSolver(const std::string &param_path) {
         raw = read_msh(param_path.substr(0, slash + 1) + grid);
     }
     const Params &p = cs.params;
-    if (p.density_model != 0) throw CaseError{"density model 1 (ideal gas) is not supported by the GPU path"};
+    if (p.density_model != 0 && p.density_model != 1) throw CaseError{"no such density model"};
+    // perfect gas: the p' matrix is not symmetric (the reference switches p' to
+    // GMRES, navier_pressure.cpp:28-31); the default mode runs it with BiCGSTAB
+    if (p.density_model == 1) opt.p.kind = SK_BICGSTAB;
     if (p.heat_conduction && !p.solve_energy)
         throw CaseError{"must turn on SolveEnergy, if Solve3DHeatConduction is on"};
     build_case(raw, cs);
@@ -267,6 +270,7 @@ void SimpleSolver::init_flow_field() {
     auto apply = [&](int i, const double *iv, size_t niv) {
         auto at = [&](size_t k) { return k < niv ? iv[k] : 0.0; };
         U[i] = at(0); V[i] = at(1); W[i] = at(2); R[i] = at(3); T[i] = at(4); P[i] = 0.0;
+        if (p.density_model == 1) R[i] = (P[i] + p.pressure_reference) / (p.rcpcv() * T[i]);
         VL[i] = at(5);
         VT[i] = 0.;
         if (p.tur_model == 1) {
@@ -432,7 +436,7 @@ void SimpleSolver::calculate_velocity() {
     const DomView &d = fd.view;
     int nc = fd.nc;
     launch_bc_velocity(d, f.R.get(), f.U.get(), f.V.get(), f.W.get(), f.BRo.get(), f.BU.get(), f.BV.get(),
-                       f.BW.get(), fd.has_outlet, rs, st);
+                       f.BW.get(), fd.has_outlet && p.density_model == 0, rs, st);
     launch_bnd_from_cell(d, f.P.get(), f.BPre.get(), st);
     const double *phi[4] = {f.U.get(), f.V.get(), f.W.get(), f.P.get()};
     const double *Bphi[4] = {f.BU.get(), f.BV.get(), f.BW.get(), f.BPre.get()};
@@ -472,12 +476,14 @@ void SimpleSolver::calculate_pressure() {
     const Params &p = cs.params;
     const DomView &d = fd.view;
     launch_bc_velocity(d, f.R.get(), f.U.get(), f.V.get(), f.W.get(), f.BRo.get(), f.BU.get(), f.BV.get(),
-                       f.BW.get(), fd.has_outlet, rs, st);
+                       f.BW.get(), fd.has_outlet && p.density_model == 0, rs, st);
     PresArgs pa{};
     pa.U = f.U.get(); pa.V = f.V.get(); pa.W = f.W.get(); pa.R = f.R.get(); pa.P = f.P.get();
     pa.dP = f.dP.get(); pa.Apr = f.Apr.get();
     pa.BRo = f.BRo.get(); pa.BU = f.BU.get(); pa.BV = f.BV.get(); pa.BW = f.BW.get();
     pa.RUFace = f.RUFace.get(); pa.fcoef = f.fcoef.get(); pa.val = f.Ap.get(); pa.bp = f.bp.get();
+    pa.density_model = p.density_model; pa.T = f.T.get(); pa.rcpcv = p.rcpcv();
+    pa.transient = tscheme() != 0; pa.dt = p.dt;
     launch_pressure_assembly(d, pa, st);
     const double *b[1] = {f.bp.get()};
     double *x[1] = {f.xp.get()};
@@ -494,11 +500,13 @@ void SimpleSolver::calculate_pressure() {
     ca.P = f.P.get(); ca.U = f.U.get(); ca.V = f.V.get(); ca.W = f.W.get();
     ca.urf_p = p.urf[3];
     ca.cell_ref = p.cell_pressure_ref;
+    ca.density_model = p.density_model; ca.T = f.T.get(); ca.rcpcv = p.rcpcv();
     launch_correct_cells(d, ca, rs, st);
     launch_bc_velocity(d, f.R.get(), f.U.get(), f.V.get(), f.W.get(), f.BRo.get(), f.BU.get(), f.BV.get(),
-                       f.BW.get(), fd.has_outlet, rs, st);
+                       f.BW.get(), fd.has_outlet && p.density_model == 0, rs, st);
     launch_correct_faces(d, f.xp.get(), f.dP.get(), f.R.get(), f.Apr.get(), f.BRo.get(), f.BU.get(), f.BV.get(),
-                         f.BW.get(), p.urf[3], f.RUFace.get(), f.fcoef.get(), st);
+                         f.BW.get(), p.urf[3], f.RUFace.get(), f.fcoef.get(), p.density_model, f.T.get(), p.rcpcv(),
+                         st);
 }
 
 // UpdateTurKEpsilon, navier_scalar.cpp:14-172
@@ -609,13 +617,7 @@ void SimpleSolver::update_scalars_batched() {
         grad_limited(fd, f, 1, phi, Bphi, grad);
         ScalarArgs ta = sa;
         ta.phi = f.T.get(); ta.Bphi = f.BTem.get(); ta.diff = f.kcond.get(); ta.src = f.zeros.get(); ta.app0 = f.zeros.get();
-        if (tscheme()) {
-            launch_fill(f.src.get(), 0.0, nc, st);
-            launch_fill(f.tapp.get(), 0.0, nc, st);
-            launch_time_term(nc, f.R.get(), fd.vol.get(), p.dt, tscheme(), f.Tnp.get(), f.tapp.get(), f.src.get(), st);
-            ta.src = f.src.get();
-            ta.app0 = f.tapp.get();
-        }
+        energy_sources(ta);
         ta.Bq = f.Bq.get();
         ta.bc_mode = SC_FLUID_ENERGY;
         ta.val = f.As3.get(); ta.b = f.bs3.get();
@@ -639,6 +641,25 @@ void SimpleSolver::update_scalars_batched() {
         launch_cht_fluid2solid(d, f.dPhi.get(), f.kcond.get(), f.Bq.get(), sd.view, s.Bq.get(), st);
 }
 
+// Source and extra diagonal of the fluid energy equation: the viscous work of
+// density model 1 (navier_scalar.cpp:277-338) and the unsteady term
+// (navier_scalar.cpp:350-366), in the reference's order.
+void SimpleSolver::energy_sources(ScalarArgs &sa) {
+    const Params &p = cs.params;
+    int nc = fd.nc;
+    if (!tscheme() && p.density_model != 1) return;
+    launch_fill(f.src.get(), 0.0, nc, st);
+    sa.src = f.src.get();
+    if (p.density_model == 1)
+        launch_energy_viscous(fd.view, f.VisLam.get(), f.VisTur.get(), f.dU.get(), f.dV.get(), f.dW.get(), f.U.get(),
+                              f.V.get(), f.W.get(), p.cp, f.src.get(), st);
+    if (tscheme()) {
+        launch_fill(f.tapp.get(), 0.0, nc, st);
+        launch_time_term(nc, f.R.get(), fd.vol.get(), p.dt, tscheme(), f.Tnp.get(), f.tapp.get(), f.src.get(), st);
+        sa.app0 = f.tapp.get();
+    }
+}
+
 // NavierStokesSolver::UpdateEnergy, navier_scalar.cpp:257-397
 void SimpleSolver::update_energy() {
     const Params &p = cs.params;
@@ -653,13 +674,7 @@ void SimpleSolver::update_energy() {
     grad_limited(fd, f, 1, phi, Bphi, grad);
     ScalarArgs sa{};
     sa.phi = f.T.get(); sa.Bphi = f.BTem.get(); sa.diff = f.kcond.get(); sa.src = f.zeros.get(); sa.app0 = f.zeros.get();
-    if (tscheme()) {  // navier_scalar.cpp:350-366
-        launch_fill(f.src.get(), 0.0, nc, st);
-        launch_fill(f.tapp.get(), 0.0, nc, st);
-        launch_time_term(nc, f.R.get(), fd.vol.get(), p.dt, tscheme(), f.Tnp.get(), f.tapp.get(), f.src.get(), st);
-        sa.src = f.src.get();
-        sa.app0 = f.tapp.get();
-    }
+    energy_sources(sa);
     sa.grad = f.dPhi.get(); sa.RUFace = f.RUFace.get(); sa.Bq = f.Bq.get(); sa.urf = p.urf[5];
     sa.bc_mode = SC_FLUID_ENERGY;
     sa.fD = f.fD.get(); sa.fE = f.fE.get(); sa.bapp = f.bapp.get(); sa.bsrc = f.bsrc.get();

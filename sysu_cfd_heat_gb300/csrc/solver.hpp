@@ -157,6 +157,7 @@ class SimpleSolver {
     void update_ke();
     void update_energy();
     void update_scalars_batched();
+    void energy_sources(ScalarArgs &sa);
     // the device work of one outer iteration, enqueued on st without any host
     // synchronisation (capturable into a CUDA graph); outer_iteration() is this
     // plus check_iteration()
