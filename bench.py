@@ -373,7 +373,11 @@ def run_ours(args, r, w, lr):
         dist.barrier()
         param = case_dir(args.workload)
     L = _lib.lib()
+    t_create = time.perf_counter()
     s = NavierStokesSolver(param, {"rtc": RTC, "timing": 1})
+    t_create = time.perf_counter() - t_create
+    ph = np.zeros(5)
+    L.sysu_setup_phases(ph.ctypes.data_as(_lib.C.POINTER(_lib.C.c_double)))
     if args.p_maxit:
         s.set_option("p.maxit", args.p_maxit)
     if args.p_mixed:
@@ -543,10 +547,16 @@ def run_ours(args, r, w, lr):
                       "flops_per_cg_iteration": f_iter},
         "p_solve_ms_mean": statistics.mean(p_ms), "p_cg_iters_mean": statistics.mean(cg_it),
         "mom_bicgstab_iters": mom_it[-1], "clocks": clocks, "forms": forms,
+        "setup": {"solver_create_s": t_create, "msh_read_s": ph[0], "faces_s": ph[1], "split_s": ph[2],
+                  "geometry_s": ph[3], "host_threads": int(ph[4]),
+                  "note": "solver creation = param.in + MSH read + faces + geometry + device upload; "
+                          "topology and geometry are bit-identical for any thread count"},
     }
     s.close()
     if r == 0 and w == 1 and not args.no_cpu_baseline:
         its, setup, err = cpu_reference_run(param, 1, args.cpu_budget, args.cpu_budget + 600)
+        if setup is not None:
+            out["setup"]["reference_setup_s"] = setup
         if its:
             nx, ny, nz = WORKLOADS[args.workload]
             out["cpu_baseline"] = {"value": 1.0 / its[0], "unit": "iters/s", "cores": 1, "kind": "reference",

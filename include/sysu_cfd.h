@@ -59,6 +59,11 @@ int sysu_case_write_tecplot(const sysu_case *c, const char *path, int nfields, c
  * create: main.cpp:14-28 (read, build, CellFaceInfo, CheckAndAllocate,
  * InitFlowField) with every field uploaded to the current CUDA device. */
 int sysu_solver_create(const char *param_path, sysu_solver **out);
+/* Wall-clock seconds of the last case preprocessing on this thread (solver or
+ * case creation): out[0] MSH read, [1] face construction, [2] fluid/solid split,
+ * [3] geometry (CellFaceInfo); out[4] = host threads used (SYSU_THREADS or the
+ * hardware count; the results do not depend on it). */
+int sysu_setup_phases(double *out);
 void sysu_solver_destroy(sysu_solver *s);
 /* out[0..5] = Ncel, Nfac, Nbnd, solid Ncel, matrix stored entries, matrix true entries */
 int sysu_solver_info(sysu_solver *s, long *out, int n);

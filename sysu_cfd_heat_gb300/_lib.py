@@ -74,6 +74,7 @@ def lib() -> C.CDLL:
             "sysu_csr_last_error": (cp, []),
             "sysu_csr_bicgstab_batched3": (C.c_int, [C.c_int, ip, ip, C.POINTER(dp), C.POINTER(dp), C.POINTER(dp),
                                                      C.c_int, C.c_double, ip, dp, ip]),
+            "sysu_setup_phases": (C.c_int, [dp]),
             "sysu_batch_create": (C.c_int, [C.c_int, C.POINTER(cp), C.POINTER(vp)]),
             "sysu_batch_free": (None, [vp]),
             "sysu_batch_size": (C.c_int, [vp]),

@@ -81,7 +81,8 @@ def build(verbose: bool = False) -> str:
                     print(out)
     if jobs or not os.path.exists(LIB):
         tmp = LIB + ".tmp"
-        _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-cudart", "static", "-Xcompiler", "-fPIC"])
+        _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-cudart", "static", "-Xcompiler", "-fPIC",
+                                                             "-lpthread"])
         os.replace(tmp, LIB)
     return LIB
 

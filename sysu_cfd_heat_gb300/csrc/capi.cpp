@@ -598,6 +598,12 @@ void sysu_batch_free(sysu_batch *b) {
     delete b;
 }
 
+int sysu_setup_phases(double *out) {
+    if (!out) return set_err(SYSU_ERR_INPUT, "null argument");
+    for (int k = 0; k < 5; ++k) out[k] = sysu::setup_phases()[k];
+    return SYSU_OK;
+}
+
 int sysu_batch_size(sysu_batch *b) { return b ? b->impl->size() : 0; }
 
 sysu_solver *sysu_batch_case(sysu_batch *b, int k) {

@@ -2,12 +2,15 @@
 // Compiled with -ffp-contract=off so that the geometry formulas round exactly
 // like the reference's (which is built in ISO C++ mode, without contraction).
 #include "case.hpp"
+#include "parallel.hpp"
 
 #include <algorithm>
 #include <cctype>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstdint>
 #include <cstring>
 #include <fstream>
 #include <sstream>
@@ -181,10 +184,53 @@ struct Tok {
 };
 }  // namespace
 
-RawMesh read_msh(const std::string &path) {
-    std::ifstream f(path, std::ios::binary);
-    if (!f) fail("grid file not found : " + path);
-    std::string buf((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+namespace {
+
+constexpr int ELEM_NODES[8] = {0, 2, 3, 4, 4, 8, 6, 5};
+
+// One element record (the reference's Preprocessor.cpp:96-146 reading and the
+// 8-vertex cell form of its element types); "" or the error message.
+template <class Sink>
+std::string read_element(Tok &t, long nv, Sink &m) {
+    int v[8], tag[10];
+    t.integer();
+    long et = t.integer();
+    long ntags = t.integer();
+    if (ntags != 2 && ntags != 3) return "element with other than 2 or 3 tags";
+    if (et < 1 || et > 7) return "Unknown element type !!!";
+    for (long q = 0; q < ntags; ++q) tag[q] = (int)t.integer();
+    for (int q = 0; q < ELEM_NODES[et]; ++q) {
+        long vi = t.integer() - 1;
+        if (vi < 0 || vi >= nv) return "element references a missing vertex";
+        v[q] = (int)vi;
+    }
+    if (et == 2 || et == 3) {
+        m.bnd_rid.push_back(tag[0]);
+        int f4[4] = {v[0], v[1], v[2], et == 2 ? v[2] : v[3]};
+        m.bnd_vert.insert(m.bnd_vert.end(), f4, f4 + 4);
+    } else if (et >= 4 && et <= 7) {
+        int c[8];
+        if (et == 4) {  // tet
+            c[0] = v[0]; c[1] = v[1]; c[2] = v[2]; c[3] = v[2];
+            c[4] = c[5] = c[6] = c[7] = v[3];
+        } else if (et == 5) {
+            for (int q = 0; q < 8; ++q) c[q] = v[q];
+        } else if (et == 6) {  // prism
+            c[0] = v[0]; c[1] = v[1]; c[2] = v[2]; c[3] = v[2];
+            c[4] = v[3]; c[5] = v[4]; c[6] = v[5]; c[7] = v[5];
+        } else {  // pyramid
+            for (int q = 0; q < 4; ++q) c[q] = v[q];
+            c[4] = c[5] = c[6] = c[7] = v[4];
+        }
+        m.cell_rid.push_back(tag[0]);
+        m.cell_vert.insert(m.cell_vert.end(), c, c + 8);
+    } else {
+        return "Unknown element type !!!";
+    }
+    return "";
+}
+
+RawMesh read_msh_seq(const std::string &buf) {
     Tok t{buf.data(), buf.data() + buf.size()};
     for (int i = 0; i < 6; ++i) t.word();
     RawMesh m;
@@ -200,46 +246,156 @@ RawMesh read_msh(const std::string &path) {
     t.word();
     long ne = t.integer();
     if (ne <= 0) fail("mesh has no elements");
-    static const int nn[8] = {0, 2, 3, 4, 4, 8, 6, 5};
-    int v[8], tag[10];
     m.cell_vert.reserve((size_t)ne * 8);
     for (long i = 0; i < ne; ++i) {
-        t.integer();
-        long et = t.integer();
-        long ntags = t.integer();
-        if (ntags != 2 && ntags != 3) fail("element with other than 2 or 3 tags");
-        if (et < 1 || et > 7) fail("Unknown element type !!!");
-        for (long q = 0; q < ntags; ++q) tag[q] = (int)t.integer();
-        for (int q = 0; q < nn[et]; ++q) {
-            long vi = t.integer() - 1;
-            if (vi < 0 || vi >= nv) fail("element references a missing vertex");
-            v[q] = (int)vi;
-        }
-        if (et == 2 || et == 3) {
-            m.bnd_rid.push_back(tag[0]);
-            int f4[4] = {v[0], v[1], v[2], et == 2 ? v[2] : v[3]};
-            m.bnd_vert.insert(m.bnd_vert.end(), f4, f4 + 4);
-        } else if (et >= 4 && et <= 7) {
-            int c[8];
-            if (et == 4) {  // tet
-                c[0] = v[0]; c[1] = v[1]; c[2] = v[2]; c[3] = v[2];
-                c[4] = c[5] = c[6] = c[7] = v[3];
-            } else if (et == 5) {
-                for (int q = 0; q < 8; ++q) c[q] = v[q];
-            } else if (et == 6) {  // prism
-                c[0] = v[0]; c[1] = v[1]; c[2] = v[2]; c[3] = v[2];
-                c[4] = v[3]; c[5] = v[4]; c[6] = v[5]; c[7] = v[5];
-            } else {  // pyramid
-                for (int q = 0; q < 4; ++q) c[q] = v[q];
-                c[4] = c[5] = c[6] = c[7] = v[4];
-            }
-            m.cell_rid.push_back(tag[0]);
-            m.cell_vert.insert(m.cell_vert.end(), c, c + 8);
-        } else {
-            fail("Unknown element type !!!");
-        }
+        std::string e = read_element(t, nv, m);
+        if (!e.empty()) fail(e);
     }
     return m;
+}
+
+// Split [b, e) into T pieces that start at line beginnings.
+std::vector<const char *> line_splits(const char *b, const char *e, int T) {
+    std::vector<const char *> cut{b};
+    for (int k = 1; k < T; ++k) {
+        const char *p = b + (e - b) * k / T;
+        if (p < cut.back()) p = cut.back();
+        while (p < e && *p != '\n') ++p;
+        if (p < e) ++p;
+        cut.push_back(p);
+    }
+    cut.push_back(e);
+    return cut;
+}
+
+const char *find_marker(const char *b, const char *e, const char *marker) {
+    size_t len = std::strlen(marker);
+    const char *p = std::search(b, e, marker, marker + len);
+    return p == e ? nullptr : p;
+}
+
+// The same reading with the node and element sections split over threads at
+// line boundaries (Gmsh writes one record per line).  Returns false when the
+// file does not have that layout or any record fails; the caller then reads it
+// sequentially, which reports the reference's error.
+bool read_msh_par(const std::string &buf, int T, RawMesh &m) {
+    const char *B = buf.data(), *E = B + buf.size();
+    Tok t{B, E};
+    for (int i = 0; i < 6; ++i) t.word();
+    long nv = t.integer();
+    if (nv <= 0) return false;
+    const char *ns = t.p, *nend = find_marker(ns, E, "$EndNodes");
+    if (!nend) return false;
+    std::vector<const char *> cut = line_splits(ns, nend, T);
+    std::vector<std::vector<double>> vparts(T);
+    std::vector<int> vok(T, 1);
+    parallel_chunks(T, T, [&](long k0, long k1, int) {
+        for (long k = k0; k < k1; ++k) {
+            Tok c{cut[k], cut[k + 1]};
+            std::vector<double> &out = vparts[k];
+            try {
+                while (c.skip_ws()) {
+                    c.integer();
+                    for (int q = 0; q < 3; ++q) out.push_back(c.real());
+                }
+            } catch (...) {
+                vok[k] = 0;
+            }
+        }
+    });
+    size_t nvals = 0;
+    for (int k = 0; k < T; ++k) {
+        if (!vok[k]) return false;
+        nvals += vparts[k].size();
+    }
+    if (nvals != (size_t)nv * 3) return false;
+    m.nv = (int)nv;
+    m.vert.clear();
+    m.vert.reserve(nvals);
+    for (auto &v : vparts) m.vert.insert(m.vert.end(), v.begin(), v.end());
+    Tok t2{nend, E};
+    t2.word();
+    t2.word();
+    long ne = t2.integer();
+    if (ne <= 0) return false;
+    const char *es = t2.p, *eend = find_marker(es, E, "$EndElements");
+    if (!eend) return false;
+    cut = line_splits(es, eend, T);
+    std::vector<RawMesh> parts(T);
+    std::vector<long> cnt(T, 0);
+    parallel_chunks(T, T, [&](long k0, long k1, int) {
+        for (long k = k0; k < k1; ++k) {
+            Tok c{cut[k], cut[k + 1]};
+            try {
+                while (c.skip_ws()) {
+                    if (!read_element(c, nv, parts[k]).empty()) {
+                        vok[k] = 0;
+                        break;
+                    }
+                    ++cnt[k];
+                }
+            } catch (...) {
+                vok[k] = 0;
+            }
+        }
+    });
+    long total = 0;
+    size_t ncv = 0, nbv = 0;
+    for (int k = 0; k < T; ++k) {
+        if (!vok[k]) return false;
+        total += cnt[k];
+        ncv += parts[k].cell_vert.size();
+        nbv += parts[k].bnd_vert.size();
+    }
+    if (total != ne) return false;
+    m.cell_vert.reserve(ncv);
+    m.cell_rid.reserve(ncv / 8);
+    m.bnd_vert.reserve(nbv);
+    m.bnd_rid.reserve(nbv / 4);
+    for (RawMesh &p : parts) {
+        m.cell_vert.insert(m.cell_vert.end(), p.cell_vert.begin(), p.cell_vert.end());
+        m.cell_rid.insert(m.cell_rid.end(), p.cell_rid.begin(), p.cell_rid.end());
+        m.bnd_vert.insert(m.bnd_vert.end(), p.bnd_vert.begin(), p.bnd_vert.end());
+        m.bnd_rid.insert(m.bnd_rid.end(), p.bnd_rid.begin(), p.bnd_rid.end());
+    }
+    return true;
+}
+
+}  // namespace
+
+double *setup_phases() {
+    static thread_local double ph[5] = {0, 0, 0, 0, 0};
+    return ph;
+}
+
+namespace {
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+}  // namespace
+
+RawMesh read_msh(const std::string &path) {
+    double t0 = now_s();
+    struct Stamp {
+        double t0;
+        ~Stamp() { setup_phases()[0] = now_s() - t0; }
+    } stamp{t0};
+    setup_phases()[4] = host_threads();
+    std::ifstream f(path, std::ios::binary);
+    if (!f) fail("grid file not found : " + path);
+    std::string buf((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    int T = host_threads();
+    if (T > 1 && buf.size() > (size_t)(1 << 20)) {
+        RawMesh m;
+        bool ok = false;
+        try {
+            ok = read_msh_par(buf, T, m);
+        } catch (...) {
+            ok = false;
+        }
+        if (ok) return m;
+    }
+    return read_msh_seq(buf);
 }
 
 // ---------------------------------------------------------------------------
@@ -287,7 +443,7 @@ struct Topo {
     std::vector<int> bnd_face, bnd_rid;
 };
 
-void create_faces(const RawMesh &m, Topo &t) {
+void create_faces_seq(const RawMesh &m, Topo &t) {
     int nc = m.ncell(), nb = m.nbnd();
     t.nv = m.nv;
     t.vert = m.vert;
@@ -357,6 +513,181 @@ void create_faces(const RawMesh &m, Topo &t) {
         if (t.face_c2[f] == -20) fail("error in face right hand side (a boundary face is not marked)");
         if (t.face_bnd[f] >= 0 && t.face_c1[f] < 0) fail("boundary element that bounds no cell");
     }
+}
+
+// The same face construction over threads.  Every candidate face gets a slot in
+// visiting order (boundary elements 0..nb-1, then nb + 6 ic + q); the candidates
+// are distributed over hash shards by key, each shard thread scans all slots in
+// order and claims the ones of its keys, so every key sees its visits in the
+// reference's order.  A face's id is the rank of its first visit among all first
+// visits (a prefix sum), which is the order in which the sequential loop creates
+// faces.  Returns false on anything the sequential loop would report (the caller
+// reruns it for the exact message).
+bool create_faces_par(const RawMesh &m, Topo &t, int T) {
+    const int nc = m.ncell(), nb = m.nbnd();
+    const long S = (long)nb + 6L * nc;
+    static const int lf[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 1, 5, 4},
+                                 {1, 2, 6, 5}, {3, 2, 6, 7}, {0, 3, 7, 4}};
+    auto slot_verts = [&](long s, int *v) {
+        if (s < nb) {
+            const int *bv = &m.bnd_vert[(size_t)s * 4];
+            for (int k = 0; k < 4; ++k) v[k] = bv[k];
+            return true;
+        }
+        long r = s - nb;
+        int ic = (int)(r / 6), q = (int)(r % 6);
+        const int *cv = &m.cell_vert[(size_t)ic * 8];
+        int n1 = cv[lf[q][0]], n2 = cv[lf[q][1]], n3 = cv[lf[q][2]], n4 = cv[lf[q][3]];
+        int irepeat = 0;
+        if (n1 == n2 || n1 == n3 || n1 == n4) ++irepeat;
+        if (n2 == n3 || n2 == n4) ++irepeat;
+        if (n3 == n4) ++irepeat;
+        v[0] = n1; v[1] = n2; v[2] = n3; v[3] = n4;
+        return irepeat <= 1;
+    };
+    std::vector<FaceKey> key((size_t)S);
+    std::vector<uint32_t> hsh((size_t)S);
+    const uint32_t INVALID = 0xFFFFFFFFu;
+    FaceKeyHash H;
+    parallel_chunks(S, T, [&](long b, long e, int) {
+        int v[4];
+        for (long s = b; s < e; ++s) {
+            if (!slot_verts(s, v)) {
+                hsh[s] = INVALID;
+                continue;
+            }
+            key[s] = key_of(v[0], v[1], v[2], v[3]);
+            hsh[s] = (uint32_t)(H(key[s]) & 0x7FFFFFFFu);
+        }
+    });
+    // shard tables: open addressing, per entry the first slot, c1, c2, bnd
+    struct Entry {
+        FaceKey k;
+        int first, c1, c2, bnd;
+    };
+    std::vector<int> first_of((size_t)S, -1);
+    std::vector<std::vector<Entry>> tab(T);
+    std::vector<int> bad(T, 0);
+    parallel_chunks(T, T, [&](long t0, long t1, int) {
+        for (long sh = t0; sh < t1; ++sh) {
+            long mine = 0;
+            for (long s = 0; s < S; ++s)
+                if (hsh[s] != INVALID && (long)(hsh[s] % (uint32_t)T) == sh) ++mine;
+            size_t cap = 16;
+            while (cap < (size_t)mine * 2) cap <<= 1;
+            std::vector<Entry> &E = tab[sh];
+            E.assign(cap, Entry{{{-3, -3, -3, -3}}, -1, 0, 0, 0});
+            const size_t mask = cap - 1;
+            for (long s = 0; s < S && !bad[sh]; ++s) {
+                uint32_t h = hsh[s];
+                if (h == INVALID || (long)(h % (uint32_t)T) != sh) continue;
+                size_t i = (h / (uint32_t)T) & mask;
+                while (E[i].first >= 0 && !(E[i].k == key[s])) i = (i + 1) & mask;
+                Entry &en = E[i];
+                if (s < nb) {
+                    if (en.first >= 0) {  // duplicate boundary element
+                        bad[sh] = 1;
+                        break;
+                    }
+                    en.k = key[s];
+                    en.first = (int)s;
+                    en.c1 = -10;
+                    en.c2 = -10;
+                    en.bnd = (int)s;
+                    first_of[s] = (int)s;
+                    continue;
+                }
+                int ic = (int)((s - nb) / 6);
+                if (en.first < 0) {
+                    en.k = key[s];
+                    en.first = (int)s;
+                    en.c1 = ic;
+                    en.c2 = -20;
+                    en.bnd = -10;
+                } else if (en.bnd >= 0) {
+                    if (en.c1 == -10) en.c1 = ic;
+                    else if (en.c2 == -10) en.c2 = ic;
+                    else { bad[sh] = 1; break; }
+                } else {
+                    if (en.c2 != -20) { bad[sh] = 1; break; }
+                    en.c2 = ic;
+                }
+                first_of[s] = en.first;
+            }
+        }
+    });
+    for (int sh = 0; sh < T; ++sh)
+        if (bad[sh]) return false;
+    // face ids: exclusive prefix count of first visits, in slot order
+    std::vector<int> fid((size_t)S, -1);
+    std::vector<long> part(T + 1, 0);
+    parallel_chunks(S, T, [&](long b, long e, int k) {
+        long c = 0;
+        for (long s = b; s < e; ++s)
+            if (first_of[s] == s) ++c;
+        part[k + 1] = c;
+    });
+    for (int k = 0; k < T; ++k) part[k + 1] += part[k];
+    const long nf = part[T];
+    parallel_chunks(S, T, [&](long b, long e, int k) {
+        long c = part[k];
+        for (long s = b; s < e; ++s)
+            if (first_of[s] == s) fid[s] = (int)c++;
+    });
+    t.nv = m.nv;
+    t.vert = m.vert;
+    t.cell_vert = m.cell_vert;
+    t.cell_rid = m.cell_rid;
+    t.bnd_rid = m.bnd_rid;
+    t.bnd_face.resize(nb);
+    for (int i = 0; i < nb; ++i) t.bnd_face[i] = i;
+    t.face_vert.assign((size_t)nf * 4, 0);
+    t.face_c1.assign(nf, 0);
+    t.face_c2.assign(nf, 0);
+    t.face_bnd.assign(nf, 0);
+    parallel_chunks(T, T, [&](long t0, long t1, int) {
+        for (long sh = t0; sh < t1; ++sh)
+            for (const Entry &en : tab[sh]) {
+                if (en.first < 0) continue;
+                int f = fid[en.first];
+                int v[4];
+                slot_verts(en.first, v);
+                for (int k = 0; k < 4; ++k) t.face_vert[(size_t)f * 4 + k] = v[k];
+                t.face_c1[f] = en.c1;
+                t.face_c2[f] = en.c2;
+                t.face_bnd[f] = en.bnd;
+            }
+    });
+    t.cell_nface.assign(nc, 0);
+    t.cell_face.assign((size_t)nc * 6, -1);
+    parallel_chunks(nc, T, [&](long b, long e, int) {
+        for (long ic = b; ic < e; ++ic) {
+            int k = 0;
+            for (int q = 0; q < 6; ++q) {
+                long s = nb + ic * 6 + q;
+                if (hsh[s] == INVALID) continue;
+                t.cell_face[(size_t)ic * 6 + k++] = fid[first_of[s]];
+            }
+            t.cell_nface[ic] = k;
+        }
+    });
+    for (long f = 0; f < nf; ++f) {
+        if (t.face_c2[f] == -20) return false;
+        if (t.face_bnd[f] >= 0 && t.face_c1[f] < 0) return false;
+    }
+    return true;
+}
+
+void create_faces(const RawMesh &m, Topo &t) {
+    int T = host_threads();
+    if (T > 1 && m.ncell() >= 20000) {
+        Topo p;
+        if (create_faces_par(m, p, T)) {
+            t = std::move(p);
+            return;
+        }
+    }
+    create_faces_seq(m, t);
 }
 
 // findCoupledBoundary (Preprocessor.cpp:308-438) for the cells in new2old.
@@ -477,18 +808,35 @@ double tet_vol(const double *x1, const double *x2, const double *x3, const doubl
 }
 }  // namespace
 
+// Each loop runs over threads (static chunks); a check that fails reports the
+// lowest failing index of its loop, the one the sequential loop meets first.
 void cell_face_info(Domain &d) {
+    const int T = d.nc >= 20000 ? host_threads() : 1;
     const double *V = d.vert.data();
     auto X = [&](int iv) { return V + (size_t)iv * 3; };
+    const long NONE = -1;
+    std::vector<long> firstbad(T);
+    auto reset_bad = [&]() { std::fill(firstbad.begin(), firstbad.end(), NONE); };
+    auto note_bad = [&](int k, long i) {
+        if (firstbad[k] == NONE || i < firstbad[k]) firstbad[k] = i;
+    };
+    auto lowest_bad = [&]() {
+        long lo = NONE;
+        for (long b : firstbad)
+            if (b != NONE && (lo == NONE || b < lo)) lo = b;
+        return lo;
+    };
     d.cell_x.assign((size_t)d.nc * 3, 0.0);
     d.cell_vol.assign(d.nc, 0.0);
-    for (int i = 0; i < d.nc; ++i) {
-        const int *cv = &d.cell_vert[(size_t)i * 8];
-        for (int j = 0; j < 3; ++j)
-            d.cell_x[(size_t)i * 3 + j] =
-                1. / 8. * (X(cv[0])[j] + X(cv[1])[j] + X(cv[2])[j] + X(cv[3])[j] + X(cv[4])[j] +
-                           X(cv[5])[j] + X(cv[6])[j] + X(cv[7])[j]);
-    }
+    parallel_chunks(d.nc, T, [&](long b, long e, int) {
+        for (long i = b; i < e; ++i) {
+            const int *cv = &d.cell_vert[(size_t)i * 8];
+            for (int j = 0; j < 3; ++j)
+                d.cell_x[(size_t)i * 3 + j] =
+                    1. / 8. * (X(cv[0])[j] + X(cv[1])[j] + X(cv[2])[j] + X(cv[3])[j] + X(cv[4])[j] +
+                               X(cv[5])[j] + X(cv[6])[j] + X(cv[7])[j]);
+        }
+    });
     d.face_x.assign((size_t)d.nf * 3, 0.0);
     d.face_n.assign((size_t)d.nf * 3, 0.0);
     d.face_area.assign(d.nf, 0.0);
@@ -496,130 +844,146 @@ void cell_face_info(Domain &d) {
     d.face_rlencos.assign(d.nf, 0.0);
     d.face_xpac.assign((size_t)d.nf * 3, 0.0);
     d.face_xnac.assign((size_t)d.nf * 3, 0.0);
-    for (int i = 0; i < d.nf; ++i) {
-        const int *fv = &d.face_vert[(size_t)i * 4];
-        const double *p1 = X(fv[0]), *p2 = X(fv[1]), *p3 = X(fv[2]), *p4 = X(fv[3]);
-        double area1 = tri_area(p1, p2, p4);
-        double area2 = tri_area(p2, p3, p4);
-        double xc1[3], xc2[3];
-        for (int j = 0; j < 3; ++j) {
-            xc1[j] = 1. / 3 * (p1[j] + p2[j] + p4[j]);
-            xc2[j] = 1. / 3 * (p2[j] + p3[j] + p4[j]);
+    reset_bad();
+    parallel_chunks(d.nf, T, [&](long b, long e, int k) {
+        for (long i = b; i < e; ++i) {
+            const int *fv = &d.face_vert[(size_t)i * 4];
+            const double *p1 = X(fv[0]), *p2 = X(fv[1]), *p3 = X(fv[2]), *p4 = X(fv[3]);
+            double area1 = tri_area(p1, p2, p4);
+            double area2 = tri_area(p2, p3, p4);
+            double xc1[3], xc2[3];
+            for (int j = 0; j < 3; ++j) {
+                xc1[j] = 1. / 3 * (p1[j] + p2[j] + p4[j]);
+                xc2[j] = 1. / 3 * (p2[j] + p3[j] + p4[j]);
+            }
+            double *fx = &d.face_x[(size_t)i * 3];
+            for (int j = 0; j < 3; ++j) fx[j] = (area1 * xc1[j] + area2 * xc2[j]) / (area1 + area2);
+            double dx1[3], dx2[3], dx[3];
+            vminus(dx1, p1, p3);
+            vminus(dx2, p2, p4);
+            double *fn = &d.face_n[(size_t)i * 3];
+            vcross(fn, dx1, dx2);
+            for (int j = 0; j < 3; ++j) fn[j] = 0.5 * fn[j];
+            int ic = d.face_c1[i];
+            vminus(dx, fx, &d.cell_x[(size_t)ic * 3]);
+            if (vdot(fn, dx) < 0.)
+                for (int j = 0; j < 3; ++j) fn[j] = -fn[j];
+            d.face_area[i] = vlen(fn);
+            if (std::fabs((area1 + area2 - d.face_area[i]) / d.face_area[i]) > 1.e-4) note_bad(k, i);
+            int ic1 = d.face_c1[i], ic2 = d.face_c2[i];
+            if (ic2 >= 0) {
+                vminus(dx1, fx, &d.cell_x[(size_t)ic1 * 3]);
+                vminus(dx2, fx, &d.cell_x[(size_t)ic2 * 3]);
+                double r1 = vlen(dx1), r2 = vlen(dx2);
+                d.face_lambda[i] = r2 / (r1 + r2);
+            } else {
+                d.face_lambda[i] = 1.;
+            }
         }
-        double *fx = &d.face_x[(size_t)i * 3];
-        for (int j = 0; j < 3; ++j) fx[j] = (area1 * xc1[j] + area2 * xc2[j]) / (area1 + area2);
-        double dx1[3], dx2[3], dx[3];
-        vminus(dx1, p1, p3);
-        vminus(dx2, p2, p4);
-        double *fn = &d.face_n[(size_t)i * 3];
-        vcross(fn, dx1, dx2);
-        for (int j = 0; j < 3; ++j) fn[j] = 0.5 * fn[j];
-        int ic = d.face_c1[i];
-        vminus(dx, fx, &d.cell_x[(size_t)ic * 3]);
-        if (vdot(fn, dx) < 0.)
-            for (int j = 0; j < 3; ++j) fn[j] = -fn[j];
-        d.face_area[i] = vlen(fn);
-        if (std::fabs((area1 + area2 - d.face_area[i]) / d.face_area[i]) > 1.e-4)
-            fail("face " + std::to_string(i) + " area is not correct (non-planar face)");
-        int ic1 = d.face_c1[i], ic2 = d.face_c2[i];
-        if (ic2 >= 0) {
-            vminus(dx1, fx, &d.cell_x[(size_t)ic1 * 3]);
-            vminus(dx2, fx, &d.cell_x[(size_t)ic2 * 3]);
-            double r1 = vlen(dx1), r2 = vlen(dx2);
-            d.face_lambda[i] = r2 / (r1 + r2);
-        } else {
-            d.face_lambda[i] = 1.;
-        }
-    }
+    });
+    if (lowest_bad() != NONE) fail("face " + std::to_string(lowest_bad()) + " area is not correct (non-planar face)");
     d.cell_nbr.assign((size_t)d.nc * 6, -100);
-    for (int i = 0; i < d.nc; ++i) {
-        const int *cv = &d.cell_vert[(size_t)i * 8];
-        double xv[8][3];
-        for (int k = 0; k < 8; ++k)
-            for (int j = 0; j < 3; ++j) xv[k][j] = X(cv[k])[j];
-        double V1 = tet_vol(xv[0], xv[1], xv[3], xv[5]);
-        double V2 = tet_vol(xv[0], xv[4], xv[3], xv[5]);
-        double V3 = tet_vol(xv[3], xv[4], xv[7], xv[5]);
-        double V4 = tet_vol(xv[1], xv[2], xv[3], xv[6]);
-        double V5 = tet_vol(xv[1], xv[5], xv[3], xv[6]);
-        double V6 = tet_vol(xv[7], xv[3], xv[5], xv[6]);
-        d.cell_vol[i] = V1 + V2 + V3 + V4 + V5 + V6;
-        double c[6][3];
-        for (int j = 0; j < 3; ++j) {
-            c[0][j] = 0.25 * (xv[0][j] + xv[1][j] + xv[3][j] + xv[5][j]);
-            c[1][j] = 0.25 * (xv[0][j] + xv[4][j] + xv[3][j] + xv[5][j]);
-            c[2][j] = 0.25 * (xv[3][j] + xv[4][j] + xv[7][j] + xv[5][j]);
-            c[3][j] = 0.25 * (xv[1][j] + xv[2][j] + xv[3][j] + xv[6][j]);
-            c[4][j] = 0.25 * (xv[1][j] + xv[5][j] + xv[3][j] + xv[6][j]);
-            c[5][j] = 0.25 * (xv[7][j] + xv[3][j] + xv[5][j] + xv[6][j]);
+    reset_bad();
+    parallel_chunks(d.nc, T, [&](long b, long e, int k) {
+        for (long i = b; i < e; ++i) {
+            const int *cv = &d.cell_vert[(size_t)i * 8];
+            double xv[8][3];
+            for (int q = 0; q < 8; ++q)
+                for (int j = 0; j < 3; ++j) xv[q][j] = X(cv[q])[j];
+            double V1 = tet_vol(xv[0], xv[1], xv[3], xv[5]);
+            double V2 = tet_vol(xv[0], xv[4], xv[3], xv[5]);
+            double V3 = tet_vol(xv[3], xv[4], xv[7], xv[5]);
+            double V4 = tet_vol(xv[1], xv[2], xv[3], xv[6]);
+            double V5 = tet_vol(xv[1], xv[5], xv[3], xv[6]);
+            double V6 = tet_vol(xv[7], xv[3], xv[5], xv[6]);
+            d.cell_vol[i] = V1 + V2 + V3 + V4 + V5 + V6;
+            double c[6][3];
+            for (int j = 0; j < 3; ++j) {
+                c[0][j] = 0.25 * (xv[0][j] + xv[1][j] + xv[3][j] + xv[5][j]);
+                c[1][j] = 0.25 * (xv[0][j] + xv[4][j] + xv[3][j] + xv[5][j]);
+                c[2][j] = 0.25 * (xv[3][j] + xv[4][j] + xv[7][j] + xv[5][j]);
+                c[3][j] = 0.25 * (xv[1][j] + xv[2][j] + xv[3][j] + xv[6][j]);
+                c[4][j] = 0.25 * (xv[1][j] + xv[5][j] + xv[3][j] + xv[6][j]);
+                c[5][j] = 0.25 * (xv[7][j] + xv[3][j] + xv[5][j] + xv[6][j]);
+            }
+            double Vsum = V1 + V2 + V3 + V4 + V5 + V6;
+            for (int j = 0; j < 3; ++j)
+                d.cell_x[(size_t)i * 3 + j] = 1. / Vsum *
+                    (V1 * c[0][j] + V2 * c[1][j] + V3 * c[2][j] + V4 * c[3][j] + V5 * c[4][j] + V6 * c[5][j]);
+            if (!(d.cell_vol[i] > 0.)) note_bad(k, i);
+            for (int j = 0; j < d.cell_nface[i]; ++j) {
+                int f = d.cell_face[(size_t)i * 6 + j];
+                int nc = d.face_c1[f];
+                if (nc == i) nc = d.face_c2[f];
+                d.cell_nbr[(size_t)i * 6 + j] = nc;
+            }
         }
-        double Vsum = V1 + V2 + V3 + V4 + V5 + V6;
-        for (int j = 0; j < 3; ++j)
-            d.cell_x[(size_t)i * 3 + j] = 1. / Vsum *
-                (V1 * c[0][j] + V2 * c[1][j] + V3 * c[2][j] + V4 * c[3][j] + V5 * c[4][j] + V6 * c[5][j]);
-        if (!(d.cell_vol[i] > 0.)) fail("error in cell volume calculation: cell " + std::to_string(i));
-        for (int j = 0; j < d.cell_nface[i]; ++j) {
-            int f = d.cell_face[(size_t)i * 6 + j];
-            int nc = d.face_c1[f];
-            if (nc == i) nc = d.face_c2[f];
-            d.cell_nbr[(size_t)i * 6 + j] = nc;
-        }
-    }
+    });
+    if (lowest_bad() != NONE) fail("error in cell volume calculation: cell " + std::to_string(lowest_bad()));
     d.bnd_distance.assign(d.nb, 0.0);
-    for (int i = 0; i < d.nb; ++i) {
-        int jf = d.bnd_face[i], jc = d.face_c1[jf];
-        double dx[3];
-        vminus(dx, &d.face_x[(size_t)jf * 3], &d.cell_x[(size_t)jc * 3]);
-        d.bnd_distance[i] = vdot(dx, &d.face_n[(size_t)jf * 3]) / d.face_area[jf];
-        if (d.bnd_distance[i] < 0.) fail("wall distance is negative." + std::to_string(i));
-    }
-    for (int i = 0; i < d.nf; ++i) {
-        int ic1 = d.face_c1[i], ic2 = d.face_c2[i];
-        const double *fx = &d.face_x[(size_t)i * 3];
-        const double *fn = &d.face_n[(size_t)i * 3];
-        double area = d.face_area[i];
-        double dx[3];
-        if (ic2 < 0) vminus(dx, fx, &d.cell_x[(size_t)ic1 * 3]);
-        else vminus(dx, &d.cell_x[(size_t)ic2 * 3], &d.cell_x[(size_t)ic1 * 3]);
-        d.face_rlencos[i] = area / (vdot(dx, fn) / area);
-        if (ic2 >= 0) {
-            double ss;
-            vminus(dx, fx, &d.cell_x[(size_t)ic1 * 3]);
-            ss = vdot(dx, fn) / area;
-            for (int j = 0; j < 3; ++j) dx[j] = ss * fn[j] / area;
-            vminus(&d.face_xpac[(size_t)i * 3], fx, dx);
-            vminus(dx, fx, &d.cell_x[(size_t)ic2 * 3]);
-            ss = vdot(dx, fn) / area;
-            for (int j = 0; j < 3; ++j) dx[j] = ss * fn[j] / area;
-            vminus(&d.face_xnac[(size_t)i * 3], fx, dx);
+    reset_bad();
+    parallel_chunks(d.nb, T, [&](long b, long e, int k) {
+        for (long i = b; i < e; ++i) {
+            int jf = d.bnd_face[i], jc = d.face_c1[jf];
+            double dx[3];
+            vminus(dx, &d.face_x[(size_t)jf * 3], &d.cell_x[(size_t)jc * 3]);
+            d.bnd_distance[i] = vdot(dx, &d.face_n[(size_t)jf * 3]) / d.face_area[jf];
+            if (d.bnd_distance[i] < 0.) note_bad(k, i);
         }
-    }
+    });
+    if (lowest_bad() != NONE) fail("wall distance is negative." + std::to_string(lowest_bad()));
+    parallel_chunks(d.nf, T, [&](long b, long e, int) {
+        for (long i = b; i < e; ++i) {
+            int ic1 = d.face_c1[i], ic2 = d.face_c2[i];
+            const double *fx = &d.face_x[(size_t)i * 3];
+            const double *fn = &d.face_n[(size_t)i * 3];
+            double area = d.face_area[i];
+            double dx[3];
+            if (ic2 < 0) vminus(dx, fx, &d.cell_x[(size_t)ic1 * 3]);
+            else vminus(dx, &d.cell_x[(size_t)ic2 * 3], &d.cell_x[(size_t)ic1 * 3]);
+            d.face_rlencos[i] = area / (vdot(dx, fn) / area);
+            if (ic2 >= 0) {
+                double ss;
+                vminus(dx, fx, &d.cell_x[(size_t)ic1 * 3]);
+                ss = vdot(dx, fn) / area;
+                for (int j = 0; j < 3; ++j) dx[j] = ss * fn[j] / area;
+                vminus(&d.face_xpac[(size_t)i * 3], fx, dx);
+                vminus(dx, fx, &d.cell_x[(size_t)ic2 * 3]);
+                ss = vdot(dx, fn) / area;
+                for (int j = 0; j < 3; ++j) dx[j] = ss * fn[j] / area;
+                vminus(&d.face_xnac[(size_t)i * 3], fx, dx);
+            }
+        }
+    });
 }
 
 void build_case(const RawMesh &raw, Case &cs) {
     Topo t;
+    double t0 = now_s();
     create_faces(raw, t);
+    double t1 = now_s();
+    setup_phases()[1] = t1 - t0;
     const Params &p = cs.params;
     auto to_domain = [&](const std::vector<int> &new2old, int crid, Domain &d) { extract_domain(t, new2old, crid, d); };
     if (!p.heat_conduction) {
         // buildSolver without heat conduction hands the global mesh over as is
         Domain &d = cs.fluid;
         d.nv = t.nv;
-        d.vert = t.vert;
+        d.vert = std::move(t.vert);
         d.nc = raw.ncell();
-        d.cell_vert = t.cell_vert;
-        d.cell_rid = t.cell_rid;
-        d.cell_nface = t.cell_nface;
-        d.cell_face = t.cell_face;
+        d.cell_vert = std::move(t.cell_vert);
+        d.cell_rid = std::move(t.cell_rid);
+        d.cell_nface = std::move(t.cell_nface);
+        d.cell_face = std::move(t.cell_face);
         d.nf = (int)t.face_c1.size();
-        d.face_vert = t.face_vert;
-        d.face_c1 = t.face_c1;
-        d.face_c2 = t.face_c2;
-        d.face_bnd = t.face_bnd;
+        d.face_vert = std::move(t.face_vert);
+        d.face_c1 = std::move(t.face_c1);
+        d.face_c2 = std::move(t.face_c2);
+        d.face_bnd = std::move(t.face_bnd);
         d.nb = raw.nbnd();
         d.ncb = d.nb;
-        d.bnd_face = t.bnd_face;
-        d.bnd_rid = t.bnd_rid;
+        d.bnd_face = std::move(t.bnd_face);
+        d.bnd_rid = std::move(t.bnd_rid);
         cs.has_solid = false;
     } else {
         // Preprocessor.cpp:453-512: a coupled wall region takes the first unused id
@@ -661,6 +1025,8 @@ void build_case(const RawMesh &raw, Case &cs) {
                      (solid ? "solid" : "fluid") + " volumn");
         }
     };
+    double t2 = now_s();
+    setup_phases()[2] = t2 - t1;
     cell_face_info(cs.fluid);
     check_domain(cs.fluid, false);
     if (cs.has_solid) {
@@ -669,6 +1035,7 @@ void build_case(const RawMesh &raw, Case &cs) {
         if (cs.fluid.nb - cs.fluid.ncb != cs.solid.nb - cs.solid.ncb)
             fail("fluid and solid have different numbers of coupled faces");
     }
+    setup_phases()[3] = now_s() - t2;
 }
 
 }  // namespace sysu

@@ -104,6 +104,9 @@ struct CaseError {
 
 Params parse_params(const std::string &path);
 RawMesh read_msh(const std::string &path);
+// Wall-clock seconds of the last preprocessing on this thread: [0] MSH read,
+// [1] face construction, [2] fluid/solid split, [3] geometry; threads used in [4].
+double *setup_phases();
 // CreateFaces + (optional) fluid/solid split + CellFaceInfo.
 void build_case(const RawMesh &raw, Case &cs);
 void cell_face_info(Domain &d);

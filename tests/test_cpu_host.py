@@ -143,3 +143,59 @@ def test_library_exports_every_declared_symbol():
     assert len(names) > 20
     missing = [n for n in sorted(names) if not hasattr(lib, n)]
     assert not missing, missing
+
+
+ALL_ARRAYS = GEOM_F + GEOM_I + ["face_xpac", "face_xnac", "cell_nbr", "cell_face", "face_bnd", "vert"]
+
+
+def _load_all(param, threads):
+    old = os.environ.get("SYSU_THREADS")
+    os.environ["SYSU_THREADS"] = str(threads)
+    try:
+        c = Case(param)
+        pre = [""] + (["solid_"] if c.info()["has_solid"] else [])
+        return {p + g: c.array(p + g) for p in pre for g in ALL_ARRAYS}
+    finally:
+        if old is None:
+            os.environ.pop("SYSU_THREADS")
+        else:
+            os.environ["SYSU_THREADS"] = old
+
+
+@pytest.mark.parametrize("kind", ["tet", "cht"])
+def test_threaded_preprocessing_is_identical(kind):
+    """MSH read, face construction and geometry over threads give the same bytes
+    as one thread (meshes above the threading thresholds: > 1 MB, > 20,000 cells)."""
+    with tempfile.TemporaryDirectory() as tmp:
+        if kind == "tet":
+            p = mg.write_case(tmp, mg.lid_cavity_tet(20, 20, 20, jitter=0.2, seed=3), mg.cavity_param("x", 10, mu=0.01))
+        else:
+            p = mg.write_case(tmp, mg.cht_channel(48, 20, 6, 24), mg.cht_param("x", 10))
+        assert os.path.getsize(os.path.join(tmp, "mesh.msh")) > (1 << 20)
+        a = _load_all(p, 1)
+        b = _load_all(p, 5)
+        assert a.keys() == b.keys()
+        for k in a:
+            assert a[k].tobytes() == b[k].tobytes(), k
+
+
+def test_threaded_reader_reports_the_reference_error():
+    with tempfile.TemporaryDirectory() as tmp:
+        p = mg.write_case(tmp, mg.lid_cavity_tet(20, 20, 20, jitter=0.2, seed=3), mg.cavity_param("x", 10, mu=0.01))
+        msh = os.path.join(tmp, "mesh.msh")
+        lines = open(msh).read().split("\n")
+        k = len(lines) - 40  # an element near the end: a vertex that does not exist
+        parts = lines[k].split()
+        parts[-1] = str(10 ** 8)
+        lines[k] = " ".join(parts)
+        open(msh, "w").write("\n".join(lines))
+        msgs = []
+        for thr in (1, 5):
+            os.environ["SYSU_THREADS"] = str(thr)
+            try:
+                with pytest.raises(SysuError) as e:
+                    Case(p)
+                msgs.append(e.value.msg)
+            finally:
+                os.environ.pop("SYSU_THREADS")
+        assert msgs[0] == msgs[1] and "missing vertex" in msgs[0]
