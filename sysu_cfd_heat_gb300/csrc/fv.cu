@@ -132,9 +132,13 @@ struct GradPtrs {
     double *grad[4];
 };
 
+// Green-Gauss gradient of NF fields, one thread per cell over its slots in
+// SELL-32 order: the slot words (face id, neighbour) of all six slots are loaded
+// first, so each cell waits for two rounds of loads instead of three per face.
+// The arithmetic and the summation order are those of the per-face form
+// (phi_f = lambda phi_c1 + (1 - lambda) phi_c2, negated for the face's cell2).
 template <int NF>
-__global__ void k_gradient_v(DomView d, GradPtrs p) {
-    // copy pointer tables to registers; indexable arrays of pointers in param space
+__global__ void __launch_bounds__(NB) k_gradient_v(DomView d, GradPtrs p) {
     const double *phi[NF];
     const double *Bphi[NF];
     double *grad[NF];
@@ -142,28 +146,46 @@ __global__ void k_gradient_v(DomView d, GradPtrs p) {
     for (int k = 0; k < NF; ++k) { phi[k] = p.phi[k]; Bphi[k] = p.Bphi[k]; grad[k] = p.grad[k]; }
     int i = blockIdx.x * NB + threadIdx.x;
     if (i >= d.nc) return;
+    const int sl = i >> 5, lane = i & 31;
+    const int base = d.ss_ptr[sl] + lane, w = d.ss_w[sl];
+    int fs[6], ns[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        fs[j] = -1;
+        ns[j] = 0;
+        if (j < w) {
+            fs[j] = __ldg(d.ss_f + base + 32 * j);
+            ns[j] = __ldg(d.ss_n + base + 32 * j);
+        }
+    }
+    double own[NF];
+#pragma unroll
+    for (int k = 0; k < NF; ++k) own[k] = __ldg(phi[k] + i);
     double g[NF][3];
 #pragma unroll
     for (int k = 0; k < NF; ++k) g[k][0] = g[k][1] = g[k][2] = 0.;
-    for (int s = d.cs_ptr[i]; s < d.cs_ptr[i + 1]; ++s) {
-        int f = d.cs_face[s];
-        double n0 = d.fn[f], n1 = d.fn[d.nf + f], n2 = d.fn[2 * d.nf + f];
-        int c1 = d.fc1[f];
+    const int nf = d.nf;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        const int f = fs[j];
+        if (f < 0) continue;
+        const int nb = ns[j];
+        double n0 = __ldg(d.fn + f), n1 = __ldg(d.fn + nf + f), n2 = __ldg(d.fn + 2 * nf + f);
         double pf[NF];
-        if (f < d.F) {
-            int c2 = d.fc2[f];
-            double lam = d.flam[f];
+        if (nb >= 0 && (nb & SS_BND)) {
+            const int b = nb & ~SS_BND;
+#pragma unroll
+            for (int k = 0; k < NF; ++k) pf[k] = __ldg(Bphi[k] + b);
+        } else {
+            const bool c2side = nb < 0;
+            const int o = nb & 0x7FFFFFFF;
+            double lam = __ldg(d.flam + f);
             double lam2 = 1. - lam;
 #pragma unroll
-            for (int k = 0; k < NF; ++k) pf[k] = lam * phi[k][c1] + lam2 * phi[k][c2];
-            if (c1 != i) {
-#pragma unroll
-                for (int k = 0; k < NF; ++k) pf[k] = -pf[k];
+            for (int k = 0; k < NF; ++k) {
+                double po = __ldg(phi[k] + o);
+                pf[k] = c2side ? -(lam * po + lam2 * own[k]) : lam * own[k] + lam2 * po;
             }
-        } else {
-            int b = f - d.F;
-#pragma unroll
-            for (int k = 0; k < NF; ++k) pf[k] = Bphi[k][b];
         }
 #pragma unroll
         for (int k = 0; k < NF; ++k) {
@@ -172,12 +194,15 @@ __global__ void k_gradient_v(DomView d, GradPtrs p) {
             g[k][2] += pf[k] * n2;
         }
     }
-    double vol = d.vol[i];
+    // one FP64 division per cell instead of 3 NF (the FP64 pipe bounds this
+    // kernel on GB300); the reference divides each component (BasicSolver.cpp:72),
+    // the results differ by at most an ulp
+    const double rvol = 1.0 / d.vol[i];
 #pragma unroll
     for (int k = 0; k < NF; ++k) {
-        grad[k][i] = g[k][0] / vol;
-        grad[k][d.nc + i] = g[k][1] / vol;
-        grad[k][2 * d.nc + i] = g[k][2] / vol;
+        grad[k][i] = g[k][0] * rvol;
+        grad[k][d.nc + i] = g[k][1] * rvol;
+        grad[k][2 * d.nc + i] = g[k][2] * rvol;
     }
 }
 
@@ -476,7 +501,7 @@ __global__ void k_rhie_chow(DomView d, PresArgs a) {
     dx0 = xn[f] - d.cx[c2]; dx1 = xn[F + f] - d.cx[nc + c2]; dx2 = xn[2 * F + f] - d.cx[2 * nc + c2];
     double P2 = a.P[c2] + (a.dP[c2] * dx0 + a.dP[nc + c2] * dx1 + a.dP[2 * nc + c2] * dx2);
     dx0 = xn[f] - xp[f]; dx1 = xn[F + f] - xp[F + f]; dx2 = xn[2 * F + f] - xp[2 * F + f];
-    double d12 = sqrt(dx0 * dx0 + dx1 * dx1 + dx2 * dx2);
+    double d12 = d.fd12[f];
     double Apr1 = a.Apr[c1], Apr2 = a.Apr[c2];
     double V1 = d.vol[c1], V2 = d.vol[c2];
     double aprf = lambda * Apr1 + lambda2 * Apr2;

@@ -22,10 +22,16 @@ struct DomView {
     const int *cs_ptr;           // nc+1 (slots = reference Cell[i].face[j] order)
     const int *cs_face;          // internal face id of each slot
     const int *cs_k;             // interior slot: position k >= 1 in the matrix row; boundary slot: record b
+    // the same slots in SELL-32 layout (slice of 32 cells, column-major, padded
+    // to the slice's widest cell): slot j of cell i at ss_ptr[i/32] + 32 j + i%32.
+    // ss_f: internal face id (-1 = padding); ss_n: neighbour cell (bit 31 set when
+    // the cell is the face's cell2) or, for a boundary slot, SS_BND | record
+    const int *ss_ptr, *ss_w, *ss_f, *ss_n;
     // faces
     const int *fc1, *fc2;        // fc2 < 0 on boundary faces
     const double *fn, *farea, *flam, *frl, *fx;  // fn, fx: 3*nf
     const double *fxpac, *fxnac; // 3*F
+    const double *fd12;          // F: |Xnac - Xpac| (geometric, precomputed: saves an FP64 sqrt per face)
     // boundary records
     const int *bcell, *btype1, *btype2, *brid;
     const double *bdist;
@@ -43,6 +49,9 @@ struct DomView {
     // matrix pattern
     SellView A;                  // val filled per equation
 };
+
+constexpr int SS_C2 = (int)0x80000000u;
+constexpr int SS_BND = 0x40000000;
 
 // Launch configuration shared by the FV kernels.
 constexpr int FV_BLOCK = 256;

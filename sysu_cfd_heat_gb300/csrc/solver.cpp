@@ -81,6 +81,36 @@ void DomainDev::build(const Domain &d, const Params &p, cudaStream_t st) {
     }
     pat = make_sell(nc, rowptr, cols);
     A.upload(pat, st);
+    {
+        // cell slots in SELL-32 layout (fv.hpp: ss_*)
+        int nsl = (nc + 31) / 32;
+        std::vector<int> sp(nsl + 1, 0), sw(nsl, 0);
+        for (int sl = 0; sl < nsl; ++sl) {
+            int w = 0;
+            for (int i = sl * 32; i < std::min(nc, sl * 32 + 32); ++i) w = std::max(w, h_csptr[i + 1] - h_csptr[i]);
+            sw[sl] = w;
+            sp[sl + 1] = sp[sl] + 32 * w;
+        }
+        std::vector<int> sf(std::max(sp[nsl], 1), -1), sn(std::max(sp[nsl], 1), 0);
+        for (int i = 0; i < nc; ++i) {
+            int sl = i >> 5, lane = i & 31;
+            for (int j = 0; j < h_csptr[i + 1] - h_csptr[i]; ++j) {
+                int fi = h_csface[h_csptr[i] + j];
+                int pos = sp[sl] + 32 * j + lane;
+                sf[pos] = fi;
+                if (fi < F) {
+                    int c1 = h_fc1[fi], c2 = h_fc2[fi];
+                    sn[pos] = c1 == i ? c2 : (c1 | SS_C2);
+                } else {
+                    sn[pos] = SS_BND | (fi - F);
+                }
+            }
+        }
+        ss_ptr.upload(sp, st);
+        ss_w.upload(sw, st);
+        ss_f.upload(sf, st);
+        ss_n.upload(sn, st);
+    }
 
     h_bcell.assign(B, 0);
     h_btype1.assign(B, 0);
@@ -137,6 +167,15 @@ void DomainDev::build(const Domain &d, const Params &p, cudaStream_t st) {
     fx.upload(h_fx, st);
     fxpac.upload(h_xp, st);
     fxnac.upload(h_xn, st);
+    {
+        std::vector<double> h_d12(std::max(F, 1), 0.0);
+        for (int fi = 0; fi < F; ++fi) {
+            double dx0 = h_xn[fi] - h_xp[fi], dx1 = h_xn[(size_t)F + fi] - h_xp[(size_t)F + fi],
+                   dx2 = h_xn[2 * (size_t)F + fi] - h_xp[2 * (size_t)F + fi];
+            h_d12[fi] = std::sqrt(dx0 * dx0 + dx1 * dx1 + dx2 * dx2);
+        }
+        fd12.upload(h_d12, st);
+    }
     bdist.upload(h_bdist, st);
     bquirk.upload(h_bquirk, st);
     bin.upload(h_bin, st);
@@ -161,9 +200,10 @@ void DomainDev::build(const Domain &d, const Params &p, cudaStream_t st) {
     v.nc = nc; v.nf = nf; v.F = F; v.B = B; v.ncb = ncb; v.nv = nv;
     v.vol = vol.get(); v.cx = cx.get();
     v.cs_ptr = cs_ptr.get(); v.cs_face = cs_face.get(); v.cs_k = cs_k.get();
+    v.ss_ptr = ss_ptr.get(); v.ss_w = ss_w.get(); v.ss_f = ss_f.get(); v.ss_n = ss_n.get();
     v.fc1 = fc1.get(); v.fc2 = fc2.get();
     v.fn = fn.get(); v.farea = farea.get(); v.flam = flam.get(); v.frl = frl.get(); v.fx = fx.get();
-    v.fxpac = fxpac.get(); v.fxnac = fxnac.get();
+    v.fxpac = fxpac.get(); v.fxnac = fxnac.get(); v.fd12 = fd12.get();
     v.bcell = bcell.get(); v.btype1 = btype1.get(); v.btype2 = btype2.get(); v.brid = brid.get();
     v.bdist = bdist.get(); v.bquirk_area = bquirk.get(); v.bin = bin.get(); v.bfixed = bfixed.get();
     v.cw_ptr = cw_ptr.get(); v.cw_b = cw_b.get();

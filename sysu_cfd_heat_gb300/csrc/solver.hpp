@@ -22,8 +22,9 @@ struct DomainDev {
     std::vector<int> ref2int;
     SellPattern pat;
     SellDev A;
-    DevBuf<double> vol, cx, fn, farea, flam, frl, fx, fxpac, fxnac, bdist, bquirk, bin, bfixed, vx;
+    DevBuf<double> vol, cx, fn, farea, flam, frl, fx, fxpac, fxnac, fd12, bdist, bquirk, bin, bfixed, vx;
     DevBuf<int> cs_ptr, cs_face, cs_k, fc1, fc2, bcell, btype1, btype2, brid, cw_ptr, cw_b, cvert, vc_ptr, vc_cell;
+    DevBuf<int> ss_ptr, ss_w, ss_f, ss_n;
     std::vector<int> h_btype1, h_btype2, h_bcell;
     void build(const Domain &d, const Params &p, cudaStream_t st);
 };
