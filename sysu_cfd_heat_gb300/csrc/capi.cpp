@@ -169,6 +169,7 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
     }
     if (k == "mom_batched") { o.mom_batched = value != 0.0; return SYSU_OK; }
     if (k == "sm_cap") { s->impl->kw.sm_cap = std::max(0, (int)value); return SYSU_OK; }
+    if (k == "spmv_variant") { sysu::set_spmv_variant((int)value); return SYSU_OK; }
     if (k == "scalars_batched") {
         const sysu::Params &pp = s->impl->cs.params;
         if (value != 0.0 && (pp.tur_model != 1 || !pp.solve_energy))

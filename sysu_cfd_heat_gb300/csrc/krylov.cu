@@ -177,6 +177,72 @@ __global__ void __launch_bounds__(256) k_spmv_stream(int n, const int *__restric
     y[i] = acc;
 }
 
+// The same product with a persistent grid: each warp takes SPW slices at a time
+// (slices s, s + W, ... for W warps in the grid), so every thread has SPW rows'
+// matrix entries in flight before its first gather.
+template <class V, int SPW>
+__global__ void __launch_bounds__(256) k_spmv_multi(int n, int nslices, const int *__restrict__ sl_ptr,
+                                                    const int *__restrict__ sl_w, const int *__restrict__ col,
+                                                    const V *__restrict__ val, const V *__restrict__ x,
+                                                    V *__restrict__ y) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int W = (gridDim.x * blockDim.x) >> 5;
+    for (int s0 = warp; s0 < nslices; s0 += SPW * W) {
+        int e[SPW], w[SPW];
+#pragma unroll
+        for (int q = 0; q < SPW; ++q) {
+            int s = s0 + q * W;
+            w[q] = 0;
+            e[q] = 0;
+            if (s < nslices) {
+                e[q] = __ldg(sl_ptr + s) + lane;
+                w[q] = __ldg(sl_w + s);
+            }
+        }
+        int c[SPW][8];
+        V a[SPW][8];
+#pragma unroll
+        for (int q = 0; q < SPW; ++q)
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (k < w[q]) {
+                    c[q][k] = __ldcs(col + e[q] + 32 * k);
+                    a[q][k] = __ldcs(val + e[q] + 32 * k);
+                }
+        V acc[SPW];
+#pragma unroll
+        for (int q = 0; q < SPW; ++q) {
+            acc[q] = (V)0;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (k < w[q]) acc[q] = fma(a[q][k], __ldg(x + c[q][k]), acc[q]);
+            for (int k = 8; k < w[q]; ++k)
+                acc[q] = fma(__ldcs(val + e[q] + 32 * k), __ldg(x + __ldcs(col + e[q] + 32 * k)), acc[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < SPW; ++q) {
+            int row = (s0 + q * W) * 32 + lane;
+            if (w[q] > 0 && row < n) y[row] = acc[q];
+        }
+    }
+}
+
+int g_spmv_variant = 0;
+
+// Reads a buffer larger than L2 (16-byte loads, one word written) so the
+// caches hold clean lines of it: evicting them costs no write-back, unlike a
+// flush by writes, whose dirty lines would be written back during the next
+// kernel and inflate its DRAM traffic.
+__global__ void k_l2_flush_read(const uint4 *__restrict__ buf, size_t n16, unsigned *sink) {
+    unsigned acc = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x) {
+        uint4 v = __ldcg(buf + i);
+        acc ^= v.x ^ v.y ^ v.z ^ v.w;
+    }
+    if (acc == 0x9e3779b9u) *sink = acc;  // keeps the loads; practically never taken
+}
+
 // A fixed, non-trivial x for the SpMV sweep: 1 + hash(i) / 2000.
 __global__ void k_fill_x(long n, double *x64, float *x32) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -433,15 +499,41 @@ void fill_sweep_x(long n, double *x64, float *x32, cudaStream_t st) {
     SYSU_CUDA(cudaGetLastError());
 }
 
-void spmv_stream(const SellDev &A, const double *val, const double *x, double *y, cudaStream_t st) {
+template <class V>
+static void spmv_dispatch(const SellDev &A, const V *val, const V *x, V *y, cudaStream_t st) {
     if (A.n == 0) return;
-    { k_spmv_stream<double><<<(A.n + 255) / 256, 256, 0, st>>>(A.n, A.sl_ptr.get(), A.sl_w.get(), A.col.get(), val, x, y); ++::sysu::g_launches; }
+    const int v = g_spmv_variant;
+    if (v == 0) {
+        k_spmv_stream<V><<<(A.n + 255) / 256, 256, 0, st>>>(A.n, A.sl_ptr.get(), A.sl_w.get(), A.col.get(), val, x, y);
+    } else {
+        int per_sm = v >= 10 ? v / 10 : 8;   // blocks of 256 per SM
+        int spw = v % 10;
+        int G = std::max(1, std::min((A.nslices * 32 + 255) / 256, num_sms() * per_sm));
+        if (spw == 1)
+            k_spmv_multi<V, 1><<<G, 256, 0, st>>>(A.n, A.nslices, A.sl_ptr.get(), A.sl_w.get(), A.col.get(), val, x, y);
+        else if (spw == 2)
+            k_spmv_multi<V, 2><<<G, 256, 0, st>>>(A.n, A.nslices, A.sl_ptr.get(), A.sl_w.get(), A.col.get(), val, x, y);
+        else
+            k_spmv_multi<V, 4><<<G, 256, 0, st>>>(A.n, A.nslices, A.sl_ptr.get(), A.sl_w.get(), A.col.get(), val, x, y);
+    }
+    ++::sysu::g_launches;
     SYSU_CUDA(cudaGetLastError());
 }
 
+void spmv_stream(const SellDev &A, const double *val, const double *x, double *y, cudaStream_t st) {
+    spmv_dispatch<double>(A, val, x, y, st);
+}
+
 void spmv_stream32(const SellDev &A, const float *val, const float *x, float *y, cudaStream_t st) {
-    if (A.n == 0) return;
-    { k_spmv_stream<float><<<(A.n + 255) / 256, 256, 0, st>>>(A.n, A.sl_ptr.get(), A.sl_w.get(), A.col.get(), val, x, y); ++::sysu::g_launches; }
+    spmv_dispatch<float>(A, val, x, y, st);
+}
+
+void set_spmv_variant(int v) { g_spmv_variant = v; }
+
+void l2_flush_read(const void *buf, size_t bytes, unsigned *sink, cudaStream_t st) {
+    size_t n16 = bytes / 16;
+    if (!n16) return;
+    { k_l2_flush_read<<<num_sms() * 8, 256, 0, st>>>(static_cast<const uint4 *>(buf), n16, sink); ++::sysu::g_launches; }
     SYSU_CUDA(cudaGetLastError());
 }
 

@@ -146,6 +146,11 @@ void spmv(const SellDev &A, const double *val, const double *x, double *y, cudaS
 // the standalone SpMV of the sweep.
 void spmv_stream(const SellDev &A, const double *val, const double *x, double *y, cudaStream_t st);
 void spmv_stream32(const SellDev &A, const float *val, const float *x, float *y, cudaStream_t st);
+// SpMV kernel form of spmv_stream / spmv_stream32: 0 one row per thread over a
+// full grid; 10 b + s: b blocks of 256 per SM, s in {1, 2, 4} slices per warp step.
+void set_spmv_variant(int v);
+// L2 flush by reading `bytes` (> L2) of buf: clean lines, no write-back later.
+void l2_flush_read(const void *buf, size_t bytes, unsigned *sink, cudaStream_t st);
 // x of the sweep (FP64 and its FP32 copy).
 void fill_sweep_x(long n, double *x64, float *x32, cudaStream_t st);
 

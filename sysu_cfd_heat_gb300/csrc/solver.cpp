@@ -924,6 +924,8 @@ double SimpleSolver::spmv_timing(const std::string &which, bool fp32, int reps) 
     DevBuf<double> x64(n), y64(n);
     DevBuf<float> x32(n), y32(n), v32;
     DevBuf<unsigned char> flush((size_t)256 << 20);
+    DevBuf<unsigned> sink(1);
+    SYSU_CUDA(cudaMemsetAsync(flush.get(), 1, flush.size(), st));
     fill_sweep_x((long)n, x64.get(), x32.get(), st);
     if (fp32) {
         v32.alloc((size_t)A.nnz);
@@ -931,7 +933,7 @@ double SimpleSolver::spmv_timing(const std::string &which, bool fp32, int reps) 
     }
     double total = 0.0;
     for (int k = 0; k < reps + 1; ++k) {
-        SYSU_CUDA(cudaMemsetAsync(flush.get(), k & 0xff, flush.size(), st));
+        l2_flush_read(flush.get(), flush.size(), sink.get(), st);
         SYSU_CUDA(cudaEventRecord(ev[4], st));
         if (fp32) spmv_stream32(A, v32.get(), x32.get(), y32.get(), st);
         else spmv_stream(A, v->get(), x64.get(), y64.get(), st);
