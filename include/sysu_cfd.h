@@ -19,6 +19,8 @@
 #ifndef SYSU_CFD_H
 #define SYSU_CFD_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -64,6 +66,11 @@ int sysu_solver_create(const char *param_path, sysu_solver **out);
  * [3] geometry (CellFaceInfo); out[4] = host threads used (SYSU_THREADS or the
  * hardware count; the results do not depend on it). */
 int sysu_setup_phases(double *out);
+/* Page-locked host memory for field transfers (sysu_solver_get_field /
+ * set_field copy it by DMA; pageable memory works too, through the driver's
+ * staging). NULL on failure. */
+void *sysu_host_alloc(size_t bytes);
+void sysu_host_free(void *p);
 void sysu_solver_destroy(sysu_solver *s);
 /* out[0..5] = Ncel, Nfac, Nbnd, solid Ncel, matrix stored entries, matrix true entries */
 int sysu_solver_info(sysu_solver *s, long *out, int n);

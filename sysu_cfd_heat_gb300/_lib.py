@@ -75,6 +75,8 @@ def lib() -> C.CDLL:
             "sysu_csr_bicgstab_batched3": (C.c_int, [C.c_int, ip, ip, C.POINTER(dp), C.POINTER(dp), C.POINTER(dp),
                                                      C.c_int, C.c_double, ip, dp, ip]),
             "sysu_setup_phases": (C.c_int, [dp]),
+            "sysu_host_alloc": (vp, [C.c_size_t]),
+            "sysu_host_free": (None, [vp]),
             "sysu_batch_create": (C.c_int, [C.c_int, C.POINTER(cp), C.POINTER(vp)]),
             "sysu_batch_free": (None, [vp]),
             "sysu_batch_size": (C.c_int, [vp]),
@@ -107,6 +109,20 @@ def lib() -> C.CDLL:
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+def pinned_empty(n: int) -> np.ndarray:
+    """A float64 array of n values in page-locked host memory (freed with the array)."""
+    import weakref
+
+    L = lib()
+    ptr = L.sysu_host_alloc(max(int(n), 1) * 8)
+    if not ptr:
+        raise SysuError(2, "page-locked host allocation failed")
+    buf = (C.c_double * max(int(n), 1)).from_address(ptr)
+    arr = np.ctypeslib.as_array(buf)[:n]
+    weakref.finalize(arr, L.sysu_host_free, ptr)
+    return arr
 
 
 def check(code: int) -> None:

@@ -599,6 +599,19 @@ void sysu_batch_free(sysu_batch *b) {
     delete b;
 }
 
+void *sysu_host_alloc(size_t bytes) {
+    void *p = nullptr;
+    if (cudaHostAlloc(&p, bytes ? bytes : 1, cudaHostAllocDefault) != cudaSuccess) {
+        set_err(SYSU_ERR_CUDA, "cudaHostAlloc failed");
+        return nullptr;
+    }
+    return p;
+}
+
+void sysu_host_free(void *p) {
+    if (p) cudaFreeHost(p);
+}
+
 int sysu_setup_phases(double *out) {
     if (!out) return set_err(SYSU_ERR_INPUT, "null argument");
     for (int k = 0; k < 5; ++k) out[k] = sysu::setup_phases()[k];

@@ -975,6 +975,27 @@ __global__ void k_scale_src(double *dst, const double *vol, double q, int n) {
     if (i < n) dst[i] = q * vol[i];
 }
 
+__global__ void k_gather(double *dst, const double *src, const int *idx, int n) {
+    int i = blockIdx.x * NB + threadIdx.x;
+    if (i < n) dst[i] = src[idx[i]];
+}
+__global__ void k_scatter(double *dst, const double *src, const int *idx, int n) {
+    int i = blockIdx.x * NB + threadIdx.x;
+    if (i < n) dst[idx[i]] = src[i];
+}
+__global__ void k_aos3_to_soa3(double *dst, const double *src, int n) {
+    int t = blockIdx.x * NB + threadIdx.x;
+    if (t >= 3 * n) return;
+    int i = t / 3, k = t % 3;
+    dst[(size_t)k * n + i] = src[t];
+}
+__global__ void k_soa3_to_aos3(double *dst, const double *src, int n) {
+    int t = blockIdx.x * NB + threadIdx.x;
+    if (t >= 3 * n) return;
+    int i = t / 3, k = t % 3;
+    dst[t] = src[(size_t)k * n + i];
+}
+
 #define CHECK_LAUNCH() SYSU_CUDA(cudaGetLastError())
 
 }  // namespace
@@ -1041,6 +1062,27 @@ void launch_momentum(const DomView &d, const MomArgs &a, cudaStream_t st) {
 void launch_commit3(const DomView &d, double *U, double *V, double *W, const double *x3, RedScratch rs,
                     cudaStream_t st) {
     { k_commit3<<<nblk_capped(d.nc, rs.max_blocks), NB, 0, st>>>(d, U, V, W, x3, rs); ++::sysu::g_launches; }
+    CHECK_LAUNCH();
+}
+
+void launch_gather(double *dst, const double *src, const int *idx, int n, cudaStream_t st) {
+    if (n <= 0) return;
+    { k_gather<<<nblk(n), NB, 0, st>>>(dst, src, idx, n); ++::sysu::g_launches; }
+    CHECK_LAUNCH();
+}
+void launch_scatter(double *dst, const double *src, const int *idx, int n, cudaStream_t st) {
+    if (n <= 0) return;
+    { k_scatter<<<nblk(n), NB, 0, st>>>(dst, src, idx, n); ++::sysu::g_launches; }
+    CHECK_LAUNCH();
+}
+void launch_aos3_to_soa3(double *dst, const double *src, int n, cudaStream_t st) {
+    if (n <= 0) return;
+    { k_aos3_to_soa3<<<nblk(3 * n), NB, 0, st>>>(dst, src, n); ++::sysu::g_launches; }
+    CHECK_LAUNCH();
+}
+void launch_soa3_to_aos3(double *dst, const double *src, int n, cudaStream_t st) {
+    if (n <= 0) return;
+    { k_soa3_to_aos3<<<nblk(3 * n), NB, 0, st>>>(dst, src, n); ++::sysu::g_launches; }
     CHECK_LAUNCH();
 }
 

@@ -153,6 +153,12 @@ void launch_correct_faces(const DomView &d, const double *dp, const double *dPdp
 void launch_energy_viscous(const DomView &d, const double *VisLam, const double *VisTur, const double *dU,
                            const double *dV, const double *dW, const double *U, const double *V, const double *W,
                            double cp, double *src, cudaStream_t st);
+// Field transfer helpers: dst[i] = src[idx[i]] / dst[idx[i]] = src[i], and the
+// [k*n + i] <-> [3 i + k] reshuffle of the gradient fields.
+void launch_gather(double *dst, const double *src, const int *idx, int n, cudaStream_t st);
+void launch_scatter(double *dst, const double *src, const int *idx, int n, cudaStream_t st);
+void launch_aos3_to_soa3(double *dst, const double *src, int n, cudaStream_t st);
+void launch_soa3_to_aos3(double *dst, const double *src, int n, cudaStream_t st);
 // Bphi[b] = phi(cell of b) for every record: SetBCPressure / SetBCDeltaP (navier_bc.cpp:110-162)
 void launch_bnd_from_cell(const DomView &d, const double *phi, double *Bphi, cudaStream_t st);
 

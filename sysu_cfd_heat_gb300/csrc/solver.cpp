@@ -81,6 +81,7 @@ void DomainDev::build(const Domain &d, const Params &p, cudaStream_t st) {
     }
     pat = make_sell(nc, rowptr, cols);
     A.upload(pat, st);
+    d_int2ref.upload(int2ref, st);
     {
         // cell slots in SELL-32 layout (fv.hpp: ss_*)
         int nsl = (nc + 31) / 32;
@@ -1003,6 +1004,10 @@ long SimpleSolver::field_size(const std::string &name) const {
     }
 }
 
+// Host <-> device field transfers: straight asynchronous copies for cell and
+// record fields (DMA when the host buffer is pinned, e.g. from
+// sysu_host_alloc), reordering on the device through a staging buffer for
+// gradients and face fluxes.
 void SimpleSolver::get_field(const std::string &name, double *out, long n) {
     int kind;
     bool solid;
@@ -1011,18 +1016,15 @@ void SimpleSolver::get_field(const std::string &name, double *out, long n) {
     long sz = field_size(name);
     if (n != sz) throw CaseError{"field " + name + " has " + std::to_string(sz) + " values"};
     const DomainDev &d = solid ? sd : fd;
-    std::vector<double> tmp((size_t)std::max(sz, 1L));
-    b->download(tmp.data(), (size_t)sz, st);
-    SYSU_CUDA(cudaStreamSynchronize(st));
-    if (kind == 1) {
-        int nc = d.nc;
-        for (int i = 0; i < nc; ++i)
-            for (int k = 0; k < 3; ++k) out[(size_t)i * 3 + k] = tmp[(size_t)k * nc + i];
-    } else if (kind == 2) {
-        for (int fi = 0; fi < d.nf; ++fi) out[d.int2ref[fi]] = tmp[fi];
-    } else {
-        std::memcpy(out, tmp.data(), sizeof(double) * (size_t)sz);
+    const double *src = b->get();
+    if (kind == 1 || kind == 2) {
+        if (io_stage.size() < (size_t)sz) io_stage.alloc((size_t)sz);
+        if (kind == 1) launch_soa3_to_aos3(io_stage.get(), b->get(), d.nc, st);
+        else launch_scatter(io_stage.get(), b->get(), d.d_int2ref.get(), d.nf, st);
+        src = io_stage.get();
     }
+    if (sz) SYSU_CUDA(cudaMemcpyAsync(out, src, sizeof(double) * (size_t)sz, cudaMemcpyDeviceToHost, st));
+    SYSU_CUDA(cudaStreamSynchronize(st));
 }
 
 void SimpleSolver::set_field(const std::string &name, const double *in, long n) {
@@ -1033,17 +1035,14 @@ void SimpleSolver::set_field(const std::string &name, const double *in, long n) 
     long sz = field_size(name);
     if (n != sz) throw CaseError{"field " + name + " has " + std::to_string(sz) + " values"};
     const DomainDev &d = solid ? sd : fd;
-    std::vector<double> tmp((size_t)std::max(sz, 1L));
-    if (kind == 1) {
-        int nc = d.nc;
-        for (int i = 0; i < nc; ++i)
-            for (int k = 0; k < 3; ++k) tmp[(size_t)k * nc + i] = in[(size_t)i * 3 + k];
-    } else if (kind == 2) {
-        for (int fi = 0; fi < d.nf; ++fi) tmp[fi] = in[d.int2ref[fi]];
-    } else {
-        std::memcpy(tmp.data(), in, sizeof(double) * (size_t)sz);
+    if (kind == 1 || kind == 2) {
+        if (io_stage.size() < (size_t)sz) io_stage.alloc((size_t)sz);
+        if (sz) SYSU_CUDA(cudaMemcpyAsync(io_stage.get(), in, sizeof(double) * (size_t)sz, cudaMemcpyHostToDevice, st));
+        if (kind == 1) launch_aos3_to_soa3(b->get(), io_stage.get(), d.nc, st);
+        else launch_gather(b->get(), io_stage.get(), d.d_int2ref.get(), d.nf, st);
+    } else if (sz) {
+        SYSU_CUDA(cudaMemcpyAsync(b->get(), in, sizeof(double) * (size_t)sz, cudaMemcpyHostToDevice, st));
     }
-    b->upload(tmp.data(), (size_t)sz, st);
     SYSU_CUDA(cudaStreamSynchronize(st));
 }
 

@@ -25,6 +25,7 @@ struct DomainDev {
     DevBuf<double> vol, cx, fn, farea, flam, frl, fx, fxpac, fxnac, fd12, bdist, bquirk, bin, bfixed, vx;
     DevBuf<int> cs_ptr, cs_face, cs_k, fc1, fc2, bcell, btype1, btype2, brid, cw_ptr, cw_b, cvert, vc_ptr, vc_cell;
     DevBuf<int> ss_ptr, ss_w, ss_f, ss_n;
+    DevBuf<int> d_int2ref;  // internal face -> reference face (field transfers)
     std::vector<int> h_btype1, h_btype2, h_bcell;
     void build(const Domain &d, const Params &p, cudaStream_t st);
 };
@@ -135,6 +136,7 @@ class SimpleSolver {
     GnnPrecond gnn;             // learned p' preconditioner (option p.learned)
     int p_solves = 0;           // p' solves so far (training window of the learned form)
     DevBuf<double> gnn_x1;      // partial solution of a training solve
+    DevBuf<double> io_stage;    // staging for reordered field transfers
     DevBuf<SolveInfo> infos;
     DevBuf<double> red_partials, red_out;
     DevBuf<unsigned int> red_ticket;

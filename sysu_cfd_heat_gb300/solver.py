@@ -186,9 +186,14 @@ class NavierStokesSolver:
             raise KeyError(name)
         return n
 
-    def get(self, name: str) -> np.ndarray:
+    def get(self, name: str, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """Field by the reference's member name; into `out` (contiguous float64,
+        e.g. page-locked from _lib.pinned_empty) when given."""
         n = self.field_size(name)
-        out = np.empty(n, dtype=np.float64)
+        if out is None:
+            out = np.empty(n, dtype=np.float64)
+        elif out.dtype != np.float64 or out.size != n or not out.flags.c_contiguous:
+            raise ValueError(f"out must be a contiguous float64 array of {n} values")
         check(lib().sysu_solver_get_field(self._h, name.encode(), _dptr(out), n))
         return out
 
