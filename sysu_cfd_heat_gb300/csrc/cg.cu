@@ -693,6 +693,7 @@ void cg_solve(const SellDev &A, const double *val, const double *b, double *x, b
     a.plan = plan_cg(A.wmax, 8);
     void *args[] = {&a};
     int G = cg_grid(A, a.plan, maxb, w.sm_cap);
+    SYSU_CUDA(cudaMemsetAsync(w.barrier.get(), 0, sizeof(GridBarrier), st));  // grid_sync starts from 0
     { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_cg_pipe, dim3(G), dim3(KBC), args, a.plan.smem, st)); ++::sysu::g_launches; }
 }
 
@@ -730,6 +731,7 @@ void cg_solve_mixed(const SellDev &A, const double *val, const float *val32, con
     a.plan = plan_cg(A.wmax, 4);
     void *args[] = {&a};
     int G = cg_grid(A, a.plan, maxb, w.sm_cap);
+    SYSU_CUDA(cudaMemsetAsync(w.barrier.get(), 0, sizeof(GridBarrier), st));  // grid_sync starts from 0
     { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_cg_mixed_pipe, dim3(G), dim3(KBC), args, a.plan.smem, st)); ++::sysu::g_launches; }
 }
 

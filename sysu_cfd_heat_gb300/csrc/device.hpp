@@ -90,9 +90,9 @@ enum DevStatus : int {
 #ifdef __CUDACC__
 
 constexpr unsigned FULL_MASK = 0xffffffffu;
-// About one second of polling at ~100 ns per poll; a wait that is still not
-// over by then records DEV_BARRIER_TIMEOUT and gives up.
-constexpr long long BARRIER_SPIN_LIMIT = 10000000LL;
+// A few seconds of polling (each poll is an L2 round trip); a wait that is
+// still not over by then records DEV_BARRIER_TIMEOUT and gives up.
+constexpr long long BARRIER_SPIN_LIMIT = 4000000LL;
 
 __device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p) {
     unsigned int v;
@@ -100,34 +100,31 @@ __device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p) {
     return v;
 }
 
-// Sense-reversing grid barrier.  Every block of a cooperative launch calls it
-// the same number of times.  Returns false (and sets *err) if the wait timed
-// out, in which case the caller must leave the kernel.
+// Grid barrier of a cooperative launch on one 32-bit counter whose low 31 bits
+// are zero between barriers: block 0 adds 2^31 - (blocks - 1), every other
+// block adds 1, so the counter's top bit flips exactly when the last block
+// arrives and returns the low bits to zero.  One release atomic per block to
+// arrive, acquire loads to wait (no reset step, no separate generation word).
+// Every block calls it the same number of times; the counter must be zero (or
+// 2^31) when the launch starts -- the solvers clear it before each launch.
+// Returns false (and sets *err) if the wait timed out, in which case the caller
+// must leave the kernel.
 __device__ __forceinline__ bool grid_sync(GridBarrier *gb, int *err) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
-        unsigned int nb = gridDim.x;
-        unsigned int my_gen = ld_acquire(&gb->gen);
-        __threadfence();
-        unsigned int arrived = atomicAdd(&gb->count, 1u);
-        if (arrived == nb - 1) {
-            atomicExch(&gb->count, 0u);
-            __threadfence();
-            atomicAdd(&gb->gen, 1u);
-        } else {
-            long long spins = 0;
-            while (ld_acquire(&gb->gen) == my_gen) {
-                if (++spins > BARRIER_SPIN_LIMIT) {
-                    atomicExch(err, (int)DEV_BARRIER_TIMEOUT);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
+        const unsigned inc = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
+        unsigned old;
+        asm volatile("atom.add.release.gpu.u32 %0, [%1], %2;" : "=r"(old) : "l"(&gb->count), "r"(inc) : "memory");
+        long long spins = 0;
+        while (((ld_acquire(&gb->count) ^ old) & 0x80000000u) == 0u) {
+            if (++spins > BARRIER_SPIN_LIMIT) {
+                atomicExch(err, (int)DEV_BARRIER_TIMEOUT);
+                ok = 0;
+                break;
             }
         }
-        __threadfence();
         s_ok = ok;
     }
     __syncthreads();

@@ -575,6 +575,7 @@ void gmres_solve(const SellDev &A, const double *val, const double *b, double *x
     a.m = restart;
     a.eps = o.eps;
     void *args[] = {&a};
+    SYSU_CUDA(cudaMemsetAsync(w.barrier.get(), 0, sizeof(GridBarrier), st));  // grid_sync starts from 0
     { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_gmres, dim3(G), dim3(GM_THREADS), args, 0, st)); ++::sysu::g_launches; }
 }
 
@@ -603,6 +604,7 @@ void pcg_solve(const SellDev &A, const double *val, const double *b, double *x, 
     a.maxit = o.maxit;
     a.eps = o.eps;
     void *args[] = {&a};
+    SYSU_CUDA(cudaMemsetAsync(w.barrier.get(), 0, sizeof(GridBarrier), st));  // grid_sync starts from 0
     { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_pcg, dim3(G), dim3(GM_THREADS), args, 0, st)); ++::sysu::g_launches; }
 }
 
@@ -623,6 +625,7 @@ void precond_solve(const SellDev &A, const double *val, int precond, double omeg
     a.gb = w.barrier.get();
     a.info = info;
     void *args[] = {&a};
+    SYSU_CUDA(cudaMemsetAsync(w.barrier.get(), 0, sizeof(GridBarrier), st));  // grid_sync starts from 0
     { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_precond_once, dim3(G), dim3(GM_THREADS), args, 0, st)); ++::sysu::g_launches; }
 }
 

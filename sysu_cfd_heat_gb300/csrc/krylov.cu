@@ -585,6 +585,7 @@ static void bicg_launch(const SellDev &A, const double *const *vals, bool multi,
     int G = grid_for(n, maxb);
     const void *k = nrhs == 1 ? (const void *)k_bicgstab<1, false>
                               : (multi ? (const void *)k_bicgstab<3, true> : (const void *)k_bicgstab<3, false>);
+    SYSU_CUDA(cudaMemsetAsync(w.barrier.get(), 0, sizeof(GridBarrier), st));  // grid_sync starts from 0
     SYSU_CUDA(cudaLaunchCooperativeKernel(k, dim3(G), dim3(KB), args, 0, st));
     ++::sysu::g_launches;
 }
