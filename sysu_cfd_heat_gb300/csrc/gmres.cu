@@ -33,6 +33,7 @@ struct Pre {
     int kind;
     double omega;
     const int *fptr, *frows, *bptr, *brows;
+    const int4 *finfo, *binfo;
     int nf, nb;
 };
 
@@ -127,58 +128,60 @@ __device__ __forceinline__ double sell_row(const SellView &A, const double *__re
     return acc;
 }
 
+// Row updates of the triangular sweeps.  (i, e, w) = row, SELL position of its
+// entry 0, slice width (one 16-byte load from the level schedule).  Rows of up
+// to 8 stored entries load all their columns and values first and then gather
+// y, so a row costs two dependent load rounds; the arithmetic and its order are
+// those of the plain loop.
+#define SWEEP_ROW(COND, COEF, ARR)                                                              \
+    if (w <= 8) {                                                                              \
+        int jj[8];                                                                             \
+        double aa[8];                                                                          \
+        _Pragma("unroll") for (int k = 1; k < 8; ++k) if (k < w) {                            \
+            jj[k] = P.A.col[e + 32 * k];                                                       \
+            aa[k] = ARR[e + 32 * k];                                                           \
+        }                                                                                      \
+        _Pragma("unroll") for (int k = 1; k < 8; ++k) if (k < w) {                            \
+            int j = jj[k];                                                                     \
+            if (COND) acc -= COEF aa[k] * y[j];                                                \
+        }                                                                                      \
+    } else {                                                                                   \
+        for (int k = 1; k < w; ++k) {                                                          \
+            int j = P.A.col[e + 32 * k];                                                       \
+            if (COND) acc -= COEF ARR[e + 32 * k] * y[j];                                     \
+        }                                                                                      \
+    }
+
 // Forward sweep of SSOR for one row: y_i = (f c_i - w sum_{j<i} a_ij y_j) / a_ii.
-__device__ __forceinline__ void ssor_fwd_row(const Pre &P, int i, double f, const double *c, double *y) {
-    int s = i >> 5;
-    int e = __ldg(P.A.sl_ptr + s) + (i & 31);
-    int w = __ldg(P.A.sl_w + s);
+__device__ __forceinline__ void ssor_fwd_row(const Pre &P, int i, int e, int w, double f, const double *c,
+                                             double *y) {
     double d = P.A.val[e];
     double acc = f * c[i];
-    for (int k = 1; k < w; ++k) {
-        int j = P.A.col[e + 32 * k];
-        if (j < i) acc -= P.omega * P.A.val[e + 32 * k] * y[j];
-    }
+    SWEEP_ROW(j < i, P.omega *, P.A.val)
     y[i] = acc / d;
 }
 
 // Backward sweep: y_i = (a_ii y_i - w sum_{j>i} a_ij y_j) / a_ii.
-__device__ __forceinline__ void ssor_bwd_row(const Pre &P, int i, double *y) {
-    int s = i >> 5;
-    int e = __ldg(P.A.sl_ptr + s) + (i & 31);
-    int w = __ldg(P.A.sl_w + s);
+__device__ __forceinline__ void ssor_bwd_row(const Pre &P, int i, int e, int w, double *y) {
     double d = P.A.val[e];
     double acc = d * y[i];
-    for (int k = 1; k < w; ++k) {
-        int j = P.A.col[e + 32 * k];
-        if (j > i) acc -= P.omega * P.A.val[e + 32 * k] * y[j];
-    }
+    SWEEP_ROW(j > i, P.omega *, P.A.val)
     y[i] = acc / d;
 }
 
 // ILU(0) apply rows: forward L y = c (unit diagonal), backward U y = y.
-__device__ __forceinline__ void ilu_fwd_row(const Pre &P, int i, const double *c, double *y) {
-    int s = i >> 5;
-    int e = __ldg(P.A.sl_ptr + s) + (i & 31);
-    int w = __ldg(P.A.sl_w + s);
+__device__ __forceinline__ void ilu_fwd_row(const Pre &P, int i, int e, int w, const double *c, double *y) {
     double acc = c[i];
-    for (int k = 1; k < w; ++k) {
-        int j = P.A.col[e + 32 * k];
-        if (j < i) acc -= P.ilu[e + 32 * k] * y[j];
-    }
+    SWEEP_ROW(j < i, , P.ilu)
     y[i] = acc;
 }
 
-__device__ __forceinline__ void ilu_bwd_row(const Pre &P, int i, double *y) {
-    int s = i >> 5;
-    int e = __ldg(P.A.sl_ptr + s) + (i & 31);
-    int w = __ldg(P.A.sl_w + s);
+__device__ __forceinline__ void ilu_bwd_row(const Pre &P, int i, int e, int w, double *y) {
     double acc = y[i];
-    for (int k = 1; k < w; ++k) {
-        int j = P.A.col[e + 32 * k];
-        if (j > i) acc -= P.ilu[e + 32 * k] * y[j];
-    }
+    SWEEP_ROW(j > i, , P.ilu)
     y[i] = acc / P.ilu[e];
 }
+#undef SWEEP_ROW
 
 // ILU(0) factorisation of row i (IKJ): its lower entries in ascending column
 // order, each eliminating with the already factorised row j.  Entries k >= 1
@@ -247,22 +250,34 @@ __device__ bool precond_dev(const Pre &P, int n, const double *c, double *y, Gri
     if (P.kind == PK_SSOR) {
         const double f = P.omega * (2.0 - P.omega);
         for (int l = 0; l < P.nf; ++l) {
-            for (int r = P.fptr[l] + gtid; r < P.fptr[l + 1]; r += T) ssor_fwd_row(P, P.frows[r], f, c, y);
+            for (int r = P.fptr[l] + gtid; r < P.fptr[l + 1]; r += T) {
+                int4 q = P.finfo[r];
+                ssor_fwd_row(P, q.x, q.y, q.z, f, c, y);
+            }
             if (!grid_sync(gb, err)) return false;
         }
         for (int l = 0; l < P.nb; ++l) {
-            for (int r = P.bptr[l] + gtid; r < P.bptr[l + 1]; r += T) ssor_bwd_row(P, P.brows[r], y);
+            for (int r = P.bptr[l] + gtid; r < P.bptr[l + 1]; r += T) {
+                int4 q = P.binfo[r];
+                ssor_bwd_row(P, q.x, q.y, q.z, y);
+            }
             if (!grid_sync(gb, err)) return false;
         }
         return true;
     }
     // ILU(0)
     for (int l = 0; l < P.nf; ++l) {
-        for (int r = P.fptr[l] + gtid; r < P.fptr[l + 1]; r += T) ilu_fwd_row(P, P.frows[r], c, y);
+        for (int r = P.fptr[l] + gtid; r < P.fptr[l + 1]; r += T) {
+            int4 q = P.finfo[r];
+            ilu_fwd_row(P, q.x, q.y, q.z, c, y);
+        }
         if (!grid_sync(gb, err)) return false;
     }
     for (int l = 0; l < P.nb; ++l) {
-        for (int r = P.bptr[l] + gtid; r < P.bptr[l + 1]; r += T) ilu_bwd_row(P, P.brows[r], y);
+        for (int r = P.bptr[l] + gtid; r < P.bptr[l + 1]; r += T) {
+            int4 q = P.binfo[r];
+            ilu_bwd_row(P, q.x, q.y, q.z, y);
+        }
         if (!grid_sync(gb, err)) return false;
     }
     return true;
@@ -524,6 +539,8 @@ Pre make_pre(const SellDev &A, const double *val, int precond, double omega, Kry
     P.frows = A.lev.frows.get();
     P.bptr = A.lev.bptr.get();
     P.brows = A.lev.brows.get();
+    P.finfo = A.lev.finfo.get();
+    P.binfo = A.lev.binfo.get();
     P.nf = A.lev.nf;
     P.nb = A.lev.nb;
     if (precond == PK_JACOBI) {

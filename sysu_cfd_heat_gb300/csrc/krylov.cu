@@ -105,6 +105,16 @@ void SellDev::upload(const SellPattern &p, cudaStream_t s) {
     lev.frows.upload(fr, s);
     lev.bptr.upload(bp, s);
     lev.brows.upload(br, s);
+    auto info = [&](const std::vector<int> &rows) {
+        std::vector<int4> v(rows.size());
+        for (size_t r = 0; r < rows.size(); ++r) {
+            int i = rows[r];
+            v[r] = make_int4(i, p.sl_ptr[i >> 5] + (i & 31), p.sl_w[i >> 5], 0);
+        }
+        return v;
+    };
+    lev.finfo.upload(info(fr), s);
+    lev.binfo.upload(info(br), s);
 }
 
 namespace {

@@ -41,6 +41,9 @@ SellPattern make_sell(int n, const std::vector<int> &row_ptr, const std::vector<
 struct LevelSchedule {
     int nf = 0, nb = 0;  // number of forward / backward levels
     DevBuf<int> fptr, frows, bptr, brows;
+    // per level-ordered row: {row, SELL position of its entry 0, slice width, 0},
+    // so a sweep reads everything it needs to start a row in one 16-byte load
+    DevBuf<int4> finfo, binfo;
 };
 
 struct SellDev {
