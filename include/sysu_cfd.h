@@ -289,6 +289,9 @@ int sysu_gnn_fcg(sysu_gnn *g, const double *b, double *x, int x0_zero, int maxit
                  int *refinements, double *seconds);
 /* hidden state h^layer (layer 1..4) of the network on r, FP32 [n][32] */
 int sysu_gnn_hidden(sysu_gnn *g, const double *r, int layer, float *h);
+/* device ms of one network application on r (mean of reps); fwd_per_sm > 0
+ * sets the forward kernel's CTAs per SM (0: derived from its registers) */
+int sysu_gnn_time_apply(sysu_gnn *g, const double *r, int reps, int fwd_per_sm, double *ms);
 const char *sysu_gnn_last_error(void);
 
 #ifdef __cplusplus

@@ -101,6 +101,7 @@ def lib() -> C.CDLL:
             "sysu_gnn_fcg": (C.c_int, [vp, dp, dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int,
                                        ip, dp, ip, ip, ip, dp]),
             "sysu_gnn_hidden": (C.c_int, [vp, dp, C.c_int, fp]),
+            "sysu_gnn_time_apply": (C.c_int, [vp, dp, C.c_int, C.c_int, dp]),
             "sysu_gnn_last_error": (cp, []),
         }
         for name, (res, args) in sig.items():

@@ -87,17 +87,6 @@ __device__ bool grid_sums(double (&v)[NV], double *part, unsigned *cnt) {
     return true;
 }
 
-// Wait for the MMA commit of this tile (bounded by COPY_WAIT_NS).
-__device__ __forceinline__ bool mma_wait(uint64_t *bar, unsigned parity, int mode) {
-    if (mode == 0) return mbar_wait(bar, parity);
-    unsigned long long t0 = global_timer_ns();
-    for (;;) {
-        bool ok = mode == 1 ? mbar_try_wait(bar, parity) : mbar_test_wait(bar, parity);
-        if (ok) return true;
-        if (global_timer_ns() - t0 > COPY_WAIT_NS) return false;
-    }
-}
-
 // ---------------------------------------------------------------- forward --
 
 struct NetArgs {
@@ -116,7 +105,6 @@ struct NetArgs {
     FcgState *fs;
     double *part;
     int *err;
-    int wait_mode;
 };
 
 template <bool L1, bool TRAIN, bool DEC>
@@ -264,7 +252,7 @@ __global__ void __launch_bounds__(GT) k_gnn_fwd(NetArgs a) {
             umma::commit(bar);
         }
         __syncwarp();
-        bool fail = !mma_wait(bar, it & 1, a.wait_mode);
+        bool fail = !mbar_wait(bar, it & 1);
         if (__syncthreads_or(fail)) {
             if (tid == 0) atomicExch(a.err, (int)DEV_BARRIER_TIMEOUT);
             break;
@@ -1087,7 +1075,6 @@ void GnnPrecond::forward(const float *r32, float *z32, bool train, FcgState *fs,
     a.fs = fs;
     a.part = part_.get();
     a.err = err_.get();
-    a.wait_mode = wait_mode;
     const size_t nn = (size_t)n_ * 32;
     for (int l = 0; l < GNN_LAYERS; ++l) {
         a.layer = l;

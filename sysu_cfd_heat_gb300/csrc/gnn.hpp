@@ -78,8 +78,7 @@ class GnnPrecond {
 
     // device time of one network application (ms), averaged over reps
     double time_apply(const double *r, int reps, cudaStream_t st);
-    int wait_mode = 0;    // MMA completion wait: 0 try_wait with sleep hint, 1 try_wait, 2 test_wait spin
-    int fwd_per_sm = 0;   // forward CTAs per SM (0: occupancy limit); applied at bind
+    int fwd_per_sm = 0;   // forward CTAs per SM (0: from registers and shared memory); applied at bind
 
     // Training pairs: a ring of `capacity` FP32 pairs.
     void set_capacity(int pairs) { capacity_ = pairs; }

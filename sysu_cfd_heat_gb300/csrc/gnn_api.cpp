@@ -196,11 +196,10 @@ int sysu_gnn_hidden(sysu_gnn *g, const double *r, int layer, float *h) {
     });
 }
 
-int sysu_gnn_time_apply(sysu_gnn *g, const double *r, int reps, int wait_mode, int fwd_per_sm, double *ms) {
+int sysu_gnn_time_apply(sysu_gnn *g, const double *r, int reps, int fwd_per_sm, double *ms) {
     if (!g || !r || !ms) return SYSU_ERR_INPUT;
     return guarded([&] {
         g->v0.upload(r, g->net.n(), g->st);
-        g->net.wait_mode = wait_mode;
         if (fwd_per_sm != g->net.fwd_per_sm) {
             g->net.fwd_per_sm = fwd_per_sm;
             g->net.bind(g->M.A, g->M.val.get(), g->val32.get(), g->st);
