@@ -300,7 +300,7 @@ def batch_form(args):
             "speedup_vs_sequential": seq_ms / ms if ms > 0 else None,
             "precision": "momentum BiCGSTAB FP64, p' CG FP32 recurrences + FP64 reliable updates, eps 1e-8",
             "autotuner": {"candidates_sms": list(DEFAULT_CAPS), "sm_cap": tune["sm_cap"],
-                          "model_makespan_ms": tune["makespan_ms"], "seconds": tune_s},
+                          "measured_makespan_ms": tune["measured_makespan_ms"], "seconds": tune_s},
             "mesh_generation_seconds": gen_s}
 
 

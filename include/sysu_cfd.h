@@ -229,7 +229,9 @@ const char *sysu_noalloc_last_error(void);
  * use -- the rows per warp of those kernels), then raises caps one step at a
  * time where that lowers the model makespan max(slowest case, SM-time / SMs),
  * while the caps add up to at most the GPU's SM count; the graph then issues
- * the longest cases first.  It resets the cases afterwards.  Cases are reached with sysu_batch_case (borrowed handles:
+ * the longest cases first; finally the model's caps scaled by 1/2, 1, 2, 4 and 8
+ * are each captured and replayed, and the fastest is kept (*makespan = its
+ * measured ms per batch iteration).  It resets the cases afterwards.  Cases are reached with sysu_batch_case (borrowed handles:
  * options, fields, solve statistics; do not destroy them).  Capture after every
  * option change.  sysu_batch_run_sequential times the cases one after another
  * with ordinary launches, for comparison. */

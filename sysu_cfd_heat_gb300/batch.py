@@ -54,7 +54,7 @@ class CaseBatch:
         dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
         check(lib().sysu_batch_tune(self._h, cand, len(candidates), caps, dp(alone), dp(full), C.byref(mk)))
         return {"sm_cap": list(caps), "ms_alone": alone.tolist(), "ms_full": full.tolist(),
-                "makespan_ms": mk.value}
+                "measured_makespan_ms": mk.value}
 
     def set_caps(self, caps: Sequence[int]):
         arr = (C.c_int * len(caps))(*caps)

@@ -134,11 +134,41 @@ TuneResult CaseBatch::tune(const std::vector<int> &candidates) {
         r.sm_cap[k] = cand[pick[k]];
         r.ms_alone[k] = t[k][pick[k]];
     }
-    set_caps(r.sm_cap);
     // the graph issues the longest cases first
     order_.resize(nc);
     for (int k = 0; k < nc; ++k) order_[k] = k;
     std::stable_sort(order_.begin(), order_.end(), [&](int a, int b) { return r.ms_alone[a] > r.ms_alone[b]; });
+    // the model ignores contention between branches: measure the real makespan of
+    // the greedy caps scaled by 1/2, 1, 2, 4 and 8 and keep the fastest
+    std::vector<int> best = r.sm_cap;
+    double best_ms = -1.0;
+    for (double fct : {1.0, 0.5, 2.0, 4.0, 8.0}) {
+        std::vector<int> caps(nc);
+        for (int k = 0; k < nc; ++k) {
+            double want = r.sm_cap[k] * fct;
+            int c = cand[0];
+            for (int x : cand)
+                if (x <= want + 1e-9) c = x;
+            caps[k] = std::min(c, S);
+        }
+        set_caps(caps);
+        capture();
+        replay(1);
+        double ms = replay(2) / 2.0;
+        for (int k = 0; k < nc; ++k) at(k).reset();
+        if (best_ms < 0.0 || ms < best_ms) {
+            best_ms = ms;
+            best = caps;
+        }
+    }
+    r.sm_cap = best;
+    r.measured_ms = best_ms;
+    for (int k = 0; k < nc; ++k) {
+        size_t j = 0;
+        while (j + 1 < cand.size() && cand[j] < best[k]) ++j;
+        r.ms_alone[k] = t[k][j];
+    }
+    set_caps(r.sm_cap);
     return r;
 }
 

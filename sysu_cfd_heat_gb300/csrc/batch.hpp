@@ -16,6 +16,7 @@ struct TuneResult {
     std::vector<double> ms_alone;   // one outer iteration at that cap, case alone
     std::vector<double> ms_full;    // one outer iteration with no cap, case alone
     double makespan_ms = 0.0;       // the model's makespan: max(slowest case, SM-time / SMs)
+    double measured_ms = 0.0;       // graph replay time of the chosen caps
 };
 
 class CaseBatch {
@@ -32,7 +33,8 @@ class CaseBatch {
     // Time one outer iteration of every case alone for each candidate SM cap,
     // then choose caps greedily against the makespan model max(slowest case,
     // SM-time / SMs) while the caps fit the GPU; the graph issues the longest
-    // cases first.  The cases are reset to their initial state afterwards.
+    // cases first.  The model's caps scaled by 1/2, 1, 2, 4 and 8 are then replayed
+    // and the fastest kept.  The cases are reset to their initial state afterwards.
     TuneResult tune(const std::vector<int> &candidates);
     void set_caps(const std::vector<int> &caps);
     // One eager iteration per case (allocates every buffer), a reset, then the

@@ -635,7 +635,7 @@ int sysu_batch_tune(sysu_batch *b, const int *cand, int ncand, int *caps, double
             if (ms_alone) ms_alone[k] = r.ms_alone[k];
             if (ms_full) ms_full[k] = r.ms_full[k];
         }
-        if (makespan) *makespan = r.makespan_ms;
+        if (makespan) *makespan = r.measured_ms;
         return SYSU_OK;
     });
 }
