@@ -304,6 +304,54 @@ def batch_form(args):
             "mesh_generation_seconds": gen_s}
 
 
+def c2_case_dir():
+    """Configuration 2: k-epsilon conjugate-heat-transfer channel, fluid 160 x 40 x 40 hexes
+    (2.0 x 0.5 x 0.5 m) bonded to a 160 x 8 x 40 solid slab (0.1 m), u_in = 1 m/s, 5 % inlet
+    turbulence with a 0.05 m mixing length, nu = 1e-5, k_s = 15 W/m/K."""
+    from sysu_cfd_heat_gb300 import meshgen as mg
+
+    d = os.path.join(tempfile.gettempdir(), "sysu_bench_c2_160x40x40")
+    p = os.path.join(d, "param.in")
+    if not os.path.exists(p):
+        tmp = d + ".tmp%d" % os.getpid()
+        mg.write_case(tmp, mg.cht_channel(160, 40, 8, 40), mg.cht_param("x", 100000, nu=1e-5, k_solid=15.0))
+        try:
+            os.rename(tmp, d)
+        except OSError:
+            pass
+    return p
+
+
+def c2_form(args):
+    """Configuration 2 on the GPU (k-epsilon CHT channel, 256,000 + 51,200 cells, volumetric
+    source 1e6 W/m^3 in the solid): outer iterations/s of the sequential form (the
+    reference's order, FP64) and of the batched scalar form (u, v, w as one 3-RHS BiCGSTAB;
+    k, eps and T as one three-matrix launch); both from the initial state."""
+    from sysu_cfd_heat_gb300.solver import NavierStokesSolver
+
+    p = c2_case_dir()
+    out = {}
+    steps = max(args.steps, 10)
+    with NavierStokesSolver(p, {"rtc": RTC, "solid_source": 1e6}) as s:
+        info = s.info()
+        for name, opts in (("sequential_fp64", {"scalars_batched": 0}), ("batched_scalars_fp64", {"scalars_batched": 1})):
+            for k, v in opts.items():
+                s.set_option(k, v)
+            s.reset()
+            s.iterate(args.warmup)
+            s.reset()
+            s.timer_start()
+            done = s.iterate(steps)
+            ms = s.timer_stop()
+            st = s.solve_stats()
+            out[name] = {"iters_per_s": done / (ms / 1000.0), "ms_per_step": ms / done,
+                         "k_eps_T_iters_last": [st["k"]["iters"][0], st["eps"]["iters"][0], st["T"]["iters"][0]],
+                         "max_residual_after": float(max(s.Residual))}
+        out["cells"] = {"fluid": info["Ncel"], "solid": info["solid_Ncel"]}
+        out["steps"] = steps
+    return out
+
+
 def learned_form(s, args, to8, field_err):
     """The learned + FP32 form: p' by flexible CG preconditioned by the message-passing
     network (FP32 recurrences, FP64 reliable updates, Jacobi fallback).  The network
@@ -531,6 +579,8 @@ def run_ours(args, r, w, lr):
     # the batched k, eps, T form needs a k-epsilon + energy case: not this cavity
     forms["batch_48_cavities"] = (batch_form(args) if args.workload == "c3" and not args.p_maxit
                                   and not args.p_mixed and not args.no_batch else None)
+    forms["c2_cht_channel"] = (c2_form(args) if args.workload == "c3" and not args.p_maxit
+                               and not args.p_mixed and not args.no_batch else None)
 
     out = {
         "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": w, "steps": args.steps,
