@@ -51,6 +51,7 @@ L2_BYTES = 129 * 1024 * 1024
 FP64_PEAK_TFLOPS = 1.25
 LEARN_ITERS = 10   # outer iterations that train the learned preconditioner
 LEARN_STEPS = 64   # Adam steps per training outer iteration
+LEARN_C5_ITERS = 40  # training outer iterations of the --learned-c5 run
 
 
 def rank_info():
@@ -352,6 +353,53 @@ def c2_form(args):
     return out
 
 
+def c5_learned_run(args):
+    """Configuration 5 (not part of the default run: --learned-c5): configuration 2 scaled
+    up, fluid 320 x 80 x 160 hexes (4,096,000 cells) + solid 320 x 16 x 160 (819,200).
+    The learned p' form trains during the first LEARN_C5_ITERS outer iterations, then the
+    p' system of the next outer iteration is solved to 1e-8 by flexible CG with the
+    network and, from the same state, by plain FP64 Jacobi-CG and the mixed FP32 CG."""
+    from sysu_cfd_heat_gb300 import meshgen as mg
+    from sysu_cfd_heat_gb300.solver import NavierStokesSolver
+
+    d = os.path.join(tempfile.gettempdir(), "sysu_bench_c5_320x80x160")
+    p = os.path.join(d, "param.in")
+    t0 = time.perf_counter()
+    if not os.path.exists(p):
+        tmp = d + ".tmp%d" % os.getpid()
+        mg.write_case(tmp, mg.cht_channel(320, 80, 16, 160), mg.cht_param("x", 100000, nu=1e-5, k_solid=15.0))
+        os.rename(tmp, d)
+    gen_s = time.perf_counter() - t0
+    out = {"mesh_generation_s": gen_s}
+    with NavierStokesSolver(p, {"rtc": RTC, "solid_source": 1e6, "timing": 1, "p.maxit": 100000}) as s:
+        info = s.info()
+        out["cells"] = {"fluid": info["Ncel"], "solid": info["solid_Ncel"]}
+        s.set_option("p.learned", 1)
+        s.set_option("p.learn_iters", LEARN_C5_ITERS)
+        s.set_option("p.learn_steps", LEARN_STEPS)
+        t0 = time.perf_counter()
+        s.iterate(LEARN_C5_ITERS)
+        s.sync()
+        out["training_s"] = time.perf_counter() - t0
+        state = {f: s.get(f) for f in ("U", "V", "W", "P", "RUFace", "TE", "ED", "VisTur", "T", "solid_T")}
+        res = {}
+        for name, opts in (("learned_fcg", {"p.learned": 1}), ("fp64_cg", {"p.learned": 0, "p.mixed": 0}),
+                           ("mixed_cg", {"p.learned": 0, "p.mixed": 1})):
+            for f, a in state.items():
+                s.set(f, a)
+            for k, v in opts.items():
+                s.set_option(k, v)
+            s.CalculateVelocity()
+            s.CalculatePressure()
+            s.check()
+            st = s.solve_stats()["p"]
+            res[name] = {"ms": s.timing()[0], "iters": st["iters"][0], "rel_residual": st["res"][0],
+                         "converged": st["status"][0] == 0}
+        out["p_solve_to_1e-8_after_training"] = res
+        out["training_outer_iterations"] = LEARN_C5_ITERS
+    return out
+
+
 def learned_form(s, args, to8, field_err):
     """The learned + FP32 form: p' by flexible CG preconditioned by the message-passing
     network (FP32 recurrences, FP64 reliable updates, Jacobi fallback).  The network
@@ -632,6 +680,8 @@ def main():
     ap.add_argument("--workload", default="c3", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 48-cavity batch form")
+    ap.add_argument("--learned-c5", action="store_true",
+                    help="only the configuration-5 learned-preconditioner run (4.9 M cells; minutes)")
     ap.add_argument("--cpu-budget", type=float, default=240.0)
     ap.add_argument("--ref-budget", type=float, default=150.0)
     ap.add_argument("--p-maxit", type=int, default=0,
@@ -645,7 +695,10 @@ def main():
         import torch.distributed as dist
 
         dist.init_process_group("gloo")
-    if args.impl == "reference":
+    if args.learned_c5:
+        if r == 0:
+            print(json.dumps({"learned_c5": c5_learned_run(args)}))
+    elif args.impl == "reference":
         run_reference(args, r, w)
     else:
         run_ours(args, r, w, lr)
