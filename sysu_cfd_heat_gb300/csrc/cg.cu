@@ -297,6 +297,52 @@ __device__ __forceinline__ void issue_matrix_tile(const Part &P, const SellView 
     }
 }
 
+// X phase over the CTA's rows: x += alpha p, r -= alpha q, z = M^-1 r and the
+// thread's partial r.r and r.z.  Two rows per thread per step with all ten
+// loads issued before the arithmetic (the buffers are distinct, so the loads of
+// a step need not wait for the stores of the previous one); the partial sums
+// take the rows in the same order as a one-row loop.
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+template <class T>
+__device__ __forceinline__ void x_phase(int R0, int R1, T alpha, const T *__restrict__ pv, const T *__restrict__ qv,
+                                        const T *__restrict__ dv, T *__restrict__ xv, T *__restrict__ rv,
+                                        T *__restrict__ zv, T &rr, T &rz) {
+    int i = R0 + (int)threadIdx.x;
+    for (; i + KBC < R1; i += 2 * KBC) {
+        const int j = i + KBC;
+        T p0 = pv[i], q0 = qv[i], x0 = xv[i], r0 = rv[i], d0 = dv[i];
+        T p1 = pv[j], q1 = qv[j], x1 = xv[j], r1 = rv[j], d1 = dv[j];
+        x0 = fma_t(alpha, p0, x0);
+        r0 = fma_t(-alpha, q0, r0);
+        x1 = fma_t(alpha, p1, x1);
+        r1 = fma_t(-alpha, q1, r1);
+        const T z0 = d0 * r0, z1 = d1 * r1;
+        xv[i] = x0;
+        rv[i] = r0;
+        zv[i] = z0;
+        xv[j] = x1;
+        rv[j] = r1;
+        zv[j] = z1;
+        rr = fma_t(r0, r0, rr);
+        rz = fma_t(r0, z0, rz);
+        rr = fma_t(r1, r1, rr);
+        rz = fma_t(r1, z1, rz);
+    }
+    if (i < R1) {
+        T pi = pv[i], qi = qv[i], xi = xv[i], ri = rv[i], di = dv[i];
+        xi = fma_t(alpha, pi, xi);
+        ri = fma_t(-alpha, qi, ri);
+        const T zi = di * ri;
+        xv[i] = xi;
+        rv[i] = ri;
+        zv[i] = zi;
+        rr = fma_t(ri, ri, rr);
+        rz = fma_t(ri, zi, rz);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // FP64
 __global__ void __launch_bounds__(KBC, 1) k_cg_pipe(CgPipeArgs a) {
@@ -356,17 +402,23 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_pipe(CgPipeArgs a) {
             producer_tiles(R, base + nt, issue, err);
         } else {
             for (int t = 0; t < nt; ++t) {
-                if (!acquire(R, err)) break;
+                // the row's own loads do not depend on the tile: issue them before its wait
                 int s0, s1, r0, nr;
                 P.tile(t, s0, s1, r0, nr);
-                if (tid < nr) {
-                    const int i = r0 + tid;
-                    double pi = 0.0, qi = 0.0;
+                const bool act = tid < nr;
+                const int i = r0 + tid;
+                const int s = s0 + (tid >> 5);
+                double pi = 0.0, qi = 0.0;
+                int es = 0, w = 0;
+                if (act) {
                     if (it > 1) { pi = a.p[i]; qi = a.q[i]; }
-                    int s = s0 + (tid >> 5);
+                    es = __ldg(a.A.sl_ptr + s);
+                    w = __ldg(a.A.sl_w + s);
+                }
+                if (!acquire(R, err)) break;
+                if (act) {
                     int e0 = tile_entry(P, a.A.sl_ptr, t), e1 = tile_entry(P, a.A.sl_ptr, t + 1);
-                    int es = __ldg(a.A.sl_ptr + s) - e0 + (tid & 31);
-                    int w = __ldg(a.A.sl_w + s);
+                    es = es - e0 + (tid & 31);
                     const double *vs;
                     const int *cs;
                     if (a.plan.direct) {
@@ -400,18 +452,7 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_pipe(CgPipeArgs a) {
         // X: the producer first queues the next S phase's tiles
         if (prod) producer_tiles(R, 0, issue, err);
         double v2[2] = {0.0, 0.0};
-#pragma unroll 4
-        for (int i = R0 + tid; i < R1; i += KBC) {
-            double pi = a.p[i], qi = a.q[i], xi = a.x[i], ri = a.r[i], di = a.dinv[i];
-            xi = fma(alpha, pi, xi);
-            ri = fma(-alpha, qi, ri);
-            double zi = di * ri;
-            a.x[i] = xi;
-            a.r[i] = ri;
-            a.z[i] = zi;
-            v2[0] = fma(ri, ri, v2[0]);
-            v2[1] = fma(ri, zi, v2[1]);
-        }
+        x_phase<double>(R0, R1, alpha, a.p, a.q, a.dinv, a.x, a.r, a.z, v2[0], v2[1]);
         if (!grid_sum_t0<2>(v2, rc, a.gb, err) || fail_flag()) break;
         stamp(a.ts, it, 2);
         if (tid == 0) {
@@ -503,17 +544,22 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_mixed_pipe(CgPipeArgs a) {
             producer_tiles(R, base + nt, issue, err);
         } else {
             for (int t = 0; t < nt; ++t) {
-                if (!acquire(R, err)) break;
                 int s0, s1, r0, nr;
                 P.tile(t, s0, s1, r0, nr);
-                if (tid < nr) {
-                    const int i = r0 + tid;
-                    float pi = 0.f, qi = 0.f;
+                const bool act = tid < nr;
+                const int i = r0 + tid;
+                const int s = s0 + (tid >> 5);
+                float pi = 0.f, qi = 0.f;
+                int es = 0, w = 0;
+                if (act) {
                     if (total > 1) { pi = a.p32[i]; qi = a.q32[i]; }
-                    int s = s0 + (tid >> 5);
+                    es = __ldg(a.A.sl_ptr + s);
+                    w = __ldg(a.A.sl_w + s);
+                }
+                if (!acquire(R, err)) break;
+                if (act) {
                     int e0 = tile_entry(P, a.A.sl_ptr, t), e1 = tile_entry(P, a.A.sl_ptr, t + 1);
-                    int es = __ldg(a.A.sl_ptr + s) - e0 + (tid & 31);
-                    int w = __ldg(a.A.sl_w + s);
+                    es = es - e0 + (tid & 31);
                     const float *vs;
                     const int *cs;
                     if (a.plan.direct) {
@@ -547,18 +593,7 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_mixed_pipe(CgPipeArgs a) {
         if (g_bc[3] != 0.0) { status = DEV_BREAKDOWN; break; }
         if (prod) producer_tiles(R, 0, issue, err);
         float h0 = 0.f, h1 = 0.f;
-#pragma unroll 4
-        for (int i = R0 + tid; i < R1; i += KBC) {
-            float pi = a.p32[i], qi = a.q32[i], ei = a.e32[i], ri = a.r32[i], di = dinv[i];
-            ei = fmaf(alpha, pi, ei);
-            ri = fmaf(-alpha, qi, ri);
-            float zi = di * ri;
-            a.e32[i] = ei;
-            a.r32[i] = ri;
-            a.z32[i] = zi;
-            h0 = fmaf(ri, ri, h0);
-            h1 = fmaf(ri, zi, h1);
-        }
+        x_phase<float>(R0, R1, alpha, a.p32, a.q32, dinv, a.e32, a.r32, a.z32, h0, h1);
         double w2[2] = {(double)h0, (double)h1};
         if (!grid_sum_t0<2>(w2, rc, a.gb, err) || fail_flag()) break;
         stamp(a.ts, total, 2);

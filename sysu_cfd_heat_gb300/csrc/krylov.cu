@@ -13,6 +13,15 @@
 // recurrences as the CPU oracle's LASPack restatement): BiCGSTAB, right
 // preconditioned, early exit on ||s||, breakdown on rho = 0.  M = D / omega
 // (Jacobi).  Stopping test ||r||_2 / ||b||_2 < eps.
+//
+// GB300 runs FP64 at 1/64 of the FP32 rate, so the FP64 instruction count per
+// row, not only the bytes, bounds these kernels.  The Jacobi scaling of the two
+// products A M^-1 p and A M^-1 s is folded into a column-scaled copy of the
+// matrix, a_ij / m_jj, built once per solve (one FMA per entry and right-hand
+// side instead of a multiply and an FMA, and no gather of the diagonal), and
+// x += alpha M^-1 p + omega M^-1 s is taken as x += M^-1 (alpha p + omega s).
+// Both are the same iterates in exact arithmetic; the rounding differs from the
+// unfolded form by a unit in the last place per product.
 #include "krylov_dev.cuh"
 
 #include <algorithm>
@@ -119,13 +128,14 @@ void SellDev::upload(const SellPattern &p, cudaStream_t s) {
 
 namespace {
 
-// y_c = A (dinv .* x_c) for NR right-hand sides, skipping inactive ones.
-// MULTI: right-hand side c has its own matrix values vals[c] (same pattern) and
-// its own diagonal inverse dinv + c n; the column indices are read once.
+// y_c = A (dinv .* x_c) for NR right-hand sides, skipping inactive ones, from
+// the column-scaled values sv[e] = a_e dinv[col e].  MULTI: right-hand side c
+// has its own scaled values svals[c] (same pattern); the column indices are
+// read once.
 template <int NR, bool MULTI>
-__device__ __forceinline__ void row_dot_scaled(const SellView &A, const double *const *vals, int i,
-                                               const double *__restrict__ dinv, const double *__restrict__ x, int n,
-                                               const bool (&act)[3], double (&y)[NR]) {
+__device__ __forceinline__ void row_dot_scaled(const SellView &A, const double *const *svals, int i,
+                                               const double *__restrict__ x, int n, const bool (&act)[3],
+                                               double (&y)[NR]) {
     int s = i >> 5;
     int e = A.sl_ptr[s] + (i & 31);
     int w = A.sl_w[s];
@@ -136,17 +146,23 @@ __device__ __forceinline__ void row_dot_scaled(const SellView &A, const double *
         if (MULTI) {
 #pragma unroll
             for (int c = 0; c < NR; ++c)
-                if (act[c]) y[c] += vals[c][e] * (dinv[(size_t)c * n + j] * x[(size_t)c * n + j]);
+                if (act[c]) y[c] = fma(svals[c][e], x[(size_t)c * n + j], y[c]);
         } else {
-            double a = A.val[e];
-            double d = dinv[j];
+            double a = svals[0][e];
 #pragma unroll
             for (int c = 0; c < NR; ++c)
-                if (act[c]) y[c] += a * (d * x[(size_t)c * n + j]);
+                if (act[c]) y[c] = fma(a, x[(size_t)c * n + j], y[c]);
         }
     }
 }
 
+// sv[e] = val[e] dinv[col e] over all stored entries (padding entries hold 0
+// and their own row as the column).
+__global__ void k_scale_cols(long nnz, const int *__restrict__ col, const double *__restrict__ val,
+                             const double *__restrict__ dinv, double *__restrict__ sv) {
+    long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < nnz) sv[e] = val[e] * dinv[col[e]];
+}
 
 __global__ void k_jacobi_apply(SellView A, double omega, const double *c, double *y) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -271,6 +287,7 @@ __global__ void k_to_fp32(long n, const double *src, float *dst) {
 struct BicgArgs {
     SellView A;
     const double *vals[3];  // per right-hand-side matrix values (MULTI)
+    const double *svals[3]; // the same, column-scaled by the Jacobi diagonal inverse
     const double *b[3];
     double *x[3];
     double *r, *rt, *p, *v, *s, *t;
@@ -282,19 +299,28 @@ struct BicgArgs {
     double eps;
 };
 
+// Scalar state of a BiCGSTAB solve.  Thread 0 of every block derives it from
+// the global sums (which every block adds up in the same fixed order, so all
+// blocks hold identical copies) and the block reads it from shared memory:
+// the square roots and divisions run once per block instead of in every thread,
+// and the vector loops keep only the few scalars they use in registers.
+struct BicgState {
+    double bnorm[3], res[3], rho[3], rho_prev[3], alpha[3], omg[3], beta[3], snorm[3];
+    int it[3], status[3], done[3], act[3], early[3], act2[3];
+    int any;
+};
+
 template <int NR, bool MULTI>
-__global__ void __launch_bounds__(KB) k_bicgstab(BicgArgs a) {
+__global__ void __launch_bounds__(KB, 4) k_bicgstab(BicgArgs a) {
     const int n = a.A.n;
     const int T = gridDim.x * KB;
     const int t0 = blockIdx.x * KB + threadIdx.x;
+    const bool lead = threadIdx.x == 0;
     int *err = &a.info->err;
     RedCtx rc{a.partials, (int)gridDim.x, 0};
     const double *__restrict__ dinv = a.dinv;
     const size_t N = (size_t)n;
-
-    double bnorm[NR], res[NR], rho[NR], rho_prev[NR], alpha[NR], omg[NR], beta[NR], snorm[NR];
-    int it[NR], status[NR];
-    bool done[NR], act[3] = {false, false, false}, early[3] = {false, false, false};
+    __shared__ BicgState S;
     {
         double v[2 * NR];
 #pragma unroll
@@ -312,40 +338,60 @@ __global__ void __launch_bounds__(KB) k_bicgstab(BicgArgs a) {
                 v[NR + c] += ri * ri;
             }
         }
-        if (!grid_reduce<2 * NR>(v, rc, a.gb, err)) return;
-#pragma unroll
-        for (int c = 0; c < NR; ++c) {
-            bnorm[c] = sqrt(v[c]);
-            if (bnorm[c] == 0.0) bnorm[c] = 1.0;
-            res[c] = sqrt(v[NR + c]) / bnorm[c];
-            rho[c] = v[NR + c];
-            rho_prev[c] = alpha[c] = omg[c] = 1.0;
-            it[c] = 0;
-            status[c] = DEV_OK;
-            done[c] = false;
-        }
-    }
-    for (;;) {
-        bool any = false;
-#pragma unroll
-        for (int c = 0; c < NR; ++c) {
-            act[c] = !done[c] && !(res[c] < a.eps) && it[c] < a.maxit;
-            if (act[c] && !isfinite(res[c])) { done[c] = true; status[c] = DEV_NONFINITE; act[c] = false; }
-            if (act[c] && rho[c] == 0.0) { done[c] = true; status[c] = DEV_BREAKDOWN; act[c] = false; }
-            if (act[c]) {
-                ++it[c];
-                any = true;
-                beta[c] = (it[c] == 1) ? 0.0 : (rho[c] / rho_prev[c]) * (alpha[c] / omg[c]);
-            }
-        }
-        if (!any) break;
-        // p = r + beta (p - omega v)
-        for (int i = t0; i < n; i += T) {
+        if (!grid_reduce_t0<2 * NR>(v, rc, a.gb, err)) return;
+        if (lead) {
 #pragma unroll
             for (int c = 0; c < NR; ++c) {
-                if (!act[c]) continue;
-                size_t k = c * N + i;
-                a.p[k] = (it[c] == 1) ? a.r[k] : a.r[k] + beta[c] * (a.p[k] - omg[c] * a.v[k]);
+                double bn = sqrt(v[c]);
+                if (bn == 0.0) bn = 1.0;
+                S.bnorm[c] = bn;
+                S.res[c] = sqrt(v[NR + c]) / bn;
+                S.rho[c] = v[NR + c];
+                S.rho_prev[c] = S.alpha[c] = S.omg[c] = 1.0;
+                S.it[c] = 0;
+                S.status[c] = DEV_OK;
+                S.done[c] = 0;
+            }
+        }
+    }
+    bool act[3] = {false, false, false};
+    for (;;) {
+        if (lead) {
+            int any = 0;
+#pragma unroll
+            for (int c = 0; c < NR; ++c) {
+                bool ac = !S.done[c] && !(S.res[c] < a.eps) && S.it[c] < a.maxit;
+                if (ac && !isfinite(S.res[c])) { S.done[c] = 1; S.status[c] = DEV_NONFINITE; ac = false; }
+                if (ac && S.rho[c] == 0.0) { S.done[c] = 1; S.status[c] = DEV_BREAKDOWN; ac = false; }
+                if (ac) {
+                    ++S.it[c];
+                    any = 1;
+                    S.beta[c] = (S.it[c] == 1) ? 0.0 : (S.rho[c] / S.rho_prev[c]) * (S.alpha[c] / S.omg[c]);
+                }
+                S.act[c] = ac;
+            }
+            S.any = any;
+        }
+        __syncthreads();
+        if (!S.any) break;
+        // p = r + beta (p - omega v)
+        {
+            double beta[NR], omg[NR];
+            bool first[NR];
+#pragma unroll
+            for (int c = 0; c < NR; ++c) {
+                act[c] = S.act[c] != 0;
+                beta[c] = S.beta[c];
+                omg[c] = S.omg[c];
+                first[c] = S.it[c] == 1;
+            }
+            for (int i = t0; i < n; i += T) {
+#pragma unroll
+                for (int c = 0; c < NR; ++c) {
+                    if (!act[c]) continue;
+                    size_t k = c * N + i;
+                    a.p[k] = first[c] ? a.r[k] : a.r[k] + beta[c] * (a.p[k] - omg[c] * a.v[k]);
+                }
             }
         }
         if (!grid_sync(a.gb, err)) return;
@@ -356,7 +402,7 @@ __global__ void __launch_bounds__(KB) k_bicgstab(BicgArgs a) {
             for (int c = 0; c < NR; ++c) red[c] = 0.0;
             for (int i = t0; i < n; i += T) {
                 double y[NR];
-                row_dot_scaled<NR, MULTI>(a.A, a.vals, i, dinv, a.p, n, act, y);
+                row_dot_scaled<NR, MULTI>(a.A, a.svals, i, a.p, n, act, y);
 #pragma unroll
                 for (int c = 0; c < NR; ++c) {
                     if (!act[c]) continue;
@@ -364,19 +410,26 @@ __global__ void __launch_bounds__(KB) k_bicgstab(BicgArgs a) {
                     red[c] += a.rt[c * N + i] * y[c];
                 }
             }
-            if (!grid_reduce<NR>(red, rc, a.gb, err)) return;
+            if (!grid_reduce_t0<NR>(red, rc, a.gb, err)) return;
+            if (lead) {
 #pragma unroll
-            for (int c = 0; c < NR; ++c) {
-                if (!act[c]) continue;
-                if (red[c] == 0.0) { done[c] = true; status[c] = DEV_BREAKDOWN; act[c] = false; continue; }
-                alpha[c] = rho[c] / red[c];
+                for (int c = 0; c < NR; ++c) {
+                    if (!S.act[c]) continue;
+                    if (red[c] == 0.0) { S.done[c] = 1; S.status[c] = DEV_BREAKDOWN; S.act[c] = 0; continue; }
+                    S.alpha[c] = S.rho[c] / red[c];
+                }
             }
+            __syncthreads();
         }
         // s = r - alpha v ; ||s||
         {
-            double red[NR];
+            double red[NR], alpha[NR];
 #pragma unroll
-            for (int c = 0; c < NR; ++c) red[c] = 0.0;
+            for (int c = 0; c < NR; ++c) {
+                red[c] = 0.0;
+                act[c] = S.act[c] != 0;
+                alpha[c] = S.alpha[c];
+            }
             for (int i = t0; i < n; i += T) {
 #pragma unroll
                 for (int c = 0; c < NR; ++c) {
@@ -387,26 +440,31 @@ __global__ void __launch_bounds__(KB) k_bicgstab(BicgArgs a) {
                     red[c] += si * si;
                 }
             }
-            if (!grid_reduce<NR>(red, rc, a.gb, err)) return;
+            if (!grid_reduce_t0<NR>(red, rc, a.gb, err)) return;
+            if (lead) {
 #pragma unroll
-            for (int c = 0; c < NR; ++c) {
-                early[c] = false;
-                if (!act[c]) continue;
-                snorm[c] = sqrt(red[c]) / bnorm[c];
-                early[c] = snorm[c] < a.eps;
+                for (int c = 0; c < NR; ++c) {
+                    S.early[c] = 0;
+                    S.act2[c] = 0;
+                    if (!S.act[c]) continue;
+                    S.snorm[c] = sqrt(red[c]) / S.bnorm[c];
+                    S.early[c] = S.snorm[c] < a.eps;
+                    S.act2[c] = !S.early[c];
+                }
             }
+            __syncthreads();
         }
         // t = A M^-1 s ; t.s, t.t
         {
             bool act2[3] = {false, false, false};
 #pragma unroll
-            for (int c = 0; c < NR; ++c) act2[c] = act[c] && !early[c];
+            for (int c = 0; c < NR; ++c) act2[c] = S.act2[c] != 0;
             double red[2 * NR];
 #pragma unroll
             for (int c = 0; c < 2 * NR; ++c) red[c] = 0.0;
             for (int i = t0; i < n; i += T) {
                 double y[NR];
-                row_dot_scaled<NR, MULTI>(a.A, a.vals, i, dinv, a.s, n, act2, y);
+                row_dot_scaled<NR, MULTI>(a.A, a.svals, i, a.s, n, act2, y);
 #pragma unroll
                 for (int c = 0; c < NR; ++c) {
                     if (!act2[c]) continue;
@@ -416,59 +474,69 @@ __global__ void __launch_bounds__(KB) k_bicgstab(BicgArgs a) {
                     red[NR + c] += y[c] * y[c];
                 }
             }
-            if (!grid_reduce<2 * NR>(red, rc, a.gb, err)) return;
+            if (!grid_reduce_t0<2 * NR>(red, rc, a.gb, err)) return;
+            if (lead) {
 #pragma unroll
-            for (int c = 0; c < NR; ++c)
-                if (act2[c]) omg[c] = red[NR + c] != 0.0 ? red[c] / red[NR + c] : 0.0;
+                for (int c = 0; c < NR; ++c)
+                    if (S.act2[c]) S.omg[c] = red[NR + c] != 0.0 ? red[c] / red[NR + c] : 0.0;
+            }
+            __syncthreads();
         }
-        // x += alpha M^-1 p + omega M^-1 s ; r = s - omega t
+        // x += M^-1 (alpha p + omega s) ; r = s - omega t
         {
-            double red[2 * NR];
+            double red[2 * NR], alpha[NR], omg[NR];
+            bool early[NR];
 #pragma unroll
-            for (int c = 0; c < 2 * NR; ++c) red[c] = 0.0;
+            for (int c = 0; c < NR; ++c) {
+                red[c] = red[NR + c] = 0.0;
+                alpha[c] = S.alpha[c];
+                omg[c] = S.omg[c];
+                early[c] = S.early[c] != 0;
+            }
             for (int i = t0; i < n; i += T) {
 #pragma unroll
                 for (int c = 0; c < NR; ++c) {
                     if (!act[c]) continue;
                     size_t k = c * N + i;
                     double di = MULTI ? dinv[k] : dinv[i];
-                    double ph = di * a.p[k];
                     if (early[c]) {
-                        a.x[c][i] += alpha[c] * ph;
+                        a.x[c][i] += alpha[c] * (di * a.p[k]);
                     } else {
-                        double sh = di * a.s[k];
-                        a.x[c][i] += alpha[c] * ph + omg[c] * sh;
-                        double ri = a.s[k] - omg[c] * a.t[k];
+                        double si = a.s[k];
+                        a.x[c][i] = fma(di, fma(alpha[c], a.p[k], omg[c] * si), a.x[c][i]);
+                        double ri = fma(-omg[c], a.t[k], si);
                         a.r[k] = ri;
                         red[c] += ri * ri;
                         red[NR + c] += a.rt[k] * ri;
                     }
                 }
             }
-            if (!grid_reduce<2 * NR>(red, rc, a.gb, err)) return;
+            if (!grid_reduce_t0<2 * NR>(red, rc, a.gb, err)) return;
+            if (lead) {
 #pragma unroll
-            for (int c = 0; c < NR; ++c) {
-                if (!act[c]) continue;
-                if (early[c]) {
-                    res[c] = snorm[c];
-                    done[c] = true;
-                } else {
-                    res[c] = sqrt(red[c]) / bnorm[c];
-                    rho_prev[c] = rho[c];
-                    rho[c] = red[NR + c];
-                    if (omg[c] == 0.0 && !(res[c] < a.eps)) { done[c] = true; status[c] = DEV_BREAKDOWN; }
+                for (int c = 0; c < NR; ++c) {
+                    if (!S.act[c]) continue;
+                    if (S.early[c]) {
+                        S.res[c] = S.snorm[c];
+                        S.done[c] = 1;
+                    } else {
+                        S.res[c] = sqrt(red[c]) / S.bnorm[c];
+                        S.rho_prev[c] = S.rho[c];
+                        S.rho[c] = red[NR + c];
+                        if (S.omg[c] == 0.0 && !(S.res[c] < a.eps)) { S.done[c] = 1; S.status[c] = DEV_BREAKDOWN; }
+                    }
                 }
             }
         }
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (blockIdx.x == 0 && lead) {
 #pragma unroll
         for (int c = 0; c < NR; ++c) {
-            int st = status[c];
-            if (st == DEV_OK && !(res[c] < a.eps)) st = isfinite(res[c]) ? DEV_MAXITER : DEV_NONFINITE;
+            int st = S.status[c];
+            if (st == DEV_OK && !(S.res[c] < a.eps)) st = isfinite(S.res[c]) ? DEV_MAXITER : DEV_NONFINITE;
             a.info->status[c] = st;
-            a.info->iters[c] = it[c];
-            a.info->res[c] = res[c];
+            a.info->iters[c] = S.it[c];
+            a.info->res[c] = S.res[c];
         }
     }
 }
@@ -572,15 +640,24 @@ static void bicg_launch(const SellDev &A, const double *const *vals, bool multi,
     int maxb = bicg_max_blocks(nrhs, multi);
     if (w.sm_cap > 0) maxb = std::min(maxb, w.sm_cap * std::max(1, maxb / num_sms()));
     w.ensure(n, nrhs == 1 ? 1 : 3, bicg_max_blocks(-1, false), st);
-    for (int c = 0; c < (multi ? nrhs : 1); ++c) {
+    const int nmat = multi ? nrhs : 1;
+    if (w.sval.size() < (size_t)A.nnz * nmat) w.sval.alloc((size_t)A.nnz * nmat);
+    for (int c = 0; c < nmat; ++c) {
         SellView Vc = view(A, vals[c]);
-        { k_jacobi_dinv<<<(n + KB - 1) / KB, KB, 0, st>>>(Vc, o.omega, o.jacobi ? 1 : 0, w.dinv.get() + (size_t)c * n); ++::sysu::g_launches; }
+        double *dc = w.dinv.get() + (size_t)c * n;
+        { k_jacobi_dinv<<<(n + KB - 1) / KB, KB, 0, st>>>(Vc, o.omega, o.jacobi ? 1 : 0, dc); ++::sysu::g_launches; }
+        if (A.nnz > 0) {
+            k_scale_cols<<<(unsigned)((A.nnz + KB - 1) / KB), KB, 0, st>>>(A.nnz, A.col.get(), vals[c], dc,
+                                                                          w.sval.get() + (size_t)c * A.nnz);
+            ++::sysu::g_launches;
+        }
     }
     SYSU_CUDA(cudaMemsetAsync(info, 0, sizeof(SolveInfo), st));
     BicgArgs a{};
     a.A = view(A, vals[0]);
     for (int c = 0; c < 3; ++c) {
         a.vals[c] = vals[multi ? std::min(c, nrhs - 1) : 0];
+        a.svals[c] = w.sval.get() + (size_t)(multi ? std::min(c, nrhs - 1) : 0) * A.nnz;
         a.b[c] = b[std::min(c, nrhs - 1)];
         a.x[c] = x[std::min(c, nrhs - 1)];
     }

@@ -74,6 +74,7 @@ struct SolveInfo {
 struct KrylovWork {
     int n = 0, nrhs = 0, max_blocks = 0;
     DevBuf<double> r, rt, p, v, s, t, dinv, partials;
+    DevBuf<double> sval;  // BiCGSTAB: matrix values scaled by the Jacobi diagonal inverse of their column
     DevBuf<float> r32, z32, p32, q32, e32, dinv32;  // mixed-precision inner solve
     DevBuf<double> gV, gZ, gW, ilu;                  // GMRES basis, preconditioned basis, ILU(0) factors
     DevBuf<long long> gpart;                         // exact multi-value partial sums
