@@ -6,9 +6,9 @@
 // iteration cap, and the iterates of Jacobi-PCG (Barrett et al., "Templates",
 // Fig. 2.5) in exact arithmetic.
 //
-// One solve = one cooperative launch of a persistent kernel, one 1024-thread
-// CTA per SM.  Each CTA owns a contiguous range of slices (32-row groups of
-// the SELL matrix).  An iteration is two phases, each closed by an exact grid
+// One solve = one cooperative launch of a persistent kernel, one CTA per SM.
+// Each CTA owns a contiguous range of slices (32-row groups of the SELL
+// matrix).  An iteration is two phases, each closed by an exact grid
 // reduction (exact_sum.cuh):
 //   S  w = A z, p = z + beta p, q = w + beta q, p.q      (gathers z)
 //   X  x += alpha p, r -= alpha q, z = M^-1 r, r.r, r.z
@@ -16,12 +16,15 @@
 // q = A p by the recurrence A (z + beta p) = A z + beta A p, so no separate grid
 // barrier is needed between the direction update and the product.
 //
-// S streams the matrix: tiles of TS = 31 slices (992 rows, one per consumer
-// thread) are moved into shared memory by bulk asynchronous copies
-// (cp.async.bulk, the TMA engine's 1-D form) through a ring of D slots.  Warp 31
-// is the producer: it issues a tile as soon as its slot has been released by
-// the 31 consumer warps, and queues the next iteration's first tiles at the
-// start of X, so S starts on landed data.  The matrix is copied with an L2
+// S streams the matrix: tiles of one slice per consumer warp (one row per
+// consumer thread) are moved into shared memory by bulk asynchronous copies
+// (cp.async.bulk, the TMA engine's 1-D form) through a ring of D slots.  The
+// last warp is the producer: it issues a tile as soon as its slot has been
+// released by all consumer warps, and queues the next iteration's first tiles
+// at the start of X, so S starts on landed data.  In the FP64 kernel the
+// consumers work one tile ahead (the next tile's gathers in flight during the
+// current tile's FMAs: GB300's FP64 pipe, 1/64 of the FP32 rate, would
+// otherwise idle while every warp waits on its gathers at once).  The matrix is copied with an L2
 // evict-first policy so that the Krylov vectors stay in L2.  X runs over the
 // CTA's rows with plain coalesced loads (all 32 warps, no per-tile
 // synchronisation).
@@ -42,14 +45,18 @@
 namespace sysu {
 namespace {
 
-constexpr int CG_CONSUMERS = KBC / 32 - 1;          // consumer warps; warp 31 produces
-constexpr int CG_PRODUCER = KBC / 32 - 1;
-constexpr int CG_MAX_TS = CG_CONSUMERS;             // 31 slices = 992 rows per tile
+// Threads per CTA (measured on the 2M-cell tet p' system: the FP64 kernel is
+// fastest with 16 warps, 128 registers a thread and 480-row tiles, the FP32
+// one with 24 warps and 736-row tiles).  The last warp produces, the others
+// consume; a tile has one slice (32 rows) per consumer warp.
+constexpr int CGT64 = 512;
+constexpr int CGT32 = 768;
 constexpr unsigned CG_SMEM_BUDGET = 200 * 1024;     // dynamic shared memory for the ring
+constexpr int CG_WR = 6;                            // gathers per row held in registers one tile ahead (FP64)
 
 // Launch plan: slices per tile, ring depth, slot size.
 struct CgPlan {
-    int ts = CG_MAX_TS;
+    int ts = 1;
     int depth = 2;
     unsigned slot = 0;     // bytes per slot (multiple of 128)
     int direct = 0;        // 1: tiles read val/col from global memory (rows too long for a slot)
@@ -133,7 +140,8 @@ __device__ __forceinline__ int tile_entry(const Part &P, const int *sl_ptr, int 
     return t <= CG_TILE_TABLE ? g_tile_e[t] : __ldg(sl_ptr + min(P.sb + t * P.ts, P.se));
 }
 
-__device__ __forceinline__ bool is_producer() { return (threadIdx.x >> 5) == CG_PRODUCER; }
+__device__ __forceinline__ int cg_consumers() { return (int)(blockDim.x >> 5) - 1; }
+__device__ __forceinline__ bool is_producer() { return (int)(threadIdx.x >> 5) == cg_consumers(); }
 
 __device__ __forceinline__ unsigned char *cslot_ptr(const Ring &R) { return g_slots + (size_t)R.cslot * R.slot; }
 
@@ -200,6 +208,20 @@ __device__ __forceinline__ bool acquire(const Ring &R, int *err) {
     return ok;
 }
 
+// As acquire/release, at an explicit slot (consumers that hold two tiles).
+__device__ __forceinline__ bool acquire_at(int slot, unsigned par, int *err) {
+    bool ok = !__any_sync(FULL_MASK, fail_flag() != 0);
+    if (ok) ok = mbar_wait(&g_full[slot], par);
+    ok = __all_sync(FULL_MASK, ok);
+    if (!ok && (threadIdx.x & 31) == 0) set_fail(err);
+    return ok;
+}
+__device__ __forceinline__ void release_at(int slot) {
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0)
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&g_empty[slot])) : "memory");
+}
+
 // Consumer warps, after their last read of the slot: release it.
 __device__ __forceinline__ void release(Ring &R) {
     __syncwarp();
@@ -212,7 +234,7 @@ __device__ __forceinline__ void release(Ring &R) {
 // slot (a slot's copies complete in order), so none is in flight when the CTA
 // leaves, whether or not its tile was consumed.
 __device__ __forceinline__ void drain(const Ring &R) {
-    if (threadIdx.x != CG_PRODUCER * 32) return;
+    if ((int)threadIdx.x != cg_consumers() * 32) return;
     long long issued = g_prod.issued;
     for (int s = 0; s < R.depth; ++s) {
         long long last = issued - 1 - ((issued - 1 - s) % R.depth + R.depth) % R.depth;
@@ -239,7 +261,7 @@ __device__ __forceinline__ void ring_init(Ring &R, const CgPlan &pl, const Part 
         Q.primed = 0;
         for (int k = 0; k < R.depth; ++k) {
             mbar_init(&g_full[k], 1);
-            mbar_init(&g_empty[k], CG_CONSUMERS);
+            mbar_init(&g_empty[k], (unsigned)cg_consumers());
         }
         g_fail = 0;
         mbar_init_fence();
@@ -305,13 +327,13 @@ __device__ __forceinline__ void issue_matrix_tile(const Part &P, const SellView 
 __device__ __forceinline__ double fma_t(double a, double b, double c) { return __fma_rn(a, b, c); }
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
-template <class T>
+template <class T, int NT>
 __device__ __forceinline__ void x_phase(int R0, int R1, T alpha, const T *__restrict__ pv, const T *__restrict__ qv,
                                         const T *__restrict__ dv, T *__restrict__ xv, T *__restrict__ rv,
                                         T *__restrict__ zv, T &rr, T &rz) {
     int i = R0 + (int)threadIdx.x;
-    for (; i + KBC < R1; i += 2 * KBC) {
-        const int j = i + KBC;
+    for (; i + NT < R1; i += 2 * NT) {
+        const int j = i + NT;
         T p0 = pv[i], q0 = qv[i], x0 = xv[i], r0 = rv[i], d0 = dv[i];
         T p1 = pv[j], q1 = qv[j], x1 = xv[j], r1 = rv[j], d1 = dv[j];
         x0 = fma_t(alpha, p0, x0);
@@ -345,7 +367,7 @@ __device__ __forceinline__ void x_phase(int R0, int R1, T alpha, const T *__rest
 
 // ---------------------------------------------------------------------------
 // FP64
-__global__ void __launch_bounds__(KBC, 1) k_cg_pipe(CgPipeArgs a) {
+__global__ void __launch_bounds__(CGT64, 1) k_cg_pipe(CgPipeArgs a) {
     const int n = a.A.n;
     const int tid = threadIdx.x;
     const bool prod = is_producer();
@@ -363,7 +385,7 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_pipe(CgPipeArgs a) {
 
     // r = b - A x, z = M^-1 r; ||b||^2, ||r||^2, r.z
     double v3[3] = {0.0, 0.0, 0.0};
-    for (int i = R0 + tid; i < R1; i += KBC) {
+    for (int i = R0 + tid; i < R1; i += CGT64) {
         double bi = a.b[i];
         double ri = bi - row_dot(a.A, i, a.x);
         double zi = a.dinv[i] * ri;
@@ -401,43 +423,87 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_pipe(CgPipeArgs a) {
         if (prod) {
             producer_tiles(R, base + nt, issue, err);
         } else {
-            for (int t = 0; t < nt; ++t) {
-                // the row's own loads do not depend on the tile: issue them before its wait
+            // One tile ahead: tile t+1's row loads and its first CG_WR gathers are
+            // in flight while tile t's FMAs run, so the FP64 work of one tile
+            // overlaps the memory latency of the next.  A warp holds two slots.
+            int aslot = R.cslot;  // acquire cursor
+            unsigned apar = R.cpar;
+            int rslot = R.cslot;  // release cursor
+            double zc[CG_WR], zn[CG_WR];
+            double pc = 0.0, qc = 0.0, pn = 0.0, qn = 0.0;
+            int ec = 0, wc = 0, en = 0, wn = 0;
+            // row loads, tile wait, column reads and gathers of tile t
+            auto fetch = [&](int t, double(&zz)[CG_WR], double &pp, double &qq, int &ee, int &ww) -> bool {
                 int s0, s1, r0, nr;
                 P.tile(t, s0, s1, r0, nr);
                 const bool act = tid < nr;
                 const int i = r0 + tid;
                 const int s = s0 + (tid >> 5);
-                double pi = 0.0, qi = 0.0;
-                int es = 0, w = 0;
+                pp = qq = 0.0;
+                ee = ww = 0;
                 if (act) {
-                    if (it > 1) { pi = a.p[i]; qi = a.q[i]; }
-                    es = __ldg(a.A.sl_ptr + s);
-                    w = __ldg(a.A.sl_w + s);
+                    if (it > 1) { pp = a.p[i]; qq = a.q[i]; }
+                    ee = __ldg(a.A.sl_ptr + s);
+                    ww = __ldg(a.A.sl_w + s);
                 }
-                if (!acquire(R, err)) break;
+                if (!acquire_at(aslot, apar, err)) return false;
+                const unsigned char *slot = g_slots + (size_t)aslot * R.slot;
+                if (++aslot == R.depth) { aslot = 0; apar ^= 1u; }
                 if (act) {
-                    int e0 = tile_entry(P, a.A.sl_ptr, t), e1 = tile_entry(P, a.A.sl_ptr, t + 1);
-                    es = es - e0 + (tid & 31);
-                    const double *vs;
-                    const int *cs;
-                    if (a.plan.direct) {
-                        vs = a.A.val + e0;
-                        cs = a.A.col + e0;
-                    } else {
-                        vs = reinterpret_cast<const double *>(cslot_ptr(R));
-                        cs = reinterpret_cast<const int *>(cslot_ptr(R) + (size_t)(e1 - e0) * 8);
+                    const int e0 = tile_entry(P, a.A.sl_ptr, t), e1 = tile_entry(P, a.A.sl_ptr, t + 1);
+                    ee = ee - e0 + (tid & 31);
+                    const int *cs = a.plan.direct ? a.A.col + e0 : reinterpret_cast<const int *>(slot + (size_t)(e1 - e0) * 8);
+                    int c[CG_WR];
+#pragma unroll
+                    for (int k = 0; k < CG_WR; ++k)
+                        if (k < ww) c[k] = cs[ee + 32 * k];
+#pragma unroll
+                    for (int k = 0; k < CG_WR; ++k)
+                        if (k < ww) zz[k] = a.z[c[k]];
+                }
+                return true;
+            };
+            // the FMAs of tile t (entries in the order of tile_row_dot), then its slot is released
+            auto finish = [&](int t, const double(&zz)[CG_WR], double pp, double qq, int ee, int ww) {
+                int s0, s1, r0, nr;
+                P.tile(t, s0, s1, r0, nr);
+                if (tid < nr) {
+                    const int i = r0 + tid;
+                    const int e0 = tile_entry(P, a.A.sl_ptr, t), e1 = tile_entry(P, a.A.sl_ptr, t + 1);
+                    const unsigned char *slot = g_slots + (size_t)rslot * R.slot;
+                    const double *vs = a.plan.direct ? a.A.val + e0 : reinterpret_cast<const double *>(slot);
+                    const int *cs = a.plan.direct ? a.A.col + e0 : reinterpret_cast<const int *>(slot + (size_t)(e1 - e0) * 8);
+                    double acc = 0.0, zi = 0.0;
+                    if (ww > 0) {
+                        acc = vs[ee] * zz[0];
+                        zi = zz[0];
                     }
-                    double zi;
-                    double wi = tile_row_dot<double, double, double>(vs, cs, es, w, a.z, zi);
-                    pi = fma(beta, pi, zi);
-                    qi = fma(beta, qi, wi);
-                    a.p[i] = pi;
-                    a.q[i] = qi;
-                    v1[0] = fma(pi, qi, v1[0]);
+#pragma unroll
+                    for (int k = 1; k < CG_WR; ++k)
+                        if (k < ww) acc = fma(vs[ee + 32 * k], zz[k], acc);
+                    for (int k = CG_WR; k < ww; ++k) acc = fma(vs[ee + 32 * k], a.z[cs[ee + 32 * k]], acc);
+                    pp = fma(beta, pp, zi);
+                    qq = fma(beta, qq, acc);
+                    a.p[i] = pp;
+                    a.q[i] = qq;
+                    v1[0] = fma(pp, qq, v1[0]);
                 }
-                release(R);
+                release_at(rslot);
+                if (++rslot == R.depth) rslot = 0;
+            };
+            bool ok = nt > 0 && fetch(0, zc, pc, qc, ec, wc);
+            for (int t = 0; ok && t < nt; ++t) {
+                if (t + 1 < nt && !fetch(t + 1, zn, pn, qn, en, wn)) break;
+                finish(t, zc, pc, qc, ec, wc);
+#pragma unroll
+                for (int k = 0; k < CG_WR; ++k) zc[k] = zn[k];
+                pc = pn;
+                qc = qn;
+                ec = en;
+                wc = wn;
             }
+            R.cslot = aslot;
+            R.cpar = apar;
         }
         base += nt;
         if (!grid_sum_t0<1>(v1, rc, a.gb, err) || fail_flag()) break;
@@ -452,7 +518,7 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_pipe(CgPipeArgs a) {
         // X: the producer first queues the next S phase's tiles
         if (prod) producer_tiles(R, 0, issue, err);
         double v2[2] = {0.0, 0.0};
-        x_phase<double>(R0, R1, alpha, a.p, a.q, a.dinv, a.x, a.r, a.z, v2[0], v2[1]);
+        x_phase<double, CGT64>(R0, R1, alpha, a.p, a.q, a.dinv, a.x, a.r, a.z, v2[0], v2[1]);
         if (!grid_sum_t0<2>(v2, rc, a.gb, err) || fail_flag()) break;
         stamp(a.ts, it, 2);
         if (tid == 0) {
@@ -482,7 +548,7 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_pipe(CgPipeArgs a) {
 // and the search direction is kept, so the Krylov process is not restarted.
 // Convergence is decided on that FP64 residual only.  Per-thread partial dot
 // products run in FP32 over the thread's rows; exact sums across threads.
-__global__ void __launch_bounds__(KBC, 1) k_cg_mixed_pipe(CgPipeArgs a) {
+__global__ void __launch_bounds__(CGT32, 1) k_cg_mixed_pipe(CgPipeArgs a) {
     const int n = a.A.n;
     const int tid = threadIdx.x;
     const bool prod = is_producer();
@@ -502,7 +568,7 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_mixed_pipe(CgPipeArgs a) {
     // FP64 residual of the initial guess and its FP32 copy
     double v3[3] = {0.0, 0.0, 0.0};
     float f2 = 0.f;
-    for (int i = R0 + tid; i < R1; i += KBC) {
+    for (int i = R0 + tid; i < R1; i += CGT32) {
         double bi = a.b[i];
         double ri = bi - row_dot(a.A, i, a.x);
         float rf = (float)ri, zf = dinv[i] * rf;
@@ -593,7 +659,7 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_mixed_pipe(CgPipeArgs a) {
         if (g_bc[3] != 0.0) { status = DEV_BREAKDOWN; break; }
         if (prod) producer_tiles(R, 0, issue, err);
         float h0 = 0.f, h1 = 0.f;
-        x_phase<float>(R0, R1, alpha, a.p32, a.q32, dinv, a.e32, a.r32, a.z32, h0, h1);
+        x_phase<float, CGT32>(R0, R1, alpha, a.p32, a.q32, dinv, a.e32, a.r32, a.z32, h0, h1);
         double w2[2] = {(double)h0, (double)h1};
         if (!grid_sum_t0<2>(w2, rc, a.gb, err) || fail_flag()) break;
         stamp(a.ts, total, 2);
@@ -610,14 +676,14 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_mixed_pipe(CgPipeArgs a) {
         }
         __syncthreads();
         if (g_bc[4] != 0.0) {
-            for (int i = R0 + tid; i < R1; i += KBC) {
+            for (int i = R0 + tid; i < R1; i += CGT32) {
                 a.x[i] += (double)a.e32[i];
                 a.e32[i] = 0.f;
             }
             if (!grid_sync(a.gb, err)) break;
             double u[2] = {0.0, 0.0};
             float fz = 0.f;
-            for (int i = R0 + tid; i < R1; i += KBC) {
+            for (int i = R0 + tid; i < R1; i += CGT32) {
                 double ri = a.b[i] - row_dot(a.A, i, a.x);
                 float rf = (float)ri, zf = dinv[i] * rf;
                 a.r32[i] = rf;
@@ -639,7 +705,7 @@ __global__ void __launch_bounds__(KBC, 1) k_cg_mixed_pipe(CgPipeArgs a) {
     }
     drain(R);
     if (status == DEV_BREAKDOWN)  // keep the correction gathered so far
-        for (int i = R0 + tid; i < R1; i += KBC) a.x[i] += (double)a.e32[i];
+        for (int i = R0 + tid; i < R1; i += CGT32) a.x[i] += (double)a.e32[i];
     if (blockIdx.x == 0 && tid == 0) {
         double res = sqrt(rr_ref) / sqrt(bb);
         if (status == DEV_OK && !(rr_ref < thr)) status = isfinite(rr_ref) ? DEV_MAXITER : DEV_NONFINITE;
@@ -658,10 +724,10 @@ __global__ void k_dinv32(SellView A, double omega, float *dinv) {
 
 // Tile size and ring depth for a matrix whose widest slice has wmax entries
 // per row; ebytes = bytes per matrix value.
-CgPlan plan_cg(int wmax, int ebytes) {
+CgPlan plan_cg(int wmax, int ebytes, int consumers) {
     CgPlan pl;
     auto round128 = [](unsigned b) { return (b + 127u) & ~127u; };
-    for (int ts = CG_MAX_TS; ts >= 1; ts /= 2) {
+    for (int ts = consumers; ts >= 1; ts /= 2) {
         unsigned slot = round128((unsigned)ts * 32 * (unsigned)std::max(wmax, 1) * (unsigned)(ebytes + 4));
         int depth = (int)std::min<unsigned>(CopyRing::DMAX, CG_SMEM_BUDGET / slot);
         if (depth >= 2) {
@@ -673,7 +739,7 @@ CgPlan plan_cg(int wmax, int ebytes) {
         }
     }
     // rows too long for a slot: tiles read the matrix from global memory
-    pl.ts = CG_MAX_TS;
+    pl.ts = consumers;
     pl.direct = 1;
     pl.slot = 128;
     pl.depth = 2;
@@ -682,10 +748,10 @@ CgPlan plan_cg(int wmax, int ebytes) {
 }
 
 template <class K>
-int cg_max_blocks(K kernel) {
+int cg_max_blocks(K kernel, int threads) {
     SYSU_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CG_SMEM_BUDGET));
     int per_sm = 0;
-    SYSU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, KBC, CG_SMEM_BUDGET));
+    SYSU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, CG_SMEM_BUDGET));
     if (per_sm < 1) throw CaseError{"persistent CG kernel cannot be resident"};
     return per_sm * num_sms();
 }
@@ -703,7 +769,7 @@ void cg_solve(const SellDev &A, const double *val, const double *b, double *x, b
     int n = A.n;
     if (n == 0) return;
     static int maxb = 0;
-    if (!maxb) maxb = cg_max_blocks(k_cg_pipe);
+    if (!maxb) maxb = cg_max_blocks(k_cg_pipe, CGT64);
     w.ensure(n, 1, maxb, st);
     check_aligned16({val, A.col.get()});
     SellView V = view(A, val);
@@ -725,11 +791,11 @@ void cg_solve(const SellDev &A, const double *val, const double *b, double *x, b
     a.maxit = o.maxit;
     a.eps = o.eps;
     a.ts = w.phase_ts;
-    a.plan = plan_cg(A.wmax, 8);
+    a.plan = plan_cg(A.wmax, 8, CGT64 / 32 - 1);
     void *args[] = {&a};
     int G = cg_grid(A, a.plan, maxb, w.sm_cap);
     SYSU_CUDA(cudaMemsetAsync(w.barrier.get(), 0, sizeof(GridBarrier), st));  // grid_sync starts from 0
-    { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_cg_pipe, dim3(G), dim3(KBC), args, a.plan.smem, st)); ++::sysu::g_launches; }
+    { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_cg_pipe, dim3(G), dim3(CGT64), args, a.plan.smem, st)); ++::sysu::g_launches; }
 }
 
 void cg_solve_mixed(const SellDev &A, const double *val, const float *val32, const double *b, double *x,
@@ -737,7 +803,7 @@ void cg_solve_mixed(const SellDev &A, const double *val, const float *val32, con
     int n = A.n;
     if (n == 0) return;
     static int maxb = 0;
-    if (!maxb) maxb = cg_max_blocks(k_cg_mixed_pipe);
+    if (!maxb) maxb = cg_max_blocks(k_cg_mixed_pipe, CGT32);
     w.ensure(n, 1, maxb, st);
     w.ensure32(n, st);
     check_aligned16({val32, A.col.get()});
@@ -763,11 +829,11 @@ void cg_solve_mixed(const SellDev &A, const double *val, const float *val32, con
     a.eps = o.eps;
     a.inner_tol = o.inner_tol;
     a.ts = w.phase_ts;
-    a.plan = plan_cg(A.wmax, 4);
+    a.plan = plan_cg(A.wmax, 4, CGT32 / 32 - 1);
     void *args[] = {&a};
     int G = cg_grid(A, a.plan, maxb, w.sm_cap);
     SYSU_CUDA(cudaMemsetAsync(w.barrier.get(), 0, sizeof(GridBarrier), st));  // grid_sync starts from 0
-    { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_cg_mixed_pipe, dim3(G), dim3(KBC), args, a.plan.smem, st)); ++::sysu::g_launches; }
+    { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_cg_mixed_pipe, dim3(G), dim3(CGT32), args, a.plan.smem, st)); ++::sysu::g_launches; }
 }
 
 }  // namespace sysu
