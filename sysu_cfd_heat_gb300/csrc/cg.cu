@@ -320,39 +320,44 @@ __device__ __forceinline__ void issue_matrix_tile(const Part &P, const SellView 
 }
 
 // X phase over the CTA's rows: x += alpha p, r -= alpha q, z = M^-1 r and the
-// thread's partial r.r and r.z.  Two rows per thread per step with all ten
+// thread's partial r.r and r.z.  RB rows per thread per step with all their
 // loads issued before the arithmetic (the buffers are distinct, so the loads of
 // a step need not wait for the stores of the previous one); the partial sums
-// take the rows in the same order as a one-row loop.
+// take the rows in the same order as a one-row loop.  (Holding the next step's
+// loads in flight during the current step's arithmetic measured no faster.)
 __device__ __forceinline__ double fma_t(double a, double b, double c) { return __fma_rn(a, b, c); }
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
-template <class T, int NT>
+template <class T, int NT, int RB>
 __device__ __forceinline__ void x_phase(int R0, int R1, T alpha, const T *__restrict__ pv, const T *__restrict__ qv,
                                         const T *__restrict__ dv, T *__restrict__ xv, T *__restrict__ rv,
                                         T *__restrict__ zv, T &rr, T &rz) {
     int i = R0 + (int)threadIdx.x;
-    for (; i + NT < R1; i += 2 * NT) {
-        const int j = i + NT;
-        T p0 = pv[i], q0 = qv[i], x0 = xv[i], r0 = rv[i], d0 = dv[i];
-        T p1 = pv[j], q1 = qv[j], x1 = xv[j], r1 = rv[j], d1 = dv[j];
-        x0 = fma_t(alpha, p0, x0);
-        r0 = fma_t(-alpha, q0, r0);
-        x1 = fma_t(alpha, p1, x1);
-        r1 = fma_t(-alpha, q1, r1);
-        const T z0 = d0 * r0, z1 = d1 * r1;
-        xv[i] = x0;
-        rv[i] = r0;
-        zv[i] = z0;
-        xv[j] = x1;
-        rv[j] = r1;
-        zv[j] = z1;
-        rr = fma_t(r0, r0, rr);
-        rz = fma_t(r0, z0, rz);
-        rr = fma_t(r1, r1, rr);
-        rz = fma_t(r1, z1, rz);
+    for (; i + (RB - 1) * NT < R1; i += RB * NT) {
+        T p[RB], q[RB], x[RB], r[RB], d[RB];
+#pragma unroll
+        for (int u = 0; u < RB; ++u) {
+            const int j = i + u * NT;
+            p[u] = pv[j];
+            q[u] = qv[j];
+            x[u] = xv[j];
+            r[u] = rv[j];
+            d[u] = dv[j];
+        }
+#pragma unroll
+        for (int u = 0; u < RB; ++u) {
+            const int j = i + u * NT;
+            x[u] = fma_t(alpha, p[u], x[u]);
+            r[u] = fma_t(-alpha, q[u], r[u]);
+            const T z = d[u] * r[u];
+            xv[j] = x[u];
+            rv[j] = r[u];
+            zv[j] = z;
+            rr = fma_t(r[u], r[u], rr);
+            rz = fma_t(r[u], z, rz);
+        }
     }
-    if (i < R1) {
+    for (; i < R1; i += NT) {
         T pi = pv[i], qi = qv[i], xi = xv[i], ri = rv[i], di = dv[i];
         xi = fma_t(alpha, pi, xi);
         ri = fma_t(-alpha, qi, ri);
@@ -518,7 +523,7 @@ __global__ void __launch_bounds__(CGT64, 1) k_cg_pipe(CgPipeArgs a) {
         // X: the producer first queues the next S phase's tiles
         if (prod) producer_tiles(R, 0, issue, err);
         double v2[2] = {0.0, 0.0};
-        x_phase<double, CGT64>(R0, R1, alpha, a.p, a.q, a.dinv, a.x, a.r, a.z, v2[0], v2[1]);
+        x_phase<double, CGT64, 4>(R0, R1, alpha, a.p, a.q, a.dinv, a.x, a.r, a.z, v2[0], v2[1]);
         if (!grid_sum_t0<2>(v2, rc, a.gb, err) || fail_flag()) break;
         stamp(a.ts, it, 2);
         if (tid == 0) {
@@ -659,7 +664,7 @@ __global__ void __launch_bounds__(CGT32, 1) k_cg_mixed_pipe(CgPipeArgs a) {
         if (g_bc[3] != 0.0) { status = DEV_BREAKDOWN; break; }
         if (prod) producer_tiles(R, 0, issue, err);
         float h0 = 0.f, h1 = 0.f;
-        x_phase<float, CGT32>(R0, R1, alpha, a.p32, a.q32, dinv, a.e32, a.r32, a.z32, h0, h1);
+        x_phase<float, CGT32, 4>(R0, R1, alpha, a.p32, a.q32, dinv, a.e32, a.r32, a.z32, h0, h1);
         double w2[2] = {(double)h0, (double)h1};
         if (!grid_sum_t0<2>(w2, rc, a.gb, err) || fail_flag()) break;
         stamp(a.ts, total, 2);
