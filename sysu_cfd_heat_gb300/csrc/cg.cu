@@ -370,6 +370,100 @@ __device__ __forceinline__ void x_phase(int R0, int R1, T alpha, const T *__rest
     }
 }
 
+// S phase of one CG iteration for a consumer warp: w = A z, p = z + beta p,
+// q = w + beta q over the CTA's tiles; returns the thread's partial p.q.  One
+// tile ahead: tile t+1's row loads and its first CG_WR gathers are in flight
+// while tile t's FMAs run, so the arithmetic of one tile overlaps the memory
+// latency of the next (the warp holds two slots).  val: the matrix values of
+// this precision (read from global memory in direct mode).  The FMAs take a
+// row's entries in order, the first as a product, as tile_row_dot does.
+template <class V>
+__device__ __forceinline__ V s_phase(const Part &P, Ring &R, const SellView &A, const V *val, int direct,
+                                     V *__restrict__ pv, V *__restrict__ qv, const V *__restrict__ zv, V beta,
+                                     bool has_dir, int *err) {
+    const int tid = threadIdx.x;
+    const int nt = P.nt;
+    int aslot = R.cslot;  // acquire cursor
+    unsigned apar = R.cpar;
+    int rslot = R.cslot;  // release cursor
+    V zc[CG_WR], zn[CG_WR];
+    V pc = 0, qc = 0, pn = 0, qn = 0, pq = 0;
+    int ec = 0, wc = 0, en = 0, wn = 0;
+    // row loads, tile wait, column reads and gathers of tile t
+    auto fetch = [&](int t, V(&zz)[CG_WR], V &pp, V &qq, int &ee, int &ww) -> bool {
+        int s0, s1, r0, nr;
+        P.tile(t, s0, s1, r0, nr);
+        const bool act = tid < nr;
+        const int i = r0 + tid;
+        const int s = s0 + (tid >> 5);
+        pp = qq = 0;
+        ee = ww = 0;
+        if (act) {
+            if (has_dir) { pp = pv[i]; qq = qv[i]; }
+            ee = __ldg(A.sl_ptr + s);
+            ww = __ldg(A.sl_w + s);
+        }
+        if (!acquire_at(aslot, apar, err)) return false;
+        const unsigned char *slot = g_slots + (size_t)aslot * R.slot;
+        if (++aslot == R.depth) { aslot = 0; apar ^= 1u; }
+        if (act) {
+            const int e0 = tile_entry(P, A.sl_ptr, t), e1 = tile_entry(P, A.sl_ptr, t + 1);
+            ee = ee - e0 + (tid & 31);
+            const int *cs = direct ? A.col + e0 : reinterpret_cast<const int *>(slot + (size_t)(e1 - e0) * sizeof(V));
+            int c[CG_WR];
+#pragma unroll
+            for (int k = 0; k < CG_WR; ++k)
+                if (k < ww) c[k] = cs[ee + 32 * k];
+#pragma unroll
+            for (int k = 0; k < CG_WR; ++k)
+                if (k < ww) zz[k] = zv[c[k]];
+        }
+        return true;
+    };
+    // the FMAs of tile t, then its slot is released
+    auto finish = [&](int t, const V(&zz)[CG_WR], V pp, V qq, int ee, int ww) {
+        int s0, s1, r0, nr;
+        P.tile(t, s0, s1, r0, nr);
+        if (tid < nr) {
+            const int i = r0 + tid;
+            const int e0 = tile_entry(P, A.sl_ptr, t), e1 = tile_entry(P, A.sl_ptr, t + 1);
+            const unsigned char *slot = g_slots + (size_t)rslot * R.slot;
+            const V *vs = direct ? val + e0 : reinterpret_cast<const V *>(slot);
+            const int *cs = direct ? A.col + e0 : reinterpret_cast<const int *>(slot + (size_t)(e1 - e0) * sizeof(V));
+            V acc = 0, zi = 0;
+            if (ww > 0) {
+                acc = vs[ee] * zz[0];
+                zi = zz[0];
+            }
+#pragma unroll
+            for (int k = 1; k < CG_WR; ++k)
+                if (k < ww) acc = fma_t(vs[ee + 32 * k], zz[k], acc);
+            for (int k = CG_WR; k < ww; ++k) acc = fma_t(vs[ee + 32 * k], zv[cs[ee + 32 * k]], acc);
+            pp = fma_t(beta, pp, zi);
+            qq = fma_t(beta, qq, acc);
+            pv[i] = pp;
+            qv[i] = qq;
+            pq = fma_t(pp, qq, pq);
+        }
+        release_at(rslot);
+        if (++rslot == R.depth) rslot = 0;
+    };
+    bool ok = nt > 0 && fetch(0, zc, pc, qc, ec, wc);
+    for (int t = 0; ok && t < nt; ++t) {
+        if (t + 1 < nt && !fetch(t + 1, zn, pn, qn, en, wn)) break;
+        finish(t, zc, pc, qc, ec, wc);
+#pragma unroll
+        for (int k = 0; k < CG_WR; ++k) zc[k] = zn[k];
+        pc = pn;
+        qc = qn;
+        ec = en;
+        wc = wn;
+    }
+    R.cslot = aslot;
+    R.cpar = apar;
+    return pq;
+}
+
 // ---------------------------------------------------------------------------
 // FP64
 __global__ void __launch_bounds__(CGT64, 1) k_cg_pipe(CgPipeArgs a) {
@@ -428,87 +522,7 @@ __global__ void __launch_bounds__(CGT64, 1) k_cg_pipe(CgPipeArgs a) {
         if (prod) {
             producer_tiles(R, base + nt, issue, err);
         } else {
-            // One tile ahead: tile t+1's row loads and its first CG_WR gathers are
-            // in flight while tile t's FMAs run, so the FP64 work of one tile
-            // overlaps the memory latency of the next.  A warp holds two slots.
-            int aslot = R.cslot;  // acquire cursor
-            unsigned apar = R.cpar;
-            int rslot = R.cslot;  // release cursor
-            double zc[CG_WR], zn[CG_WR];
-            double pc = 0.0, qc = 0.0, pn = 0.0, qn = 0.0;
-            int ec = 0, wc = 0, en = 0, wn = 0;
-            // row loads, tile wait, column reads and gathers of tile t
-            auto fetch = [&](int t, double(&zz)[CG_WR], double &pp, double &qq, int &ee, int &ww) -> bool {
-                int s0, s1, r0, nr;
-                P.tile(t, s0, s1, r0, nr);
-                const bool act = tid < nr;
-                const int i = r0 + tid;
-                const int s = s0 + (tid >> 5);
-                pp = qq = 0.0;
-                ee = ww = 0;
-                if (act) {
-                    if (it > 1) { pp = a.p[i]; qq = a.q[i]; }
-                    ee = __ldg(a.A.sl_ptr + s);
-                    ww = __ldg(a.A.sl_w + s);
-                }
-                if (!acquire_at(aslot, apar, err)) return false;
-                const unsigned char *slot = g_slots + (size_t)aslot * R.slot;
-                if (++aslot == R.depth) { aslot = 0; apar ^= 1u; }
-                if (act) {
-                    const int e0 = tile_entry(P, a.A.sl_ptr, t), e1 = tile_entry(P, a.A.sl_ptr, t + 1);
-                    ee = ee - e0 + (tid & 31);
-                    const int *cs = a.plan.direct ? a.A.col + e0 : reinterpret_cast<const int *>(slot + (size_t)(e1 - e0) * 8);
-                    int c[CG_WR];
-#pragma unroll
-                    for (int k = 0; k < CG_WR; ++k)
-                        if (k < ww) c[k] = cs[ee + 32 * k];
-#pragma unroll
-                    for (int k = 0; k < CG_WR; ++k)
-                        if (k < ww) zz[k] = a.z[c[k]];
-                }
-                return true;
-            };
-            // the FMAs of tile t (entries in the order of tile_row_dot), then its slot is released
-            auto finish = [&](int t, const double(&zz)[CG_WR], double pp, double qq, int ee, int ww) {
-                int s0, s1, r0, nr;
-                P.tile(t, s0, s1, r0, nr);
-                if (tid < nr) {
-                    const int i = r0 + tid;
-                    const int e0 = tile_entry(P, a.A.sl_ptr, t), e1 = tile_entry(P, a.A.sl_ptr, t + 1);
-                    const unsigned char *slot = g_slots + (size_t)rslot * R.slot;
-                    const double *vs = a.plan.direct ? a.A.val + e0 : reinterpret_cast<const double *>(slot);
-                    const int *cs = a.plan.direct ? a.A.col + e0 : reinterpret_cast<const int *>(slot + (size_t)(e1 - e0) * 8);
-                    double acc = 0.0, zi = 0.0;
-                    if (ww > 0) {
-                        acc = vs[ee] * zz[0];
-                        zi = zz[0];
-                    }
-#pragma unroll
-                    for (int k = 1; k < CG_WR; ++k)
-                        if (k < ww) acc = fma(vs[ee + 32 * k], zz[k], acc);
-                    for (int k = CG_WR; k < ww; ++k) acc = fma(vs[ee + 32 * k], a.z[cs[ee + 32 * k]], acc);
-                    pp = fma(beta, pp, zi);
-                    qq = fma(beta, qq, acc);
-                    a.p[i] = pp;
-                    a.q[i] = qq;
-                    v1[0] = fma(pp, qq, v1[0]);
-                }
-                release_at(rslot);
-                if (++rslot == R.depth) rslot = 0;
-            };
-            bool ok = nt > 0 && fetch(0, zc, pc, qc, ec, wc);
-            for (int t = 0; ok && t < nt; ++t) {
-                if (t + 1 < nt && !fetch(t + 1, zn, pn, qn, en, wn)) break;
-                finish(t, zc, pc, qc, ec, wc);
-#pragma unroll
-                for (int k = 0; k < CG_WR; ++k) zc[k] = zn[k];
-                pc = pn;
-                qc = qn;
-                ec = en;
-                wc = wn;
-            }
-            R.cslot = aslot;
-            R.cpar = apar;
+            v1[0] = s_phase<double>(P, R, a.A, a.A.val, a.plan.direct, a.p, a.q, a.z, beta, it > 1, err);
         }
         base += nt;
         if (!grid_sum_t0<1>(v1, rc, a.gb, err) || fail_flag()) break;
@@ -614,6 +628,8 @@ __global__ void __launch_bounds__(CGT32, 1) k_cg_mixed_pipe(CgPipeArgs a) {
         if (prod) {
             producer_tiles(R, base + nt, issue, err);
         } else {
+            // one tile at a time: the look-ahead of s_phase measured slower here (FP32
+            // arithmetic is cheap, and its registers spill at 768 threads)
             for (int t = 0; t < nt; ++t) {
                 int s0, s1, r0, nr;
                 P.tile(t, s0, s1, r0, nr);
