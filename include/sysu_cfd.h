@@ -189,6 +189,12 @@ int sysu_csr_solve(int method, int precond, int n, const int *rowptr, const int 
                    const double *b, double *x, int maxit, double eps, double omega, int *iters, double *res,
                    int *status);
 int sysu_csr_spmv(int n, const int *rowptr, const int *col, const double *val, const double *x, double *y);
+/* Kernel form of the standalone SpMV (sysu_csr_spmv and the sweep of
+ * sysu_solver_spmv_timing), process-wide: 0 one row per thread over a full
+ * grid (default), 100 persistent ring (matrix streamed through shared memory
+ * by bulk copies, one CTA per SM), 10 b + s the persistent grid with s slices
+ * per warp step and b blocks per SM.  All forms give bit-identical y. */
+int sysu_set_spmv_variant(int variant);
 /* Three systems sharing one sparsity pattern (rowptr, col), values vals[c],
  * right-hand sides b[c], x[c] (x0 in, solution out), solved by one batched
  * BiCGSTAB + Jacobi launch (the k, eps, T form of option "scalars_batched"). */

@@ -71,6 +71,7 @@ def lib() -> C.CDLL:
             "sysu_csr_solve": (C.c_int, [C.c_int, C.c_int, C.c_int, ip, ip, dp, dp, dp, C.c_int, C.c_double,
                                          C.c_double, ip, dp, ip]),
             "sysu_csr_spmv": (C.c_int, [C.c_int, ip, ip, dp, dp, dp]),
+            "sysu_set_spmv_variant": (C.c_int, [C.c_int]),
             "sysu_csr_last_error": (cp, []),
             "sysu_csr_bicgstab_batched3": (C.c_int, [C.c_int, ip, ip, C.POINTER(dp), C.POINTER(dp), C.POINTER(dp),
                                                      C.c_int, C.c_double, ip, dp, ip]),

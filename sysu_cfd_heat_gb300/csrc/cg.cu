@@ -150,7 +150,7 @@ __device__ __forceinline__ unsigned char *cslot_ptr(const Ring &R) { return g_sl
 // issues the copies and takes the barrier decisions, broadcast to the warp.
 // The state is worked on in registers (the copy instructions clobber memory).
 template <class Issue>
-__device__ __forceinline__ bool produce(const Ring &R, long long must_end, Issue &&issue) {
+__device__ __forceinline__ bool produce(const Ring &R, long long must_end, long long stop, Issue &&issue) {
     Producer &Q = g_prod;
     const bool lead = (threadIdx.x & 31) == 0;
     const int nt = Q.nt, depth = R.depth;
@@ -160,6 +160,7 @@ __device__ __forceinline__ bool produce(const Ring &R, long long must_end, Issue
     const uint64_t pol = l2_policy_evict_first();
     bool ok = true;
     for (;;) {
+        if (issued >= stop) break;
         if (primed == depth) {  // the slot's previous tile must be released by all consumers
             int free_slot = lead ? (int)mbar_test_wait(&g_empty[islot], ipar ^ 1u) : 0;
             free_slot = __shfl_sync(FULL_MASK, free_slot, 0);
@@ -190,11 +191,12 @@ __device__ __forceinline__ bool produce(const Ring &R, long long must_end, Issue
 }
 
 // Producer warp: the running S phase's tiles up to must_end (blocking) and
-// whatever fits in free slots after them.
+// whatever fits in free slots after them, never past tile job `stop`.
 template <class Issue>
-__device__ __forceinline__ void producer_tiles(const Ring &R, long long must_end, Issue &&issue, int *err) {
+__device__ __forceinline__ void producer_tiles(const Ring &R, long long must_end, Issue &&issue, int *err,
+                                               long long stop = LLONG_MAX) {
     if (!__all_sync(FULL_MASK, !fail_flag())) return;
-    bool ok = produce(R, must_end, issue);
+    bool ok = produce(R, must_end, stop, issue);
     if (!ok && (threadIdx.x & 31) == 0) set_fail(err);
 }
 
@@ -370,24 +372,24 @@ __device__ __forceinline__ void x_phase(int R0, int R1, T alpha, const T *__rest
     }
 }
 
-// S phase of one CG iteration for a consumer warp: w = A z, p = z + beta p,
-// q = w + beta q over the CTA's tiles; returns the thread's partial p.q.  One
+// Consumer warps over the CTA's tiles, one row per thread per tile: w = A z for
+// the row, then epi(i, w, z_i, p_i, q_i) (p_i, q_i loaded when has_dir).  One
 // tile ahead: tile t+1's row loads and its first CG_WR gathers are in flight
 // while tile t's FMAs run, so the arithmetic of one tile overlaps the memory
 // latency of the next (the warp holds two slots).  val: the matrix values of
 // this precision (read from global memory in direct mode).  The FMAs take a
 // row's entries in order, the first as a product, as tile_row_dot does.
-template <class V>
-__device__ __forceinline__ V s_phase(const Part &P, Ring &R, const SellView &A, const V *val, int direct,
-                                     V *__restrict__ pv, V *__restrict__ qv, const V *__restrict__ zv, V beta,
-                                     bool has_dir, int *err) {
+template <class V, class Epi>
+__device__ __forceinline__ void tiles_ahead(const Part &P, Ring &R, const SellView &A, const V *val, int direct,
+                                            const V *pv, const V *qv, const V *__restrict__ zv, bool has_dir,
+                                            int *err, Epi &&epi) {
     const int tid = threadIdx.x;
     const int nt = P.nt;
     int aslot = R.cslot;  // acquire cursor
     unsigned apar = R.cpar;
     int rslot = R.cslot;  // release cursor
     V zc[CG_WR], zn[CG_WR];
-    V pc = 0, qc = 0, pn = 0, qn = 0, pq = 0;
+    V pc = 0, qc = 0, pn = 0, qn = 0;
     int ec = 0, wc = 0, en = 0, wn = 0;
     // row loads, tile wait, column reads and gathers of tile t
     auto fetch = [&](int t, V(&zz)[CG_WR], V &pp, V &qq, int &ee, int &ww) -> bool {
@@ -439,11 +441,7 @@ __device__ __forceinline__ V s_phase(const Part &P, Ring &R, const SellView &A, 
             for (int k = 1; k < CG_WR; ++k)
                 if (k < ww) acc = fma_t(vs[ee + 32 * k], zz[k], acc);
             for (int k = CG_WR; k < ww; ++k) acc = fma_t(vs[ee + 32 * k], zv[cs[ee + 32 * k]], acc);
-            pp = fma_t(beta, pp, zi);
-            qq = fma_t(beta, qq, acc);
-            pv[i] = pp;
-            qv[i] = qq;
-            pq = fma_t(pp, qq, pq);
+            epi(i, acc, zi, pp, qq);
         }
         release_at(rslot);
         if (++rslot == R.depth) rslot = 0;
@@ -461,6 +459,22 @@ __device__ __forceinline__ V s_phase(const Part &P, Ring &R, const SellView &A, 
     }
     R.cslot = aslot;
     R.cpar = apar;
+}
+
+// S phase of one CG iteration for a consumer warp: w = A z, p = z + beta p,
+// q = w + beta q; returns the thread's partial p.q.
+template <class V>
+__device__ __forceinline__ V s_phase(const Part &P, Ring &R, const SellView &A, const V *val, int direct,
+                                     V *__restrict__ pv, V *__restrict__ qv, const V *__restrict__ zv, V beta,
+                                     bool has_dir, int *err) {
+    V pq = 0;
+    tiles_ahead<V>(P, R, A, val, direct, pv, qv, zv, has_dir, err, [&](int i, V w, V zi, V pp, V qq) {
+        pp = fma_t(beta, pp, zi);
+        qq = fma_t(beta, qq, w);
+        pv[i] = pp;
+        qv[i] = qq;
+        pq = fma_t(pp, qq, pq);
+    });
     return pq;
 }
 
@@ -743,6 +757,28 @@ __global__ void k_dinv32(SellView A, double omega, float *dinv) {
     dinv[i] = (float)(omega / A.val[A.sl_ptr[i >> 5] + (i & 31)]);
 }
 
+// ---------------------------------------------------------------------------
+// Standalone y = A x with the matrix streamed through the same ring (the SpMV
+// of the sweep): one CTA per SM, the producer issues each of the CTA's tiles
+// once, the consumers gather x one tile ahead.
+template <class V>
+__global__ void __launch_bounds__(CGT64, 1) k_spmv_ring(SellView A, const V *val, const V *x, V *y, CgPlan plan,
+                                                       int *err) {
+    const Part P = make_part(A.n, A.nslices, plan.ts);
+    Ring R;
+    ring_init(R, plan, P, A.sl_ptr);
+    auto issue = [&](int t, unsigned char *dst, uint64_t *bar, uint64_t pol) {
+        issue_matrix_tile<V>(P, A, val, plan.direct, t, dst, bar, pol);
+    };
+    if (is_producer()) {
+        producer_tiles(R, P.nt, issue, err, P.nt);
+    } else {
+        tiles_ahead<V>(P, R, A, val, plan.direct, nullptr, nullptr, x, false, err,
+                       [&](int i, V w, V, V, V) { y[i] = w; });
+    }
+    drain(R);
+}
+
 // Tile size and ring depth for a matrix whose widest slice has wmax entries
 // per row; ebytes = bytes per matrix value.
 CgPlan plan_cg(int wmax, int ebytes, int consumers) {
@@ -817,6 +853,28 @@ void cg_solve(const SellDev &A, const double *val, const double *b, double *x, b
     int G = cg_grid(A, a.plan, maxb, w.sm_cap);
     SYSU_CUDA(cudaMemsetAsync(w.barrier.get(), 0, sizeof(GridBarrier), st));  // grid_sync starts from 0
     { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_cg_pipe, dim3(G), dim3(CGT64), args, a.plan.smem, st)); ++::sysu::g_launches; }
+}
+
+template <class V>
+static void spmv_ring_t(const SellDev &A, const V *val, const V *x, V *y, int *err, cudaStream_t st) {
+    if (A.n == 0) return;
+    static int maxb = 0;
+    if (!maxb) maxb = cg_max_blocks(k_spmv_ring<V>, CGT64);
+    check_aligned16({val, A.col.get()});
+    const CgPlan pl = plan_cg(A.wmax, (int)sizeof(V), CGT64 / 32 - 1);
+    const int G = cg_grid(A, pl, maxb, 0);
+    SellView Av = view(A, nullptr);
+    k_spmv_ring<V><<<G, CGT64, pl.smem, st>>>(Av, val, x, y, pl, err);
+    ++::sysu::g_launches;
+    SYSU_CUDA(cudaGetLastError());
+}
+
+void spmv_ring(const SellDev &A, const double *val, const double *x, double *y, int *err, cudaStream_t st) {
+    spmv_ring_t<double>(A, val, x, y, err, st);
+}
+
+void spmv_ring32(const SellDev &A, const float *val, const float *x, float *y, int *err, cudaStream_t st) {
+    spmv_ring_t<float>(A, val, x, y, err, st);
 }
 
 void cg_solve_mixed(const SellDev &A, const double *val, const float *val32, const double *b, double *x,

@@ -76,6 +76,15 @@ int sysu_csr_solve(int method, int precond, int n, const int *rowptr, const int 
     }
 }
 
+int sysu_set_spmv_variant(int variant) {
+    if (variant != 0 && variant != sysu::SPMV_RING && !(variant >= 11 && variant <= 99 && (variant % 10 == 1 || variant % 10 == 2 || variant % 10 == 4))) {
+        g_csr_err = "sysu_set_spmv_variant: 0, 100 or 10 b + s with s in {1, 2, 4}";
+        return SYSU_ERR_INPUT;
+    }
+    sysu::set_spmv_variant(variant);
+    return SYSU_OK;
+}
+
 // y = A x for a host CSR matrix, on the GPU.
 int sysu_csr_spmv(int n, const int *rowptr, const int *col, const double *val, const double *x, double *y) {
     try {
@@ -86,9 +95,15 @@ int sysu_csr_spmv(int n, const int *rowptr, const int *col, const double *val, c
             M.load(n, rowptr, col, val, st);
             sysu::DevBuf<double> dx(n), dy(n);
             dx.upload(x, n, st);
-            sysu::spmv(M.A, M.val.get(), dx.get(), dy.get(), st);
+            sysu::DevBuf<int> err(1);
+            err.zero(st);
+            if (sysu::spmv_variant() == sysu::SPMV_RING) sysu::spmv_ring(M.A, M.val.get(), dx.get(), dy.get(), err.get(), st);
+            else sysu::spmv(M.A, M.val.get(), dx.get(), dy.get(), st);
             dy.download(y, n, st);
+            int e = 0;
+            err.download(&e, 1, st);
             SYSU_CUDA(cudaStreamSynchronize(st));
+            if (e != 0) throw sysu::CaseError{"sysu_csr_spmv: a bounded wait of the ring SpMV gave up"};
         }
         cudaStreamDestroy(st);
         return SYSU_OK;

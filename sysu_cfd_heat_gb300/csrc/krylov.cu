@@ -607,6 +607,7 @@ void spmv_stream32(const SellDev &A, const float *val, const float *x, float *y,
 }
 
 void set_spmv_variant(int v) { g_spmv_variant = v; }
+int spmv_variant() { return g_spmv_variant; }
 
 void l2_flush_read(const void *buf, size_t bytes, unsigned *sink, cudaStream_t st) {
     size_t n16 = bytes / 16;

@@ -153,6 +153,13 @@ void spmv_stream32(const SellDev &A, const float *val, const float *x, float *y,
 // SpMV kernel form of spmv_stream / spmv_stream32: 0 one row per thread over a
 // full grid; 10 b + s: b blocks of 256 per SM, s in {1, 2, 4} slices per warp step.
 void set_spmv_variant(int v);
+int spmv_variant();
+constexpr int SPMV_RING = 100;  // spmv_variant value that selects spmv_ring in the sweep
+// y = A x by a persistent kernel that streams the matrix through a shared-memory
+// ring with bulk copies (one CTA per SM; cg.cu).  *err (device) is set if a
+// bounded wait in the ring gave up.  val and the column indices 16-byte aligned.
+void spmv_ring(const SellDev &A, const double *val, const double *x, double *y, int *err, cudaStream_t st);
+void spmv_ring32(const SellDev &A, const float *val, const float *x, float *y, int *err, cudaStream_t st);
 // L2 flush by reading `bytes` (> L2) of buf: clean lines, no write-back later.
 void l2_flush_read(const void *buf, size_t bytes, unsigned *sink, cudaStream_t st);
 // x of the sweep (FP64 and its FP32 copy).

@@ -926,6 +926,9 @@ double SimpleSolver::spmv_timing(const std::string &which, bool fp32, int reps) 
     DevBuf<float> x32(n), y32(n), v32;
     DevBuf<unsigned char> flush((size_t)256 << 20);
     DevBuf<unsigned> sink(1);
+    DevBuf<int> err(1);
+    err.zero(st);
+    const bool ring = spmv_variant() == SPMV_RING;
     SYSU_CUDA(cudaMemsetAsync(flush.get(), 1, flush.size(), st));
     fill_sweep_x((long)n, x64.get(), x32.get(), st);
     if (fp32) {
@@ -936,7 +939,9 @@ double SimpleSolver::spmv_timing(const std::string &which, bool fp32, int reps) 
     for (int k = 0; k < reps + 1; ++k) {
         l2_flush_read(flush.get(), flush.size(), sink.get(), st);
         SYSU_CUDA(cudaEventRecord(ev[4], st));
-        if (fp32) spmv_stream32(A, v32.get(), x32.get(), y32.get(), st);
+        if (ring && fp32) spmv_ring32(A, v32.get(), x32.get(), y32.get(), err.get(), st);
+        else if (ring) spmv_ring(A, v->get(), x64.get(), y64.get(), err.get(), st);
+        else if (fp32) spmv_stream32(A, v32.get(), x32.get(), y32.get(), st);
         else spmv_stream(A, v->get(), x64.get(), y64.get(), st);
         SYSU_CUDA(cudaEventRecord(ev[5], st));
         SYSU_CUDA(cudaEventSynchronize(ev[5]));
@@ -944,6 +949,9 @@ double SimpleSolver::spmv_timing(const std::string &which, bool fp32, int reps) 
         SYSU_CUDA(cudaEventElapsedTime(&ms, ev[4], ev[5]));
         if (k > 0) total += ms;  // the first product warms up
     }
+    int e = 0;
+    SYSU_CUDA(cudaMemcpy(&e, err.get(), sizeof(int), cudaMemcpyDeviceToHost));
+    if (e != 0) throw CaseError{"spmv_timing: a bounded wait of the ring SpMV gave up"};
     return total / reps;
 }
 

@@ -244,6 +244,13 @@ def csr_solve(rowptr, col, val, b, x0=None, method: str = "CG", precond: str = "
     return x, it.value, rs.value, stt.value
 
 
+def set_spmv_variant(variant: int) -> None:
+    """Kernel form of the standalone SpMV (csr_spmv, spmv_timing), process-wide:
+    0 one row per thread (default), 100 persistent ring with bulk copies."""
+    if lib().sysu_set_spmv_variant(int(variant)) != 0:
+        raise RuntimeError(lib().sysu_csr_last_error().decode())
+
+
 def csr_spmv(rowptr, col, val, x):
     L = lib()
     fn = L.sysu_csr_spmv

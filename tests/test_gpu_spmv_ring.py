@@ -1,0 +1,73 @@
+"""The standalone SpMV forms give the same y bit for bit.
+
+The persistent ring product (matrix tiles streamed through shared memory by bulk
+copies, x gathered one tile ahead) against the one-row-per-thread kernel and a
+numpy CSR product, on ragged sizes, rows wider than the six gathers held in
+registers, and rows too wide for a ring slot (read from global memory).
+"""
+import numpy as np
+import pytest
+
+from sysu_cfd_heat_gb300.solver import csr_spmv, set_spmv_variant
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(autouse=True)
+def _default_variant():
+    yield
+    set_spmv_variant(0)
+
+
+def _random_csr(n, wmin, wmax, seed, wide_rows=()):
+    rng = np.random.default_rng(seed)
+    rows, cols, vals = [], [], []
+    for i in range(n):
+        w = int(rng.integers(wmin, wmax + 1)) if i not in wide_rows else min(n, 300)
+        nb = rng.choice(n, size=min(n, w), replace=False)
+        nb = [i] + [int(c) for c in nb if c != i][: max(0, w - 1)]
+        rows.append(len(nb))
+        cols.extend(nb)
+        vals.extend(rng.standard_normal(len(nb)).tolist())
+    rowptr = np.concatenate([[0], np.cumsum(rows)]).astype(np.int32)
+    return rowptr, np.array(cols, np.int32), np.array(vals, np.float64)
+
+
+def _numpy_spmv(rowptr, col, val, x):
+    y = np.zeros(len(rowptr) - 1)
+    for i in range(len(y)):
+        a, b = rowptr[i], rowptr[i + 1]
+        y[i] = np.dot(val[a:b], x[col[a:b]])
+    return y
+
+
+@pytest.mark.parametrize("n,wmin,wmax,wide", [
+    (40003, 1, 9, ()),          # ragged slices, widths past the register gathers
+    (20000, 5, 5, ()),          # tet-like, uniform width
+    (31, 1, 4, ()),             # one partial slice
+    (5000, 2, 7, (17, 4321)),   # two rows of 300 entries: the matrix is read from global memory
+])
+def test_ring_matches_stream(n, wmin, wmax, wide):
+    rowptr, col, val = _random_csr(n, wmin, wmax, seed=n + wmax, wide_rows=wide)
+    x = np.random.default_rng(7).standard_normal(n)
+    set_spmv_variant(0)
+    y0 = csr_spmv(rowptr, col, val, x)
+    set_spmv_variant(100)
+    y1 = csr_spmv(rowptr, col, val, x)
+    assert np.array_equal(y0, y1)
+    if n <= 20000:
+        ref = _numpy_spmv(rowptr, col, val, x)
+        np.testing.assert_allclose(y1, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+
+
+def test_single_row_and_empty():
+    set_spmv_variant(100)
+    y = csr_spmv(np.array([0, 1], np.int32), np.array([0], np.int32), np.array([2.5]), np.array([4.0]))
+    assert y.tolist() == [10.0]
+    y = csr_spmv(np.array([0], np.int32), np.zeros(0, np.int32), np.zeros(0), np.zeros(0))
+    assert y.size == 0
+
+
+def test_bad_variant_rejected():
+    with pytest.raises(RuntimeError):
+        set_spmv_variant(7)
