@@ -254,6 +254,109 @@ __global__ void __launch_bounds__(256) k_spmv_multi(int n, int nslices, const in
     }
 }
 
+// The same product with the matrix entries staged in shared memory by each warp
+// through cp.async (4- and 8-byte copies, no registers held while they are in
+// flight): a warp takes slices gw, gw + W, ... and keeps SPMV_AS of them in a
+// pipeline -- the entries of the slice SPMV_AS - 1 ahead are copied while the
+// current slice's x gathers and FMAs run, and the slice pointers are loaded one
+// step before they are needed.  A thread reads back only the entries it copied
+// itself, so cp.async.wait_group alone orders them.  Slices wider than
+// SPMV_AW are read from global memory.  Same FMA order as k_spmv_stream.
+constexpr int SPMV_AS = 3;    // slices in flight per warp
+constexpr int SPMV_AW = 8;    // widest staged slice
+constexpr int SPMV_AT = 256;  // threads per block
+
+template <int B>
+__device__ __forceinline__ void cp_async_ca(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src),
+                 "n"(B)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+template <class V>
+constexpr size_t spmv_async_smem() {
+    return (size_t)(SPMV_AT / 32) * SPMV_AS * 32 * SPMV_AW * (sizeof(V) + sizeof(int));
+}
+
+template <class V>
+__global__ void __launch_bounds__(SPMV_AT) k_spmv_async(int n, int nslices, const int *__restrict__ sl_ptr,
+                                                        const int *__restrict__ sl_w, const int *__restrict__ col,
+                                                        const V *__restrict__ val, const V *__restrict__ x,
+                                                        V *__restrict__ y) {
+    extern __shared__ __align__(16) unsigned char spmv_smem[];
+    constexpr int SLOT = 32 * SPMV_AW;  // entries of one stage
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int gw = blockIdx.x * (SPMV_AT / 32) + wib;
+    const int W = gridDim.x * (SPMV_AT / 32);
+    V *vb = reinterpret_cast<V *>(spmv_smem) + (size_t)wib * SPMV_AS * SLOT;
+    int *cb = reinterpret_cast<int *>(spmv_smem + (size_t)(SPMV_AT / 32) * SPMV_AS * SLOT * sizeof(V)) +
+              (size_t)wib * SPMV_AS * SLOT;
+    const int J = gw < nslices ? (nslices - 1 - gw) / W + 1 : 0;  // slices of this warp
+    int me[SPMV_AS], mw[SPMV_AS];                                  // slice pointer and width, by stage
+    auto load_meta = [&](int j, int &e, int &w) {
+        e = 0;
+        w = 0;
+        if (j < J) {
+            const int s = gw + j * W;
+            e = __ldg(sl_ptr + s);
+            w = __ldg(sl_w + s);
+        }
+    };
+    auto issue = [&](int j, int stage, int e, int w) {
+        if (j < J && w <= SPMV_AW) {
+            const int eb = e + lane;
+            V *vd = vb + stage * SLOT + lane;
+            int *cd = cb + stage * SLOT + lane;
+            for (int k = 0; k < w; ++k) {
+                cp_async_ca<(int)sizeof(V)>(vd + 32 * k, val + eb + 32 * k);
+                cp_async_ca<4>(cd + 32 * k, col + eb + 32 * k);
+            }
+        }
+        cp_async_commit();  // possibly empty: one group per slice keeps the count uniform
+    };
+#pragma unroll
+    for (int u = 0; u < SPMV_AS; ++u) load_meta(u, me[u], mw[u]);
+#pragma unroll
+    for (int u = 0; u < SPMV_AS - 1; ++u) issue(u, u, me[u], mw[u]);
+    for (int j0 = 0; j0 < J; j0 += SPMV_AS) {
+#pragma unroll
+        for (int u = 0; u < SPMV_AS; ++u) {
+            const int j = j0 + u;
+            cp_async_wait<SPMV_AS - 2>();  // slice j's copies have landed
+            if (j < J) {
+                const int row = (gw + j * W) * 32 + lane;
+                const int w = mw[u];
+                V acc = (V)0;
+                if (w <= SPMV_AW) {
+                    int c[SPMV_AW];
+                    V xv[SPMV_AW];
+#pragma unroll
+                    for (int k = 0; k < SPMV_AW; ++k)
+                        if (k < w) c[k] = cb[u * SLOT + 32 * k + lane];
+#pragma unroll
+                    for (int k = 0; k < SPMV_AW; ++k)
+                        if (k < w) xv[k] = __ldg(x + c[k]);
+#pragma unroll
+                    for (int k = 0; k < SPMV_AW; ++k)
+                        if (k < w) acc = fma(vb[u * SLOT + 32 * k + lane], xv[k], acc);
+                } else {
+                    const int e = me[u] + lane;
+                    for (int k = 0; k < w; ++k) acc = fma(__ldcs(val + e + 32 * k), __ldg(x + __ldcs(col + e + 32 * k)), acc);
+                }
+                if (row < n) y[row] = acc;
+            }
+            // the slice SPMV_AS - 1 ahead goes into the stage freed one step ago
+            const int nxt = (u + SPMV_AS - 1) % SPMV_AS;
+            issue(j + SPMV_AS - 1, nxt, me[nxt], mw[nxt]);
+            load_meta(j + SPMV_AS, me[u], mw[u]);
+        }
+    }
+    cp_async_wait<0>();
+}
+
 int g_spmv_variant = 0;
 
 // Reads a buffer larger than L2 (16-byte loads, one word written) so the
@@ -581,7 +684,18 @@ template <class V>
 static void spmv_dispatch(const SellDev &A, const V *val, const V *x, V *y, cudaStream_t st) {
     if (A.n == 0) return;
     const int v = g_spmv_variant;
-    if (v == 0) {
+    if (v == SPMV_ASYNC) {
+        static int per_sm[2] = {0, 0};
+        int &ps = per_sm[sizeof(V) == 8 ? 1 : 0];
+        const int sm = (int)spmv_async_smem<V>();
+        if (!ps) {
+            SYSU_CUDA(cudaFuncSetAttribute(k_spmv_async<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+            SYSU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, k_spmv_async<V>, SPMV_AT, sm));
+            ps = std::max(ps, 1);
+        }
+        const int G = std::max(1, std::min((A.nslices + SPMV_AT / 32 - 1) / (SPMV_AT / 32), num_sms() * ps));
+        k_spmv_async<V><<<G, SPMV_AT, sm, st>>>(A.n, A.nslices, A.sl_ptr.get(), A.sl_w.get(), A.col.get(), val, x, y);
+    } else if (v == 0 || v == SPMV_RING) {
         k_spmv_stream<V><<<(A.n + 255) / 256, 256, 0, st>>>(A.n, A.sl_ptr.get(), A.sl_w.get(), A.col.get(), val, x, y);
     } else {
         int per_sm = v >= 10 ? v / 10 : 8;   // blocks of 256 per SM

@@ -1,9 +1,10 @@
 """The standalone SpMV forms give the same y bit for bit.
 
 The persistent ring product (matrix tiles streamed through shared memory by bulk
-copies, x gathered one tile ahead) against the one-row-per-thread kernel and a
-numpy CSR product, on ragged sizes, rows wider than the six gathers held in
-registers, and rows too wide for a ring slot (read from global memory).
+copies, x gathered one tile ahead) and the per-warp cp.async pipeline against the
+one-row-per-thread kernel and a numpy CSR product, on ragged sizes, rows wider
+than the gathers held in registers or the staged width, and rows too wide for a
+ring slot (read from global memory).
 """
 import numpy as np
 import pytest
@@ -45,7 +46,8 @@ def _numpy_spmv(rowptr, col, val, x):
     (40003, 1, 9, ()),          # ragged slices, widths past the register gathers
     (20000, 5, 5, ()),          # tet-like, uniform width
     (31, 1, 4, ()),             # one partial slice
-    (5000, 2, 7, (17, 4321)),   # two rows of 300 entries: the matrix is read from global memory
+    (5000, 2, 7, (17, 4321)),   # two rows of 300 entries: read from global memory by both forms
+    (3000, 7, 12, ()),          # slices wider than the staged width of the cp.async form
 ])
 def test_ring_matches_stream(n, wmin, wmax, wide):
     rowptr, col, val = _random_csr(n, wmin, wmax, seed=n + wmax, wide_rows=wide)
@@ -55,13 +57,17 @@ def test_ring_matches_stream(n, wmin, wmax, wide):
     set_spmv_variant(100)
     y1 = csr_spmv(rowptr, col, val, x)
     assert np.array_equal(y0, y1)
+    set_spmv_variant(200)
+    y2 = csr_spmv(rowptr, col, val, x)
+    assert np.array_equal(y0, y2)
     if n <= 20000:
         ref = _numpy_spmv(rowptr, col, val, x)
         np.testing.assert_allclose(y1, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
 
 
-def test_single_row_and_empty():
-    set_spmv_variant(100)
+@pytest.mark.parametrize("variant", [100, 200])
+def test_single_row_and_empty(variant):
+    set_spmv_variant(variant)
     y = csr_spmv(np.array([0, 1], np.int32), np.array([0], np.int32), np.array([2.5]), np.array([4.0]))
     assert y.tolist() == [10.0]
     y = csr_spmv(np.array([0], np.int32), np.zeros(0, np.int32), np.zeros(0), np.zeros(0))
