@@ -180,11 +180,13 @@ long sysu_solver_matrix(sysu_solver *s, const char *which, int *rowptr, int *col
  * The Krylov kernels of the SIMPLE path applied to a host CSR matrix (0-based,
  * any column order).  method: 0 CG, 1 BiCGSTAB, 2 CG with FP32 recurrences and
  * FP64 reliable updates (Jacobi only; iters = FP32 iterations), 3 GMRES(10)
- * right preconditioned; precond: 0 none, 1 Jacobi (y = omega D^-1 c), 2 SSOR(omega),
+ * right preconditioned, 4 BiCGSTAB with FP32 inner iterations in FP64 defect
+ * correction (none or Jacobi; iters = FP32 iterations); precond: 0 none, 1 Jacobi (y = omega D^-1 c), 2 SSOR(omega),
  * 3 ILU(0) (level-scheduled sweeps; not with BiCGSTAB).  Stopping test ||b - A x||_2 / ||b||_2 < eps, as the
  * reference's SolveLinearEqu (tools.cpp:56-64) expects.  x: x0 in, solution out.
  * status: 0 converged, 1 max iterations, 2 breakdown, 3 barrier timeout,
- * 4 non-finite. */
+ * 4 non-finite (a mixed solve whose FP32 refinement stalls is finished by the
+ * FP64 method from its current x; the status is then the FP64 one). */
 int sysu_csr_solve(int method, int precond, int n, const int *rowptr, const int *col, const double *val,
                    const double *b, double *x, int maxit, double eps, double omega, int *iters, double *res,
                    int *status);

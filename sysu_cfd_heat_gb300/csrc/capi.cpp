@@ -177,6 +177,8 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
         if (value != 0.0 && (o.ke.kind != sysu::SK_BICGSTAB || o.t.kind != sysu::SK_BICGSTAB ||
                              o.ke.precond > sysu::PK_JACOBI || o.t.precond > sysu::PK_JACOBI))
             return set_err(SYSU_ERR_INPUT, "scalars_batched runs k, eps and T with BiCGSTAB + Jacobi");
+        if (value != 0.0 && (o.ke.mixed || o.t.mixed))
+            return set_err(SYSU_ERR_INPUT, "scalars_batched solves k, eps and T in FP64; turn ke.mixed / t.mixed off first");
         o.scalars_batched = value != 0.0;
         return SYSU_OK;
     }
@@ -213,10 +215,14 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
             if (f == "maxit") { e->maxit = (int)value; return SYSU_OK; }
             if (f == "omega") { e->omega = value; return SYSU_OK; }
             if (f == "mixed") {
-                if (value != 0.0 && e->kind != sysu::SK_CG)
-                    return set_err(SYSU_ERR_INPUT, "mixed precision is available for CG solves (p, ts)");
-                if (value != 0.0 && e->precond != sysu::PK_JACOBI)
+                if (value != 0.0 && e == &o.mom)
+                    return set_err(SYSU_ERR_INPUT, "mixed precision is available for p, ke, t and ts (not momentum)");
+                if (value != 0.0 && e->kind == sysu::SK_GMRES)
+                    return set_err(SYSU_ERR_INPUT, "mixed precision is available for CG and BiCGSTAB solves");
+                if (value != 0.0 && e->kind == sysu::SK_CG && e->precond != sysu::PK_JACOBI)
                     return set_err(SYSU_ERR_INPUT, "the mixed-precision CG uses the Jacobi preconditioner");
+                if (value != 0.0 && o.scalars_batched && (e == &o.ke || e == &o.t))
+                    return set_err(SYSU_ERR_INPUT, "scalars_batched solves k, eps and T in FP64; turn it off first");
                 e->mixed = value != 0.0;
                 return SYSU_OK;
             }
@@ -230,7 +236,7 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
                     return set_err(SYSU_ERR_INPUT, "the perfect-gas p' matrix is not symmetric");
                 if (kind == sysu::SK_BICGSTAB && e->precond > sysu::PK_JACOBI)
                     return set_err(SYSU_ERR_INPUT, "BiCGSTAB runs with no or the Jacobi preconditioner");
-                if (kind != sysu::SK_CG) e->mixed = 0;
+                if (kind == sysu::SK_GMRES) e->mixed = 0;
                 e->kind = kind;
                 return SYSU_OK;
             }

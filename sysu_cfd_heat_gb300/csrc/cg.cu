@@ -79,6 +79,9 @@ struct CgPipeArgs {
     double eps, inner_tol;
     unsigned long long *ts;
     CgPlan plan;
+    // FP64 kernel behind a mixed solve: run only if gate->status[0] is
+    // DEV_STALLED (the iterations of both are reported); null: always run
+    const SolveInfo *gate;
 };
 
 __shared__ uint64_t g_full[CopyRing::DMAX];
@@ -481,6 +484,8 @@ __device__ __forceinline__ V s_phase(const Part &P, Ring &R, const SellView &A, 
 // ---------------------------------------------------------------------------
 // FP64
 __global__ void __launch_bounds__(CGT64, 1) k_cg_pipe(CgPipeArgs a) {
+    if (a.gate && a.gate->status[0] != DEV_STALLED) return;  // the same word for every block
+    const int it_before = a.gate ? a.gate->iters[0] : 0;
     const int n = a.A.n;
     const int tid = threadIdx.x;
     const bool prod = is_producer();
@@ -567,7 +572,7 @@ __global__ void __launch_bounds__(CGT64, 1) k_cg_pipe(CgPipeArgs a) {
         double res = sqrt(rr) / sqrt(bb);
         if (status == DEV_OK && !(rr < thr)) status = isfinite(rr) ? DEV_MAXITER : DEV_NONFINITE;
         a.info->status[0] = status;
-        a.info->iters[0] = it;
+        a.info->iters[0] = it_before + it;
         a.info->res[0] = res;
     }
 }
@@ -578,7 +583,9 @@ __global__ void __launch_bounds__(CGT64, 1) k_cg_pipe(CgPipeArgs a) {
 // residuals in hybrid Bi-CG methods", Computing 56, 1996): once the FP32
 // residual has fallen by inner_tol since the last update, e is added to the
 // FP64 solution, e is zeroed, the FP64 residual b - A x replaces the FP32 one
-// and the search direction is kept, so the Krylov process is not restarted.
+// and the search direction is kept, so the Krylov process is not restarted --
+// unless that FP64 residual norm has not halved since the previous update
+// (near FP32's rounding floor at tight tolerances), when it restarts from z.
 // Convergence is decided on that FP64 residual only.  Per-thread partial dot
 // products run in FP32 over the thread's rows; exact sums across threads.
 __global__ void __launch_bounds__(CGT32, 1) k_cg_mixed_pipe(CgPipeArgs a) {
@@ -598,35 +605,52 @@ __global__ void __launch_bounds__(CGT32, 1) k_cg_mixed_pipe(CgPipeArgs a) {
     };
     if (prod) producer_tiles(R, 0, issue, err);
 
-    // FP64 residual of the initial guess and its FP32 copy
-    double v3[3] = {0.0, 0.0, 0.0};
-    float f2 = 0.f;
+    // FP64 residual of the initial guess (kept in a.r), then its FP32 copy scaled
+    // by a power of two sig to norm ~1: the FP32 process runs in sig units
+    double v2i[2] = {0.0, 0.0};
     for (int i = R0 + tid; i < R1; i += CGT32) {
         double bi = a.b[i];
         double ri = bi - row_dot(a.A, i, a.x);
-        float rf = (float)ri, zf = dinv[i] * rf;
-        a.r32[i] = rf;
-        a.z32[i] = zf;
-        a.e32[i] = 0.f;
-        v3[0] = fma(bi, bi, v3[0]);
-        v3[1] = fma(ri, ri, v3[1]);
-        f2 = fmaf(rf, zf, f2);
+        a.r[i] = ri;
+        v2i[0] = fma(bi, bi, v2i[0]);
+        v2i[1] = fma(ri, ri, v2i[1]);
     }
-    v3[2] = (double)f2;
-    if (!grid_sum_t0<3>(v3, rc, a.gb, err)) { drain(R); return; }
+    if (!grid_sum_t0<2>(v2i, rc, a.gb, err)) { drain(R); return; }
     // thread-0 scalar state, kept in shared memory (no registers in the other threads);
-    // rr_ref: FP64 ||b - A x||^2 at the last reliable update
-    __shared__ double s_state[4];
-    double &bb = s_state[0], &thr = s_state[1], &rho = s_state[2], &rr_ref = s_state[3];
+    // rr_ref: FP64 ||b - A x||^2 at the last reliable update; sig: the scale of the
+    // FP32 vectors (r32 = sig r), sig_next: the scale after the next update
+    __shared__ double s_state[6];
+    __shared__ int s_stalls;  // consecutive updates that did not halve the FP64 residual norm
+    double &bb = s_state[0], &thr = s_state[1], &rho = s_state[2], &rr_ref = s_state[3], &sig = s_state[4],
+           &sig_next = s_state[5];
     if (tid == 0) {
-        bb = v3[0] == 0.0 ? 1.0 : v3[0];
+        bb = v2i[0] == 0.0 ? 1.0 : v2i[0];
         thr = a.eps * a.eps * bb;
-        rr_ref = v3[1];
-        rho = v3[2];
-        g_bc[0] = stop_code(rr_ref, thr);
-        g_bc[1] = 0.0;
+        rr_ref = v2i[1];
+        sig = pow2_scale(rr_ref);
+        s_stalls = 0;
+        g_bc[5] = sig;
     }
     __syncthreads();
+    {
+        const double sg = g_bc[5];
+        float f2 = 0.f;
+        for (int i = R0 + tid; i < R1; i += CGT32) {
+            float rf = (float)(sg * a.r[i]), zf = dinv[i] * rf;
+            a.r32[i] = rf;
+            a.z32[i] = zf;
+            a.e32[i] = 0.f;
+            f2 = fmaf(rf, zf, f2);
+        }
+        double v1[1] = {(double)f2};
+        if (!grid_sum_t0<1>(v1, rc, a.gb, err)) { drain(R); return; }
+        if (tid == 0) {
+            rho = v1[0];
+            g_bc[0] = stop_code(rr_ref, thr);
+            g_bc[1] = 0.0;
+        }
+        __syncthreads();
+    }
 
     long long base = 0;
     int total = 0, nupd = 0, status = DEV_OK;
@@ -636,6 +660,7 @@ __global__ void __launch_bounds__(CGT32, 1) k_cg_mixed_pipe(CgPipeArgs a) {
         __syncthreads();
         if (code == 1.0 || total >= a.maxit) break;
         if (code == 2.0) { status = DEV_NONFINITE; break; }
+        if (code == 3.0) { status = DEV_STALLED; break; }
         ++total;
         stamp(a.ts, total, 0);
         float g0 = 0.f;
@@ -701,18 +726,25 @@ __global__ void __launch_bounds__(CGT32, 1) k_cg_mixed_pipe(CgPipeArgs a) {
         if (tid == 0) {
             // reliable update once the FP32 residual fell by inner_tol since the
             // last one, when it looks converged, or at the iteration cap
-            const double d2 = a.inner_tol * a.inner_tol;
-            bool upd = w2[0] <= d2 * rr_ref || w2[0] <= thr || total >= a.maxit || !(w2[0] == w2[0]);
+            // (the FP32 sums are in sig^2 units)
+            const double d2 = a.inner_tol * a.inner_tol, s2 = sig * sig;
+            bool upd = w2[0] <= d2 * rr_ref * s2 || w2[0] <= thr * s2 || total >= a.maxit || !(w2[0] == w2[0]);
             if (!upd) {
                 g_bc[1] = w2[1] / rho;
                 rho = w2[1];
+            } else {
+                // the next scale from the FP32 estimate of the new residual
+                sig_next = sig * pow2_scale(w2[0]);
+                g_bc[5] = 1.0 / sig;  // x += e / sig (a power of two: exact)
+                g_bc[6] = sig_next;
             }
             g_bc[4] = upd ? 1.0 : 0.0;
         }
         __syncthreads();
         if (g_bc[4] != 0.0) {
+            const double isg = g_bc[5], sn = g_bc[6];
             for (int i = R0 + tid; i < R1; i += CGT32) {
-                a.x[i] += (double)a.e32[i];
+                a.x[i] += (double)a.e32[i] * isg;
                 a.e32[i] = 0.f;
             }
             if (!grid_sync(a.gb, err)) break;
@@ -720,7 +752,7 @@ __global__ void __launch_bounds__(CGT32, 1) k_cg_mixed_pipe(CgPipeArgs a) {
             float fz = 0.f;
             for (int i = R0 + tid; i < R1; i += CGT32) {
                 double ri = a.b[i] - row_dot(a.A, i, a.x);
-                float rf = (float)ri, zf = dinv[i] * rf;
+                float rf = (float)(sn * ri), zf = dinv[i] * rf;
                 a.r32[i] = rf;
                 a.z32[i] = zf;
                 u[0] = fma(ri, ri, u[0]);
@@ -729,18 +761,30 @@ __global__ void __launch_bounds__(CGT32, 1) k_cg_mixed_pipe(CgPipeArgs a) {
             u[1] = (double)fz;
             if (!grid_sum_t0<2>(u, rc, a.gb, err)) break;
             if (tid == 0) {
+                // keep the direction (beta from the replaced residual) while the
+                // updates make progress; once the FP64 residual norm has not at
+                // least halved since the last update (the FP32 recurrence has met
+                // its rounding floor), restart it from z: beta = 0
+                // beta in the new units: (rho_new / rho_old) (sig / sig_next), so
+                // that the kept p and q (in sig units) scale with the new r
+                const bool stalled = !(u[0] < 0.25 * rr_ref);
+                s_stalls = stalled ? s_stalls + 1 : 0;
                 rr_ref = u[0];
                 g_bc[0] = stop_code(rr_ref, thr);
-                g_bc[1] = u[1] / rho;  // keep the direction: beta from the replaced residual
+                if (g_bc[0] == 0.0 && s_stalls >= 3) g_bc[0] = 3.0;  // hand over to FP64
+                g_bc[1] = stalled ? 0.0 : (u[1] / rho) * (sig / sig_next);
                 rho = u[1];
+                sig = sig_next;
                 ++nupd;
             }
             __syncthreads();
         }
     }
     drain(R);
-    if (status == DEV_BREAKDOWN)  // keep the correction gathered so far
-        for (int i = R0 + tid; i < R1; i += CGT32) a.x[i] += (double)a.e32[i];
+    if (status == DEV_BREAKDOWN) {  // keep the correction gathered so far
+        const double isg = 1.0 / s_state[4];
+        for (int i = R0 + tid; i < R1; i += CGT32) a.x[i] += (double)a.e32[i] * isg;
+    }
     if (blockIdx.x == 0 && tid == 0) {
         double res = sqrt(rr_ref) / sqrt(bb);
         if (status == DEV_OK && !(rr_ref < thr)) status = isfinite(rr_ref) ? DEV_MAXITER : DEV_NONFINITE;
@@ -821,8 +865,11 @@ int cg_grid(const SellDev &A, const CgPlan &pl, int maxb, int sm_cap) {
 
 }  // namespace
 
-void cg_solve(const SellDev &A, const double *val, const double *b, double *x, bool x0_zero,
-              const KrylovOpts &o, KrylovWork &w, SolveInfo *info, cudaStream_t st) {
+// The FP64 persistent CG.  gate: see CgPipeArgs (then x is not zeroed and
+// info is not cleared: the solve continues the mixed one's).
+static void cg_launch64(const SellDev &A, const double *val, const double *b, double *x, bool x0_zero,
+                        const KrylovOpts &o, KrylovWork &w, SolveInfo *info, const SolveInfo *gate,
+                        cudaStream_t st) {
     int n = A.n;
     if (n == 0) return;
     static int maxb = 0;
@@ -831,9 +878,10 @@ void cg_solve(const SellDev &A, const double *val, const double *b, double *x, b
     check_aligned16({val, A.col.get()});
     SellView V = view(A, val);
     { k_jacobi_dinv<<<(n + KB - 1) / KB, KB, 0, st>>>(V, o.omega, o.jacobi ? 1 : 0, w.dinv.get()); ++::sysu::g_launches; }
-    if (x0_zero) { k_zero<<<(n + KB - 1) / KB, KB, 0, st>>>(x, n); ++::sysu::g_launches; }
-    SYSU_CUDA(cudaMemsetAsync(info, 0, sizeof(SolveInfo), st));
+    if (!gate && x0_zero) { k_zero<<<(n + KB - 1) / KB, KB, 0, st>>>(x, n); ++::sysu::g_launches; }
+    if (!gate) SYSU_CUDA(cudaMemsetAsync(info, 0, sizeof(SolveInfo), st));
     CgPipeArgs a{};
+    a.gate = gate;
     a.A = V;
     a.b = b;
     a.x = x;
@@ -853,6 +901,11 @@ void cg_solve(const SellDev &A, const double *val, const double *b, double *x, b
     int G = cg_grid(A, a.plan, maxb, w.sm_cap);
     SYSU_CUDA(cudaMemsetAsync(w.barrier.get(), 0, sizeof(GridBarrier), st));  // grid_sync starts from 0
     { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_cg_pipe, dim3(G), dim3(CGT64), args, a.plan.smem, st)); ++::sysu::g_launches; }
+}
+
+void cg_solve(const SellDev &A, const double *val, const double *b, double *x, bool x0_zero,
+              const KrylovOpts &o, KrylovWork &w, SolveInfo *info, cudaStream_t st) {
+    cg_launch64(A, val, b, x, x0_zero, o, w, info, nullptr, st);
 }
 
 template <class V>
@@ -895,6 +948,7 @@ void cg_solve_mixed(const SellDev &A, const double *val, const float *val32, con
     a.val32 = val32;
     a.b = b;
     a.x = x;
+    a.r = w.r.get();  // FP64 initial residual
     a.r32 = w.r32.get();
     a.z32 = w.z32.get();
     a.p32 = w.p32.get();
@@ -913,6 +967,9 @@ void cg_solve_mixed(const SellDev &A, const double *val, const float *val32, con
     int G = cg_grid(A, a.plan, maxb, w.sm_cap);
     SYSU_CUDA(cudaMemsetAsync(w.barrier.get(), 0, sizeof(GridBarrier), st));  // grid_sync starts from 0
     { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_cg_mixed_pipe, dim3(G), dim3(CGT32), args, a.plan.smem, st)); ++::sysu::g_launches; }
+    // FP64 takes over from the current x if the FP32 refinement stalled (the
+    // launch returns at once otherwise)
+    cg_launch64(A, val, b, x, false, o, w, info, info, st);
 }
 
 }  // namespace sysu

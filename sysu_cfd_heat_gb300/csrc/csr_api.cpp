@@ -57,8 +57,11 @@ int sysu_csr_solve(int method, int precond, int n, const int *rowptr, const int 
                 const double *bb[1] = {db.get()};
                 double *xx[1] = {dx.get()};
                 sysu::bicgstab_solve(M.A, M.val.get(), 1, bb, xx, o, w, info.get(), st);
+            } else if (method == 4) {
+                if (precond > 1) throw sysu::CaseError{"BiCGSTAB runs with no or the Jacobi preconditioner"};
+                sysu::bicgstab_solve_mixed(M.A, M.val.get(), db.get(), dx.get(), o, w, info.get(), st);
             } else {
-                throw sysu::CaseError{"method: 0 CG, 1 BiCGSTAB, 2 CG-mixed, 3 GMRES"};
+                throw sysu::CaseError{"method: 0 CG, 1 BiCGSTAB, 2 CG-mixed, 3 GMRES, 4 BiCGSTAB-mixed"};
             }
             sysu::SolveInfo h;
             info.download(&h, 1, st);

@@ -85,6 +85,10 @@ enum DevStatus : int {
     DEV_BREAKDOWN = 2,
     DEV_BARRIER_TIMEOUT = 3,
     DEV_NONFINITE = 4,
+    // mixed-precision solves: three FP64 updates in a row did not halve the
+    // residual norm (FP32's rounding floor); the FP64 solve launched behind it
+    // finishes from the current x and reports its own status
+    DEV_STALLED = 5,
 };
 
 #ifdef __CUDACC__

@@ -381,6 +381,13 @@ __global__ void k_fill_x(long n, double *x64, float *x32) {
     x32[i] = (float)v;
 }
 
+// sv[e] = (float)(val[e] dinv[col e]) over all stored entries
+__global__ void k_scale_cols32(long nnz, const int *__restrict__ col, const double *__restrict__ val,
+                               const double *__restrict__ dinv, float *__restrict__ sv) {
+    long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < nnz) sv[e] = (float)(val[e] * dinv[col[e]]);
+}
+
 __global__ void k_to_fp32(long n, const double *src, float *dst) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) dst[i] = (float)src[i];
@@ -400,6 +407,9 @@ struct BicgArgs {
     SolveInfo *info;
     int maxit;
     double eps;
+    // behind a mixed solve: run only if gate->status[0] is DEV_STALLED (one
+    // system; the iterations of both are reported); null: always run
+    const SolveInfo *gate;
 };
 
 // Scalar state of a BiCGSTAB solve.  Thread 0 of every block derives it from
@@ -415,6 +425,8 @@ struct BicgState {
 
 template <int NR, bool MULTI>
 __global__ void __launch_bounds__(KB, 4) k_bicgstab(BicgArgs a) {
+    if (a.gate && a.gate->status[0] != DEV_STALLED) return;  // the same word for every block
+    const int it_before = a.gate ? a.gate->iters[0] : 0;
     const int n = a.A.n;
     const int T = gridDim.x * KB;
     const int t0 = blockIdx.x * KB + threadIdx.x;
@@ -638,9 +650,238 @@ __global__ void __launch_bounds__(KB, 4) k_bicgstab(BicgArgs a) {
             int st = S.status[c];
             if (st == DEV_OK && !(S.res[c] < a.eps)) st = isfinite(S.res[c]) ? DEV_MAXITER : DEV_NONFINITE;
             a.info->status[c] = st;
-            a.info->iters[c] = S.it[c];
+            a.info->iters[c] = S.it[c] + (c == 0 ? it_before : 0);
             a.info->res[c] = S.res[c];
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Mixed-precision BiCGSTAB for one system: FP32 inner iterations on the
+// correction equation A e = r, FP64 defect correction.  The FP32 vectors hold
+// the residual scaled by a power of two sig with sig ||r|| ~ 1 (pow2_scale),
+// so residuals that have become tiny in FP64 do not underflow in FP32.  The inner recurrences
+// are those of k_bicgstab with FP32 vectors and the column-scaled FP32 matrix
+// a_ij / m_jj (rounded from FP64); its dot products are FP32 over a thread's
+// rows and summed across threads in FP64.  Once the FP32 residual has fallen
+// by inner_tol since the last update (or s is that small already, or a
+// recurrence breaks down), x += M^-1 e in FP64, the FP64 residual b - A x
+// replaces r and the inner process restarts from it.  Convergence is decided
+// on that FP64 residual only: ||b - A x|| / ||b|| < eps, the test of the FP64
+// solve.  Three updates in a row that do not lower the FP64 residual end it
+// with DEV_STALLED, and the FP64 BiCGSTAB launched behind it continues from x.  info->iters counts inner iterations,
+// info->refinements the FP64 updates.
+struct BicgMixedArgs {
+    SellView A;            // FP64 values (residuals)
+    const float *sv32;     // FP32 column-scaled values
+    const double *b;
+    double *x;
+    const double *dinv;    // FP64 Jacobi diagonal inverse
+    double *r64;           // FP64 residual scratch
+    float *r, *rt, *p, *v, *s, *t, *e;  // in units of sig (a power of two, sig ||r|| ~ 1)
+    double *partials;
+    GridBarrier *gb;
+    SolveInfo *info;
+    int maxit;
+    double eps, inner_tol;
+};
+
+struct BicgMixedState {
+    double bb, thr, rr64, rr_ref, r0in, rho, rho_prev, alpha, omg, beta, snorm2, sig;
+    int it, inner, status, upd, stall, act, early, done;
+};
+
+// y = A_s x over FP32 column-scaled values, one row (FMA order of row_dot_scaled)
+__device__ __forceinline__ float row_dot32(const SellView &A, const float *__restrict__ sv, int i,
+                                           const float *__restrict__ x) {
+    const int s = i >> 5;
+    int e = A.sl_ptr[s] + (i & 31);
+    const int w = A.sl_w[s];
+    float y = 0.f;
+    for (int k = 0; k < w; ++k, e += 32) y = fmaf(sv[e], x[A.col[e]], y);
+    return y;
+}
+
+__global__ void __launch_bounds__(KB, 4) k_bicgstab_mixed(BicgMixedArgs a) {
+    const int n = a.A.n;
+    const int T = gridDim.x * KB;
+    const int t0 = blockIdx.x * KB + threadIdx.x;
+    const bool lead = threadIdx.x == 0;
+    int *err = &a.info->err;
+    RedCtx rc{a.partials, (int)gridDim.x, 0};
+    __shared__ BicgMixedState S;
+    // FP64 residual of x into r (FP32), rt = r, e = p = v = 0; ||b||^2 (first
+    // call) and ||b - A x||^2.  The lead thread then restarts the inner process.
+    auto residual = [&](bool first) -> bool {
+        double v2[2] = {0.0, 0.0}, rf2 = 0.0;
+        for (int i = t0; i < n; i += T) {
+            const double bi = a.b[i];
+            const double ri = bi - row_dot(a.A, i, a.x);
+            a.r64[i] = ri;
+            if (first) v2[0] = fma(bi, bi, v2[0]);
+            v2[1] = fma(ri, ri, v2[1]);
+        }
+        if (!grid_reduce_t0<2>(v2, rc, a.gb, err)) return false;
+        if (lead) S.sig = pow2_scale(v2[1]);  // the FP32 vectors hold sig r (exact scaling)
+        __syncthreads();
+        {
+            const double sg = S.sig;
+            float f2 = 0.f;
+            for (int i = t0; i < n; i += T) {
+                const float rf = (float)(sg * a.r64[i]);
+                a.r[i] = rf;
+                a.rt[i] = rf;
+                a.e[i] = 0.f;
+                a.p[i] = 0.f;
+                a.v[i] = 0.f;
+                f2 = fmaf(rf, rf, f2);
+            }
+            double v1[1] = {(double)f2};
+            if (!grid_reduce_t0<1>(v1, rc, a.gb, err)) return false;
+            rf2 = v1[0];
+        }
+        if (lead) {
+            if (first) {
+                S.bb = v2[0] == 0.0 ? 1.0 : v2[0];
+                S.thr = a.eps * a.eps * S.bb;
+                S.it = 0;
+                S.upd = 0;
+                S.stall = 0;
+                S.status = DEV_OK;
+                S.done = 0;
+                S.rr_ref = v2[1];
+            } else {
+                ++S.upd;
+                S.stall = v2[1] < S.rr_ref ? 0 : S.stall + 1;
+                S.rr_ref = fmin(S.rr_ref, v2[1]);
+            }
+            S.rr64 = v2[1];
+            S.r0in = rf2;
+            S.rho = rf2;  // rt . r with rt = r, in the FP32 inner precision (sig^2 units)
+            S.rho_prev = S.alpha = S.omg = 1.0;
+            S.inner = 0;
+            if (!isfinite(v2[1])) { S.status = DEV_NONFINITE; S.done = 1; }
+            else if (v2[1] < S.thr) S.done = 1;
+            else if (S.stall >= 3) { S.status = DEV_STALLED; S.done = 1; }  // FP64 takes over
+            else if (S.it >= a.maxit) { S.status = DEV_MAXITER; S.done = 1; }
+        }
+        __syncthreads();
+        return true;
+    };
+    // x += M^-1 e / sig in FP64, then the FP64 residual
+    auto update = [&]() -> bool {
+        const double isg = 1.0 / S.sig;
+        for (int i = t0; i < n; i += T) a.x[i] = fma(a.dinv[i] * isg, (double)a.e[i], a.x[i]);
+        if (!grid_sync(a.gb, err)) return false;
+        return residual(false);
+    };
+    if (!residual(true)) return;
+    const float *__restrict__ sv = a.sv32;
+    const double d2 = a.inner_tol * a.inner_tol;
+    for (;;) {
+        if (S.done) break;
+        // p = r + beta (p - omega v)
+        if (lead) {
+            ++S.it;
+            ++S.inner;
+            S.beta = S.inner == 1 ? 0.0 : (S.rho / S.rho_prev) * (S.alpha / S.omg);
+        }
+        __syncthreads();
+        {
+            const float beta = (float)S.beta, omg = (float)S.omg;
+            const bool first = S.inner == 1;
+            for (int i = t0; i < n; i += T)
+                a.p[i] = first ? a.r[i] : fmaf(beta, fmaf(-omg, a.v[i], a.p[i]), a.r[i]);
+        }
+        if (!grid_sync(a.gb, err)) return;
+        // v = A M^-1 p ; rt . v
+        {
+            float f = 0.f;
+            for (int i = t0; i < n; i += T) {
+                const float y = row_dot32(a.A, sv, i, a.p);
+                a.v[i] = y;
+                f = fmaf(a.rt[i], y, f);
+            }
+            double red[1] = {(double)f};
+            if (!grid_reduce_t0<1>(red, rc, a.gb, err)) return;
+            if (lead) {
+                S.act = red[0] != 0.0;  // 0: the recurrence broke down, update and restart
+                if (S.act) S.alpha = S.rho / red[0];
+            }
+            __syncthreads();
+        }
+        if (!S.act) {
+            if (!update()) return;
+            continue;
+        }
+        // s = r - alpha v ; ||s||
+        {
+            const float alpha = (float)S.alpha;
+            float f = 0.f;
+            for (int i = t0; i < n; i += T) {
+                const float si = fmaf(-alpha, a.v[i], a.r[i]);
+                a.s[i] = si;
+                f = fmaf(si, si, f);
+            }
+            double red[1] = {(double)f};
+            if (!grid_reduce_t0<1>(red, rc, a.gb, err)) return;
+            if (lead) {
+                S.snorm2 = red[0];
+                S.early = red[0] <= d2 * S.r0in;
+            }
+            __syncthreads();
+        }
+        if (S.early) {  // e += alpha p, then the FP64 update
+            const float alpha = (float)S.alpha;
+            for (int i = t0; i < n; i += T) a.e[i] = fmaf(alpha, a.p[i], a.e[i]);
+            if (!update()) return;
+            continue;
+        }
+        // t = A M^-1 s ; t.s, t.t
+        {
+            float f0 = 0.f, f1 = 0.f;
+            for (int i = t0; i < n; i += T) {
+                const float y = row_dot32(a.A, sv, i, a.s);
+                a.t[i] = y;
+                f0 = fmaf(y, a.s[i], f0);
+                f1 = fmaf(y, y, f1);
+            }
+            double red[2] = {(double)f0, (double)f1};
+            if (!grid_reduce_t0<2>(red, rc, a.gb, err)) return;
+            if (lead) S.omg = red[1] != 0.0 ? red[0] / red[1] : 0.0;
+            __syncthreads();
+        }
+        // e += alpha p + omega s ; r = s - omega t ; r.r, rt.r
+        {
+            const float alpha = (float)S.alpha, omg = (float)S.omg;
+            float f0 = 0.f, f1 = 0.f;
+            for (int i = t0; i < n; i += T) {
+                const float si = a.s[i];
+                a.e[i] = fmaf(alpha, a.p[i], fmaf(omg, si, a.e[i]));
+                const float ri = fmaf(-omg, a.t[i], si);
+                a.r[i] = ri;
+                f0 = fmaf(ri, ri, f0);
+                f1 = fmaf(a.rt[i], ri, f1);
+            }
+            double red[2] = {(double)f0, (double)f1};
+            if (!grid_reduce_t0<2>(red, rc, a.gb, err)) return;
+            if (lead) {
+                S.rho_prev = S.rho;
+                S.rho = red[1];
+                // FP64 update once the FP32 residual fell by inner_tol, at the
+                // iteration cap, or when the next step would divide by zero
+                S.act = !(red[0] <= d2 * S.r0in || S.it >= a.maxit || S.omg == 0.0 || S.rho == 0.0 ||
+                          !(red[0] == red[0]));
+            }
+            __syncthreads();
+        }
+        if (!S.act && !update()) return;
+    }
+    if (blockIdx.x == 0 && lead) {
+        a.info->status[0] = S.status;
+        a.info->iters[0] = S.it;
+        a.info->res[0] = sqrt(S.rr64) / sqrt(S.bb);
+        a.info->refinements = S.upd;
     }
 }
 
@@ -750,7 +991,8 @@ static int bicg_max_blocks(int nrhs, bool multi) {
 }
 
 static void bicg_launch(const SellDev &A, const double *const *vals, bool multi, int nrhs, const double *const *b,
-                        double *const *x, const KrylovOpts &o, KrylovWork &w, SolveInfo *info, cudaStream_t st) {
+                        double *const *x, const KrylovOpts &o, KrylovWork &w, SolveInfo *info, cudaStream_t st,
+                        const SolveInfo *gate = nullptr) {
     int n = A.n;
     int maxb = bicg_max_blocks(nrhs, multi);
     if (w.sm_cap > 0) maxb = std::min(maxb, w.sm_cap * std::max(1, maxb / num_sms()));
@@ -767,8 +1009,9 @@ static void bicg_launch(const SellDev &A, const double *const *vals, bool multi,
             ++::sysu::g_launches;
         }
     }
-    SYSU_CUDA(cudaMemsetAsync(info, 0, sizeof(SolveInfo), st));
+    if (!gate) SYSU_CUDA(cudaMemsetAsync(info, 0, sizeof(SolveInfo), st));
     BicgArgs a{};
+    a.gate = gate;
     a.A = view(A, vals[0]);
     for (int c = 0; c < 3; ++c) {
         a.vals[c] = vals[multi ? std::min(c, nrhs - 1) : 0];
@@ -798,6 +1041,56 @@ void bicgstab_solve(const SellDev &A, const double *val, int nrhs, const double 
     if (nrhs != 1 && nrhs != 3) throw CaseError{"bicgstab_solve: use 1 or 3 right-hand sides"};
     const double *vals[1] = {val};
     bicg_launch(A, vals, false, nrhs, b, x, o, w, info, st);
+}
+
+void bicgstab_solve_mixed(const SellDev &A, const double *val, const double *b, double *x, const KrylovOpts &o,
+                          KrylovWork &w, SolveInfo *info, cudaStream_t st) {
+    const int n = A.n;
+    if (n == 0) return;
+    static int maxb = 0;
+    if (!maxb) maxb = coresident_blocks(k_bicgstab_mixed);
+    int mb = maxb;
+    if (w.sm_cap > 0) mb = std::min(mb, w.sm_cap * std::max(1, maxb / num_sms()));
+    w.ensure(n, 1, std::max(bicg_max_blocks(-1, false), maxb), st);
+    w.ensure32(n, st);
+    if (w.rt32.size() < (size_t)n) {
+        w.rt32.alloc(n); w.v32.alloc(n); w.s32.alloc(n); w.t32.alloc(n);
+    }
+    if (w.sval32.size() < (size_t)A.nnz) w.sval32.alloc(A.nnz);
+    SellView V = view(A, val);
+    { k_jacobi_dinv<<<(n + KB - 1) / KB, KB, 0, st>>>(V, o.omega, o.jacobi ? 1 : 0, w.dinv.get()); ++::sysu::g_launches; }
+    if (A.nnz > 0) {
+        k_scale_cols32<<<(unsigned)((A.nnz + KB - 1) / KB), KB, 0, st>>>(A.nnz, A.col.get(), val, w.dinv.get(),
+                                                                        w.sval32.get());
+        ++::sysu::g_launches;
+    }
+    SYSU_CUDA(cudaMemsetAsync(info, 0, sizeof(SolveInfo), st));
+    BicgMixedArgs a{};
+    a.A = V;
+    a.sv32 = w.sval32.get();
+    a.b = b;
+    a.x = x;
+    a.dinv = w.dinv.get();
+    a.r64 = w.r.get();
+    a.r = w.r32.get(); a.rt = w.rt32.get(); a.p = w.p32.get(); a.v = w.v32.get();
+    a.s = w.s32.get(); a.t = w.t32.get(); a.e = w.e32.get();
+    a.partials = w.partials.get();
+    a.gb = w.barrier.get();
+    a.info = info;
+    a.maxit = o.maxit;
+    a.eps = o.eps;
+    a.inner_tol = o.inner_tol;
+    void *args[] = {&a};
+    const int G = grid_for(n, mb);
+    SYSU_CUDA(cudaMemsetAsync(w.barrier.get(), 0, sizeof(GridBarrier), st));  // grid_sync starts from 0
+    SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_bicgstab_mixed, dim3(G), dim3(KB), args, 0, st));
+    ++::sysu::g_launches;
+    // FP64 takes over from the current x if the FP32 refinement stalled (the
+    // launch returns at once otherwise)
+    const double *bb[1] = {b};
+    double *xx[1] = {x};
+    const double *vv[1] = {val};
+    bicg_launch(A, vv, false, 1, bb, xx, o, w, info, st, info);
 }
 
 void bicgstab_solve_multi(const SellDev &A, const double *const *vals, const double *const *b, double *const *x,

@@ -76,6 +76,7 @@ struct KrylovWork {
     DevBuf<double> r, rt, p, v, s, t, dinv, partials;
     DevBuf<double> sval;  // BiCGSTAB: matrix values scaled by the Jacobi diagonal inverse of their column
     DevBuf<float> r32, z32, p32, q32, e32, dinv32;  // mixed-precision inner solve
+    DevBuf<float> rt32, v32, s32, t32, sval32;      // mixed BiCGSTAB (with r32, p32, e32)
     DevBuf<double> gV, gZ, gW, ilu;                  // GMRES basis, preconditioned basis, ILU(0) factors
     DevBuf<long long> gpart;                         // exact multi-value partial sums
     DevBuf<GridBarrier> barrier;
@@ -136,6 +137,13 @@ void cg_solve(const SellDev &A, const double *val, const double *b, double *x, b
 // BiCGSTAB on nrhs (1..3) right-hand sides sharing one matrix; b[c], x[c].
 void bicgstab_solve(const SellDev &A, const double *val, int nrhs, const double *const *b, double *const *x,
                     const KrylovOpts &o, KrylovWork &w, SolveInfo *info_dev, cudaStream_t st);
+
+// BiCGSTAB for one system with FP32 inner iterations (column-scaled FP32 matrix,
+// Jacobi) in FP64 defect correction: x += M^-1 e and the FP64 residual b - A x
+// once the FP32 residual fell by o.inner_tol; stops on ||b - A x|| / ||b|| < eps.
+// x holds x0 on entry.
+void bicgstab_solve_mixed(const SellDev &A, const double *val, const double *b, double *x, const KrylovOpts &o,
+                          KrylovWork &w, SolveInfo *info_dev, cudaStream_t st);
 
 // BiCGSTAB on three systems with one sparsity pattern and their own values
 // vals[c] (and Jacobi diagonals), in one launch: the column indices are read

@@ -176,6 +176,17 @@ __device__ __forceinline__ bool grid_sum_t0(double (&v)[NV], RedCtx &rc, GridBar
 // scalars broadcast from thread 0 to the block
 __shared__ double g_bc[8];
 
+// A power of two s with s^2 rr in [1, 4) (1 when rr is zero or not finite).
+// The FP32 inner solves of the mixed-precision forms work on s r, so residuals
+// that have become tiny (or huge) in FP64 neither underflow nor overflow in
+// FP32; scaling by a power of two is exact.
+__device__ __forceinline__ double pow2_scale(double rr) {
+    if (!(rr > 0.0) || !isfinite(rr)) return 1.0;
+    const int e = ilogb(rr);
+    const int h = e >= 0 ? e / 2 : -((1 - e) / 2);  // floor(e / 2)
+    return ldexp(1.0, -h);
+}
+
 // One SELL row: the loads of four entries are issued before their FMAs, so a
 // thread keeps several independent gathers in flight (rows hold 4-7 entries).
 __device__ __forceinline__ double row_dot(const SellView &A, int i, const double *__restrict__ x) {

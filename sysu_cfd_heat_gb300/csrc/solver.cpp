@@ -422,6 +422,12 @@ void SimpleSolver::solve(int slot, const EqOpts &o, const SellDev &A, const doub
     }
     if (x0_zero)
         for (int c = 0; c < nrhs; ++c) launch_fill(x[c], 0.0, A.n, st);
+    if (o.mixed) {
+        if (nrhs != 1) throw CaseError{"mixed-precision BiCGSTAB solves one right-hand side"};
+        ko.inner_tol = o.inner_tol;
+        bicgstab_solve_mixed(A, val, b[0], x[0], ko, kw, info, st);
+        return;
+    }
     if (nrhs == 3 && !opt.mom_batched) {
         for (int c = 0; c < 3; ++c) bicgstab_solve(A, val, 1, &b[c], &x[c], ko, kw, infos.get() + SLOT_N + c, st);
         return;
