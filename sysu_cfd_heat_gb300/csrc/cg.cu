@@ -968,8 +968,11 @@ void cg_solve_mixed(const SellDev &A, const double *val, const float *val32, con
     SYSU_CUDA(cudaMemsetAsync(w.barrier.get(), 0, sizeof(GridBarrier), st));  // grid_sync starts from 0
     { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_cg_mixed_pipe, dim3(G), dim3(CGT32), args, a.plan.smem, st)); ++::sysu::g_launches; }
     // FP64 takes over from the current x if the FP32 refinement stalled (the
-    // launch returns at once otherwise)
-    cg_launch64(A, val, b, x, false, o, w, info, info, st);
+    // launch returns at once otherwise).  Not for solves capped to a share of
+    // the SMs (cases of one CUDA graph): there a cooperative launch that needs
+    // whole SMs waits for room and holds up the graph's other branches, and a
+    // stalled solve reports DEV_STALLED instead.
+    if (w.sm_cap <= 0) cg_launch64(A, val, b, x, false, o, w, info, info, st);
 }
 
 }  // namespace sysu
