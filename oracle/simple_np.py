@@ -467,6 +467,31 @@ class Domain:
         return gr
 
 
+    # Least-squares gradient -- not the reference's (it has Green-Gauss only,
+    # BasicSolver.cpp:29-77): the GPU implementation's option "gradient" 1, restated
+    # here as its CPU check.  grad phi_c solves sum_j w_j d_j d_j^T g = sum_j w_j d_j
+    # (phi_j - phi_c) over the cell's faces, d_j from the cell centroid to the
+    # neighbour's centroid (interior face) or to the face centroid (boundary face,
+    # phi_j the boundary value), w_j = 1 / |d_j|^2.
+    def gradient_lsq(self, phi, bphi):
+        m, g = self.m, self.g
+        M = np.zeros((self.nc, 3, 3))
+        rhs = np.zeros((self.nc, 3))
+        inn = self.inner
+        for c, o in ((m.c1[inn], m.c2[inn]), (m.c2[inn], m.c1[inn])):
+            d = g.cx[o] - g.cx[c]
+            w = 1. / _dot3(d, d)
+            np.add.at(M, c, w[:, None, None] * d[:, :, None] * d[:, None, :])
+            np.add.at(rhs, c, (w * (phi[o] - phi[c]))[:, None] * d)
+        bf = m.bface
+        c = m.c1[bf]
+        d = g.fx[bf] - g.cx[c]
+        w = 1. / _dot3(d, d)
+        np.add.at(M, c, w[:, None, None] * d[:, :, None] * d[:, None, :])
+        np.add.at(rhs, c, (w * (bphi - phi[c]))[:, None] * d)
+        return np.linalg.solve(M, rhs[:, :, None])[:, :, 0]
+
+
 class SimpleNP:
     """The reference's NavierStokesSolver + HeatConductionSolver, restated."""
 

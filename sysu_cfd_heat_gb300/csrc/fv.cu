@@ -207,6 +207,109 @@ __global__ void __launch_bounds__(NB) k_gradient_v(DomView d, GradPtrs p) {
 }
 
 // ---------------------------------------------------------------------------
+// Least-squares gradients (an option beside the reference's Green-Gauss one):
+// grad phi_c = M^-1 sum_j w_j d_j (phi_j - phi_c) over the cell's faces, phi_j the
+// neighbour's value or the boundary value, d_j from the cell centroid to the
+// neighbour's centroid or the boundary face's, w_j = 1 / |d_j|^2.  Exact for
+// linear fields.  The geometry part c_j = M^-1 w_j d_j is computed once.
+__device__ __forceinline__ void lsq_offset(const DomView &d, int i, int f, int nb, double &d0, double &d1,
+                                           double &d2) {
+    double x0, x1, x2;
+    if (nb >= 0 && (nb & SS_BND)) {
+        x0 = d.fx[f];
+        x1 = d.fx[d.nf + f];
+        x2 = d.fx[2 * d.nf + f];
+    } else {
+        const int o = nb & 0x7FFFFFFF;
+        x0 = d.cx[o];
+        x1 = d.cx[d.nc + o];
+        x2 = d.cx[2 * d.nc + o];
+    }
+    d0 = x0 - d.cx[i];
+    d1 = x1 - d.cx[d.nc + i];
+    d2 = x2 - d.cx[2 * d.nc + i];
+}
+
+__global__ void __launch_bounds__(NB) k_lsq_setup(DomView d, double *c) {
+    const int i = blockIdx.x * NB + threadIdx.x;
+    if (i >= d.nc) return;
+    const int base = d.ss_ptr[i >> 5] + (i & 31), w = d.ss_w[i >> 5];
+    double a = 0, b = 0, cc = 0, dd = 0, e = 0, ff = 0;  // M = [a b cc; b dd e; cc e ff]
+    for (int j = 0; j < w; ++j) {
+        const int f = d.ss_f[base + 32 * j];
+        if (f < 0) continue;
+        double d0, d1, d2;
+        lsq_offset(d, i, f, d.ss_n[base + 32 * j], d0, d1, d2);
+        const double wt = 1.0 / (d0 * d0 + d1 * d1 + d2 * d2);
+        a += wt * d0 * d0;
+        b += wt * d0 * d1;
+        cc += wt * d0 * d2;
+        dd += wt * d1 * d1;
+        e += wt * d1 * d2;
+        ff += wt * d2 * d2;
+    }
+    // symmetric inverse by cofactors
+    const double A00 = dd * ff - e * e, A01 = cc * e - b * ff, A02 = b * e - cc * dd;
+    const double A11 = a * ff - cc * cc, A12 = b * cc - a * e, A22 = a * dd - b * b;
+    const double det = a * A00 + b * A01 + cc * A02;
+    const double tr = a + dd + ff;
+    const bool ok = isfinite(det) && fabs(det) > 1e-12 * tr * tr * tr;
+    const double r = ok ? 1.0 / det : 0.0;
+    for (int j = 0; j < w; ++j) {
+        const int pos = base + 32 * j;
+        const int f = d.ss_f[pos];
+        double c0 = 0, c1 = 0, c2 = 0;
+        if (f >= 0 && ok) {
+            double d0, d1, d2;
+            lsq_offset(d, i, f, d.ss_n[pos], d0, d1, d2);
+            const double wt = 1.0 / (d0 * d0 + d1 * d1 + d2 * d2);
+            c0 = r * wt * (A00 * d0 + A01 * d1 + A02 * d2);
+            c1 = r * wt * (A01 * d0 + A11 * d1 + A12 * d2);
+            c2 = r * wt * (A02 * d0 + A12 * d1 + A22 * d2);
+        }
+        c[pos] = c0;
+        c[d.ss_tot + pos] = c1;
+        c[2 * d.ss_tot + pos] = c2;
+    }
+}
+
+template <int NF>
+__global__ void __launch_bounds__(NB) k_gradient_lsq(DomView d, GradPtrs p) {
+    const int i = blockIdx.x * NB + threadIdx.x;
+    if (i >= d.nc) return;
+    const int base = d.ss_ptr[i >> 5] + (i & 31), w = d.ss_w[i >> 5];
+    double own[NF], g[NF][3];
+#pragma unroll
+    for (int k = 0; k < NF; ++k) {
+        own[k] = __ldg(p.phi[k] + i);
+        g[k][0] = g[k][1] = g[k][2] = 0.;
+    }
+    for (int j = 0; j < w; ++j) {
+        const int pos = base + 32 * j;
+        const int f = __ldg(d.ss_f + pos);
+        if (f < 0) continue;
+        const int nb = __ldg(d.ss_n + pos);
+        const double c0 = __ldg(d.lsq_c + pos), c1 = __ldg(d.lsq_c + d.ss_tot + pos),
+                     c2 = __ldg(d.lsq_c + 2 * d.ss_tot + pos);
+        const bool bnd = nb >= 0 && (nb & SS_BND);
+        const int o = bnd ? (nb & ~SS_BND) : (nb & 0x7FFFFFFF);
+#pragma unroll
+        for (int k = 0; k < NF; ++k) {
+            const double dphi = (bnd ? __ldg(p.Bphi[k] + o) : __ldg(p.phi[k] + o)) - own[k];
+            g[k][0] = fma(c0, dphi, g[k][0]);
+            g[k][1] = fma(c1, dphi, g[k][1]);
+            g[k][2] = fma(c2, dphi, g[k][2]);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < NF; ++k) {
+        p.grad[k][i] = g[k][0];
+        p.grad[k][d.nc + i] = g[k][1];
+        p.grad[k][2 * d.nc + i] = g[k][2];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Limiters, BasicSolver.cpp:88-288
 __device__ __forceinline__ double barth_fun(double us, double umin, double umax) {
     if (us > 1.0e-10) return cmin(1., umax / us);
@@ -1026,12 +1129,27 @@ void launch_gradient(const DomView &d, int nfield, const double *const *phi, con
         p.Bphi[k] = Bphi[k];
         p.grad[k] = grad[k];
     }
-    switch (nfield) {
-    case 1: { k_gradient_v<1><<<nblk(d.nc), NB, 0, st>>>(d, p); ++::sysu::g_launches; } break;
-    case 3: { k_gradient_v<3><<<nblk(d.nc), NB, 0, st>>>(d, p); ++::sysu::g_launches; } break;
-    case 4: { k_gradient_v<4><<<nblk(d.nc), NB, 0, st>>>(d, p); ++::sysu::g_launches; } break;
-    default: throw CaseError{"launch_gradient: 1, 3 or 4 fields"};
+    if (nfield != 1 && nfield != 3 && nfield != 4) throw CaseError{"launch_gradient: 1, 3 or 4 fields"};
+    if (d.lsq_c) {
+        switch (nfield) {
+        case 1: k_gradient_lsq<1><<<nblk(d.nc), NB, 0, st>>>(d, p); break;
+        case 3: k_gradient_lsq<3><<<nblk(d.nc), NB, 0, st>>>(d, p); break;
+        default: k_gradient_lsq<4><<<nblk(d.nc), NB, 0, st>>>(d, p); break;
+        }
+    } else {
+        switch (nfield) {
+        case 1: k_gradient_v<1><<<nblk(d.nc), NB, 0, st>>>(d, p); break;
+        case 3: k_gradient_v<3><<<nblk(d.nc), NB, 0, st>>>(d, p); break;
+        default: k_gradient_v<4><<<nblk(d.nc), NB, 0, st>>>(d, p); break;
+        }
     }
+    ++::sysu::g_launches;
+    CHECK_LAUNCH();
+}
+
+void launch_lsq_setup(const DomView &d, double *lsq_c, cudaStream_t st) {
+    if (d.nc == 0) return;
+    { k_lsq_setup<<<nblk(d.nc), NB, 0, st>>>(d, lsq_c); ++::sysu::g_launches; }
     CHECK_LAUNCH();
 }
 

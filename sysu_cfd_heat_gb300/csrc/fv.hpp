@@ -27,6 +27,10 @@ struct DomView {
     // ss_f: internal face id (-1 = padding); ss_n: neighbour cell (bit 31 set when
     // the cell is the face's cell2) or, for a boundary slot, SS_BND | record
     const int *ss_ptr, *ss_w, *ss_f, *ss_n;
+    int ss_tot;                  // slots stored (the component stride of lsq_c)
+    // least-squares gradients (option "gradient" 1; null: Green-Gauss): per slot
+    // the vector c_j = M^-1 w_j d_j (3 * ss_tot, SoA), so grad = sum_j c_j (phi_j - phi_c)
+    const double *lsq_c;
     // faces
     const int *fc1, *fc2;        // fc2 < 0 on boundary faces
     const double *fn, *farea, *flam, *frl, *fx;  // fn, fx: 3*nf
@@ -79,6 +83,11 @@ void launch_bc_velocity(const DomView &d, const double *R, const double *U, cons
                         cudaStream_t st);
 // Green-Gauss gradient (BasicSolver.cpp:29-63) of 1, 3 or 4 fields with
 // boundary values Bphi[k].
+// Coefficients of the least-squares gradient (lsq_c of DomView) from the geometry:
+// d_j = x_j - x_c (x_j the neighbour's centroid, or the boundary face's), w_j =
+// 1 / |d_j|^2, M = sum_j w_j d_j d_j^T, c_j = M^-1 w_j d_j; cells whose M is
+// singular get c_j = 0 (zero gradient).
+void launch_lsq_setup(const DomView &d, double *lsq_c, cudaStream_t st);
 void launch_gradient(const DomView &d, int nfield, const double *const *phi, const double *const *Bphi,
                      double *const *grad, cudaStream_t st);
 // Limiters (BasicSolver.cpp:118-288) applied in place to grad of phi.

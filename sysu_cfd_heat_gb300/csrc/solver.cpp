@@ -202,6 +202,8 @@ void DomainDev::build(const Domain &d, const Params &p, cudaStream_t st) {
     v.vol = vol.get(); v.cx = cx.get();
     v.cs_ptr = cs_ptr.get(); v.cs_face = cs_face.get(); v.cs_k = cs_k.get();
     v.ss_ptr = ss_ptr.get(); v.ss_w = ss_w.get(); v.ss_f = ss_f.get(); v.ss_n = ss_n.get();
+    v.ss_tot = (int)ss_f.size();
+    v.lsq_c = nullptr;  // Green-Gauss unless option "gradient" selects least squares
     v.fc1 = fc1.get(); v.fc2 = fc2.get();
     v.fn = fn.get(); v.farea = farea.get(); v.flam = flam.get(); v.frl = frl.get(); v.fx = fx.get();
     v.fxpac = fxpac.get(); v.fxnac = fxnac.get(); v.fd12 = fd12.get();
@@ -373,6 +375,23 @@ void SimpleSolver::init_flow_field() {
         double *grad[1] = {s.dPhi.get()};
         grad_limited(sd, s, 1, phi, Bphi, grad);
     }
+}
+
+// Option "gradient": 0 Green-Gauss (BasicSolver.cpp:29-77, the reference's), 1 least
+// squares (fv.cu k_gradient_lsq) for every gradient of both domains.
+void SimpleSolver::set_gradient_scheme(int scheme) {
+    if (scheme != 0 && scheme != 1) throw CaseError{"gradient: 0 Green-Gauss, 1 least squares"};
+    for (DomainDev *d : {&fd, &sd}) {
+        if (d->nc == 0) continue;
+        if (scheme == 1) {
+            if (d->lsq_c.size() < (size_t)3 * d->view.ss_tot) d->lsq_c.alloc((size_t)3 * d->view.ss_tot);
+            launch_lsq_setup(d->view, d->lsq_c.get(), st);
+            d->view.lsq_c = d->lsq_c.get();
+        } else {
+            d->view.lsq_c = nullptr;
+        }
+    }
+    gradient_scheme = scheme;
 }
 
 void SimpleSolver::grad_limited(DomainDev &d, FieldSet &fs, int nfield, const double *const *phi,

@@ -25,6 +25,7 @@ struct DomainDev {
     DevBuf<double> vol, cx, fn, farea, flam, frl, fx, fxpac, fxnac, fd12, bdist, bquirk, bin, bfixed, vx;
     DevBuf<int> cs_ptr, cs_face, cs_k, fc1, fc2, bcell, btype1, btype2, brid, cw_ptr, cw_b, cvert, vc_ptr, vc_cell;
     DevBuf<int> ss_ptr, ss_w, ss_f, ss_n;
+    DevBuf<double> lsq_c;   // least-squares gradient coefficients (option "gradient" 1)
     DevBuf<int> d_int2ref;  // internal face -> reference face (field transfers)
     std::vector<int> h_btype1, h_btype2, h_bcell;
     void build(const Domain &d, const Params &p, cudaStream_t st);
@@ -175,6 +176,8 @@ class SimpleSolver {
     std::string check_iteration();  // read back infos + residuals (one sync)
     // field I/O by reference name (host buffers, reference ordering)
     long field_size(const std::string &name) const;
+    int gradient_scheme = 0;  // 0 Green-Gauss (the reference's), 1 least squares
+    void set_gradient_scheme(int scheme);
     void get_field(const std::string &name, double *out, long n);
     void set_field(const std::string &name, const double *in, long n);
     void sync();

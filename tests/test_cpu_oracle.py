@@ -233,3 +233,19 @@ def test_laspack_zero_rhs_converges_immediately(las):
     assert las.GetLastNoIter() == 0
     assert np.all(_get(x, n) == 0.0)
     las.Q_Destr(C.byref(q))
+
+
+@pytest.mark.parametrize("mesh", ["tet", "hex"])
+def test_lsq_gradient_restatement_exact_for_linear_fields(mesh):
+    """The least-squares gradient (an option of this implementation; the reference
+    has Green-Gauss only) is exact for a linear field with consistent boundary
+    values on any mesh: pins the restatement the GPU kernel is checked against."""
+    m = mg.lid_cavity_tet(5, 5, 4, jitter=0.2, seed=3) if mesh == "tet" else mg.lid_cavity_hex(6)
+    with tempfile.TemporaryDirectory() as tmp:
+        s = simple_np.SimpleNP(mg.write_case(tmp, m, mg.cavity_param("x", 2, mu=0.01)))
+        d = s.d
+        a = np.array([1.5, -2.0, 0.75])
+        phi = 3.0 + d.g.cx @ a
+        bphi = 3.0 + d.g.fx[d.m.bface] @ a
+        gr = d.gradient_lsq(phi, bphi)
+        np.testing.assert_allclose(gr, np.broadcast_to(a, gr.shape), rtol=0, atol=1e-10)
