@@ -516,6 +516,9 @@ class SimpleNP:
         if rtc is not None:
             self.eps = {k: rtc for k in self.eps}
         self.Residual = np.zeros(10)
+        # momentum convection: False the reference's scheme; True the hybrid scheme of
+        # the GPU implementation's option "convection" 1 (not in the reference)
+        self.hybrid = False
         self.init_flow_field()
 
     # navier.cpp:113-188, HeatConductionSolver.cpp:334-369
@@ -632,6 +635,8 @@ class SimpleNP:
         phis = (self.U, self.V, self.W)
         grs = (self.dU, self.dV, self.dW)
         fcs = [RU * ((ph[up] + _dot3(gr[up], dx)) - ph[up]) for ph, gr in zip(phis, grs)]
+        if self.hybrid:  # option of the GPU implementation: no deferred correction
+            fcs = [np.zeros_like(RU) for _ in range(3)]
         du, dv, dw = G
         fde = [((du[:, 0] + du[:, 0]) * S[:, 0] + (du[:, 1] + dv[:, 0]) * S[:, 1] + (du[:, 2] + dw[:, 0]) * S[:, 2]) * Visc,
                ((dv[:, 0] + du[:, 1]) * S[:, 0] + (dv[:, 1] + dv[:, 1]) * S[:, 1] + (dv[:, 2] + dw[:, 1]) * S[:, 2]) * Visc,
@@ -647,9 +652,14 @@ class SimpleNP:
         f = d.slot_face
         first = m.c1[f] == d.slot_row
         RUn = np.where(first, self.RUFace[f], -self.RUFace[f])
-        conv = np.minimum(RUn, 0.)
-        offd = conv - Df[f]
-        np.add.at(app, d.slot_row, -conv + Df[f])
+        if self.hybrid:  # hybrid (Spalding): a_nb = max(-F, D - F/2, 0)
+            anb = np.maximum(np.maximum(-RUn, Df[f] - 0.5 * RUn), 0.)
+            offd = -anb
+            np.add.at(app, d.slot_row, anb)
+        else:
+            conv = np.minimum(RUn, 0.)
+            offd = conv - Df[f]
+            np.add.at(app, d.slot_row, -conv + Df[f])
         np.add.at(src, d.slot_row, np.where(first[:, None], E[f], -E[f]))
         # boundary faces (:126-223)
         bf = m.bface

@@ -170,6 +170,11 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
     if (k == "mom_batched") { o.mom_batched = value != 0.0; return SYSU_OK; }
     if (k == "sm_cap") { s->impl->kw.sm_cap = std::max(0, (int)value); return SYSU_OK; }
     if (k == "spmv_variant") { sysu::set_spmv_variant((int)value); return SYSU_OK; }
+    if (k == "convection") {
+        if (value != 0.0 && value != 1.0) return set_err(SYSU_ERR_INPUT, "convection: 0 upwind + deferred correction, 1 hybrid");
+        o.convection = (int)value;
+        return SYSU_OK;
+    }
     if (k == "gradient") {
         if (value != 0.0 && value != 1.0) return set_err(SYSU_ERR_INPUT, "gradient: 0 Green-Gauss, 1 least squares");
         try {
@@ -293,6 +298,7 @@ int sysu_solver_get_option(sysu_solver *s, const char *key, double *value) {
     if (k == "mom_batched") { *value = o.mom_batched; return SYSU_OK; }
     if (k == "scalars_batched") { *value = o.scalars_batched; return SYSU_OK; }
     if (k == "gradient") { *value = s->impl->gradient_scheme; return SYSU_OK; }
+    if (k == "convection") { *value = o.convection; return SYSU_OK; }
     if (k == "sm_cap") { *value = s->impl->kw.sm_cap; return SYSU_OK; }
     if (k == "solid_source") { *value = o.solid_source; return SYSU_OK; }
     if (k == "fatal_checks") { *value = o.fatal_checks; return SYSU_OK; }

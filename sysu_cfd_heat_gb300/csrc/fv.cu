@@ -437,14 +437,19 @@ __global__ void k_mom_face(DomView d, MomArgs a) {
     double dwdy = lambda * a.dW[nc + c1] + lambda2 * a.dW[nc + c2];
     double dwdz = lambda * a.dW[2 * nc + c1] + lambda2 * a.dW[2 * nc + c2];
     double D = Visc * d.frl[f];
-    // deferred correction to linear upwind (:269-295)
-    int up = RU > 0. ? c1 : c2;
-    double dx0 = d.fx[f] - d.cx[up], dx1 = d.fx[nf + f] - d.cx[nc + up], dx2 = d.fx[2 * nf + f] - d.cx[2 * nc + up];
-    double ufi = a.U[up], vfi = a.V[up], wfi = a.W[up];
-    double ufh = ufi + (a.dU[up] * dx0 + a.dU[nc + up] * dx1 + a.dU[2 * nc + up] * dx2);
-    double vfh = vfi + (a.dV[up] * dx0 + a.dV[nc + up] * dx1 + a.dV[2 * nc + up] * dx2);
-    double wfh = wfi + (a.dW[up] * dx0 + a.dW[nc + up] * dx1 + a.dW[2 * nc + up] * dx2);
-    double fcs0 = RU * (ufh - ufi), fcs1 = RU * (vfh - vfi), fcs2 = RU * (wfh - wfi);
+    // deferred correction to linear upwind (:269-295); none with the hybrid scheme
+    double fcs0 = 0., fcs1 = 0., fcs2 = 0.;
+    if (!a.hybrid) {
+        int up = RU > 0. ? c1 : c2;
+        double dx0 = d.fx[f] - d.cx[up], dx1 = d.fx[nf + f] - d.cx[nc + up], dx2 = d.fx[2 * nf + f] - d.cx[2 * nc + up];
+        double ufi = a.U[up], vfi = a.V[up], wfi = a.W[up];
+        double ufh = ufi + (a.dU[up] * dx0 + a.dU[nc + up] * dx1 + a.dU[2 * nc + up] * dx2);
+        double vfh = vfi + (a.dV[up] * dx0 + a.dV[nc + up] * dx1 + a.dV[2 * nc + up] * dx2);
+        double wfh = wfi + (a.dW[up] * dx0 + a.dW[nc + up] * dx1 + a.dW[2 * nc + up] * dx2);
+        fcs0 = RU * (ufh - ufi);
+        fcs1 = RU * (vfh - vfi);
+        fcs2 = RU * (wfh - wfi);
+    }
     // explicit part of the stress (:302-309) and non-orthogonal correction (:313-316)
     double fde0 = ((dudx + dudx) * sav1 + (dudy + dvdx) * sav2 + (dudz + dwdx) * sav3) * Visc;
     double fde1 = ((dvdx + dudy) * sav1 + (dvdy + dvdy) * sav2 + (dvdz + dwdy) * sav3) * Visc;
@@ -528,14 +533,20 @@ __global__ void k_mom_cell(DomView d, MomArgs a) {
         if (f < d.F) {
             bool first = d.fc1[f] == i;
             double RUn = first ? a.RUFace[f] : -a.RUFace[f];
-            double apn = 0.;
-            if (RUn < 0.) {
-                apn += RUn;
-                app -= RUn;
-            }
             double D = a.fD[f];
-            app += D;
-            apn += -D;
+            double apn = 0.;
+            if (a.hybrid) {
+                const double anb = cmax(cmax(-RUn, D - 0.5 * RUn), 0.);
+                app += anb;
+                apn = -anb;
+            } else {
+                if (RUn < 0.) {
+                    apn += RUn;
+                    app -= RUn;
+                }
+                app += D;
+                apn += -D;
+            }
             a.val[sell_pos(d.A, i, d.cs_k[s])] = apn;
             double e0 = a.fE[f], e1 = a.fE[d.F + f], e2 = a.fE[2 * d.F + f];
             if (first) { su += e0; sv += e1; sw += e2; }

@@ -110,6 +110,11 @@ struct MomArgs {
     const double *Unp = nullptr, *Vnp = nullptr, *Wnp = nullptr;
     double dt = 0.0;
     int tscheme = 0;
+    // convection of interior faces: 0 the reference's implicit upwind with deferred
+    // correction to linear upwind (navier_velocity.cpp:255-295); 1 hybrid (Spalding):
+    // a_nb = max(-F, D - F/2, 0) with F the face's outward mass flux, no deferred
+    // correction (an option; the reference has no hybrid scheme)
+    int hybrid = 0;
 };
 // BuildVelocityMatrix, navier_velocity.cpp:77-357
 void launch_momentum(const DomView &d, const MomArgs &a, cudaStream_t st);

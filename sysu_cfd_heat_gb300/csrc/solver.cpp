@@ -518,6 +518,7 @@ void SimpleSolver::calculate_velocity() {
     a.fD = f.fD.get(); a.fE = f.fE.get(); a.bapp = f.bapp.get(); a.bsrc = f.bsrc.get();
     a.val = f.Amom.get();
     a.tscheme = tscheme();
+    a.hybrid = opt.convection == 1;
     if (a.tscheme) {
         a.Unp = f.Unp.get(); a.Vnp = f.Vnp.get(); a.Wnp = f.Wnp.get();
         a.dt = p.dt;
