@@ -516,8 +516,9 @@ class SimpleNP:
         if rtc is not None:
             self.eps = {k: rtc for k in self.eps}
         self.Residual = np.zeros(10)
-        # momentum convection: False the reference's scheme; True the hybrid scheme of
-        # the GPU implementation's option "convection" 1 (not in the reference)
+        # convection of momentum and the fluid scalars: False the reference's scheme;
+        # True the hybrid scheme of the GPU implementation's option "convection" 1
+        # (not in the reference)
         self.hybrid = False
         self.init_flow_field()
 
@@ -778,7 +779,7 @@ class SimpleNP:
         gf = lam[:, None] * grad[c1] + (1. - lam)[:, None] * grad[c2]
         D = Visc * g.rl[inn]
         fcs = np.zeros(len(inn))
-        if mode != "solid":
+        if mode != "solid" and not self.hybrid:
             RU = RUFace[inn]
             up = np.where(RU > 0., c1, c2)
             fcs = RU * ((phi[up] + _dot3(grad[up], g.fx[inn] - g.cx[up])) - phi[up])
@@ -790,13 +791,19 @@ class SimpleNP:
         first = m.c1[f] == d.slot_row
         app = app0.copy()
         sphi = src.copy()
-        if mode != "solid":
+        if mode != "solid" and self.hybrid:  # hybrid (option of the GPU implementation)
             RUn = np.where(first, RUFace[f], -RUFace[f])
-            conv = np.minimum(RUn, 0.)
+            anb = np.maximum(np.maximum(-RUn, Df[f] - 0.5 * RUn), 0.)
+            offd = -anb
+            np.add.at(app, d.slot_row, anb)
         else:
-            conv = np.zeros(len(f))
-        offd = conv - Df[f]
-        np.add.at(app, d.slot_row, -conv + Df[f])
+            if mode != "solid":
+                RUn = np.where(first, RUFace[f], -RUFace[f])
+                conv = np.minimum(RUn, 0.)
+            else:
+                conv = np.zeros(len(f))
+            offd = conv - Df[f]
+            np.add.at(app, d.slot_row, -conv + Df[f])
         np.add.at(sphi, d.slot_row, np.where(first, E[f], -E[f]))
         bf = m.bface
         ic = d.bc1

@@ -796,7 +796,7 @@ __global__ void k_scalar_face(DomView d, ScalarArgs a) {
     double gz = lambda * a.grad[2 * nc + c1] + lambda2 * a.grad[2 * nc + c2];
     double D = Visc * d.frl[f];
     double fcs = 0.;
-    if (a.bc_mode != SC_SOLID) {
+    if (a.bc_mode != SC_SOLID && !a.hybrid) {
         double RU = a.RUFace[f];
         int up = RU > 0. ? c1 : c2;
         double dx0 = d.fx[f] - d.cx[up], dx1 = d.fx[nf + f] - d.cx[nc + up], dx2 = d.fx[2 * nf + f] - d.cx[2 * nc + up];
@@ -874,16 +874,23 @@ __global__ void k_scalar_cell(DomView d, ScalarArgs a) {
         if (f < d.F) {
             bool first = d.fc1[f] == i;
             double apn = 0.;
-            if (conv) {
-                double RUn = first ? a.RUFace[f] : -a.RUFace[f];
-                if (RUn < 0.) {
-                    apn += RUn;
-                    app -= RUn;
-                }
-            }
             double D = a.fD[f];
-            app += D;
-            apn += -D;
+            if (conv && a.hybrid) {
+                const double RUn = first ? a.RUFace[f] : -a.RUFace[f];
+                const double anb = cmax(cmax(-RUn, D - 0.5 * RUn), 0.);
+                app += anb;
+                apn = -anb;
+            } else {
+                if (conv) {
+                    double RUn = first ? a.RUFace[f] : -a.RUFace[f];
+                    if (RUn < 0.) {
+                        apn += RUn;
+                        app -= RUn;
+                    }
+                }
+                app += D;
+                apn += -D;
+            }
             a.val[sell_pos(d.A, i, d.cs_k[s])] = apn;
             double e = a.fE[f];
             if (first) sphi += e;

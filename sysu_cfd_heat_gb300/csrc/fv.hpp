@@ -187,6 +187,7 @@ struct ScalarArgs {
     double *bapp, *bsrc;   // boundary scratch
     double *val, *b;
     int *flags;
+    int hybrid = 0;        // convection of interior faces: see MomArgs::hybrid
 };
 void launch_scalar(const DomView &d, const ScalarArgs &a, cudaStream_t st);
 

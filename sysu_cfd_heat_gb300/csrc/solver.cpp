@@ -594,6 +594,7 @@ void SimpleSolver::update_ke() {
     launch_time_term(nc, f.R.get(), fd.vol.get(), p.dt, tscheme(), f.TEp.get(), f.ApTE.get(), f.TESrc.get(), st);
     launch_time_term(nc, f.R.get(), fd.vol.get(), p.dt, tscheme(), f.EDp.get(), f.ApED.get(), f.EDSrc.get(), st);
     ScalarArgs sa{};
+    sa.hybrid = opt.convection == 1;
     sa.RUFace = f.RUFace.get(); sa.grad = f.dPhi.get(); sa.urf = p.urf[5]; sa.bc_mode = SC_FLUID_PLAIN;
     sa.fD = f.fD.get(); sa.fE = f.fE.get(); sa.bapp = f.bapp.get(); sa.bsrc = f.bsrc.get();
     sa.val = f.As.get(); sa.b = f.bs.get(); sa.flags = flags.get();
@@ -650,6 +651,7 @@ void SimpleSolver::update_scalars_batched() {
     launch_time_term(nc, f.R.get(), fd.vol.get(), p.dt, tscheme(), f.EDp.get(), f.ApED.get(), f.EDSrc.get(), st);
     launch_ke_eps_sources(d, k, st);
     ScalarArgs sa{};
+    sa.hybrid = opt.convection == 1;
     sa.RUFace = f.RUFace.get(); sa.grad = f.dPhi.get(); sa.urf = p.urf[5]; sa.bc_mode = SC_FLUID_PLAIN;
     sa.fD = f.fD.get(); sa.fE = f.fE.get(); sa.bapp = f.bapp.get(); sa.bsrc = f.bsrc.get();
     sa.flags = flags.get();
@@ -740,6 +742,7 @@ void SimpleSolver::update_energy() {
     double *grad[1] = {f.dPhi.get()};
     grad_limited(fd, f, 1, phi, Bphi, grad);
     ScalarArgs sa{};
+    sa.hybrid = opt.convection == 1;
     sa.phi = f.T.get(); sa.Bphi = f.BTem.get(); sa.diff = f.kcond.get(); sa.src = f.zeros.get(); sa.app0 = f.zeros.get();
     energy_sources(sa);
     sa.grad = f.dPhi.get(); sa.RUFace = f.RUFace.get(); sa.Bq = f.Bq.get(); sa.urf = p.urf[5];
@@ -768,6 +771,7 @@ void SimpleSolver::solid_solve() {
     double *grad[1] = {s.dPhi.get()};
     grad_limited(sd, s, 1, phi, Bphi, grad);
     ScalarArgs sa{};
+    sa.hybrid = opt.convection == 1;
     sa.phi = s.T.get(); sa.Bphi = s.BTem.get(); sa.diff = s.diff.get(); sa.src = s.src.get(); sa.app0 = s.zeros.get();
     if (tscheme()) {  // HeatConductionSolver.cpp:66-80 (solid density)
         // Always Euler: NavierStokesSolver declares its own TimeScheme (navier.h:29),

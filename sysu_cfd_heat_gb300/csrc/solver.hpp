@@ -93,7 +93,7 @@ struct SolverOptions {
         mom_batched = true;
     }
     bool mom_batched = true;      // u, v, w as one 3-RHS solve
-    int convection = 0;           // momentum convection: 0 the reference's upwind + deferred correction, 1 hybrid
+    int convection = 0;           // convection of momentum and fluid scalars: 0 the reference's upwind + deferred correction, 1 hybrid
     double solid_source = 0.0;    // W/m^3 (extension; the reference has none)
     bool fatal_checks = true;     // the reference's convergence checks
     bool timing = false;          // CUDA events around the p' solve

@@ -60,3 +60,21 @@ def test_hybrid_differs_from_default_and_option_checked():
             assert _rel(u1, u0) > 1e-4
             with pytest.raises(SysuError):
                 s.set_option("convection", 3)
+
+
+def test_hybrid_scalars_cht_ke_channel_matches_oracle():
+    """k, eps and T convected with the hybrid scheme too (the solid has no convection)."""
+    iters = 10
+    with tempfile.TemporaryDirectory() as tmp:
+        p = mg.write_case(tmp, mg.cht_channel(8, 4, 2, 3), mg.cht_param("x", iters + 1, turb=True))
+        ref = simple_np.SimpleNP(p, rtc=1e-12)
+        ref.hybrid = True
+        assert ref.iterate(iters) == iters
+        with NavierStokesSolver(p, {"rtc": 1e-12, "convection": 1}) as s:
+            assert s.iterate(iters) == iters
+            pairs = [("U", ref.U), ("V", ref.V), ("W", ref.W), ("TE", ref.TE), ("ED", ref.ED), ("T", ref.T)]
+            for f, r in pairs:
+                e = _rel(s.get(f), r)
+                assert e < 1e-8, (f, e)
+            e = _rel(s.get("solid_T"), ref.sT)
+            assert e < 1e-8, ("solid_T", e)
