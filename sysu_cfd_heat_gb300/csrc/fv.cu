@@ -417,6 +417,7 @@ __global__ void k_limiter_mlp(DomView d, const double *phi, const double *vmax, 
 
 // ---------------------------------------------------------------------------
 // Momentum, navier_velocity.cpp:77-357.  Interior face pass, from cell1's side.
+template <bool HYB>  // the hybrid scheme: a compile-time branch, so the default kernel does no extra work
 __global__ void k_mom_face(DomView d, MomArgs a) {
     int f = blockIdx.x * NB + threadIdx.x;
     if (f >= d.F) return;
@@ -439,7 +440,7 @@ __global__ void k_mom_face(DomView d, MomArgs a) {
     double D = Visc * d.frl[f];
     // deferred correction to linear upwind (:269-295); none with the hybrid scheme
     double fcs0 = 0., fcs1 = 0., fcs2 = 0.;
-    if (!a.hybrid) {
+    if (!HYB) {
         int up = RU > 0. ? c1 : c2;
         double dx0 = d.fx[f] - d.cx[up], dx1 = d.fx[nf + f] - d.cx[nc + up], dx2 = d.fx[2 * nf + f] - d.cx[2 * nc + up];
         double ufi = a.U[up], vfi = a.V[up], wfi = a.W[up];
@@ -509,6 +510,7 @@ __global__ void k_mom_bnd(DomView d, MomArgs a) {
 }
 
 // cell pass (:95-355): diagonal, off-diagonals, Apr and the three RHS
+template <bool HYB>
 __global__ void k_mom_cell(DomView d, MomArgs a) {
     int i = blockIdx.x * NB + threadIdx.x;
     if (i >= d.nc) return;
@@ -535,7 +537,7 @@ __global__ void k_mom_cell(DomView d, MomArgs a) {
             double RUn = first ? a.RUFace[f] : -a.RUFace[f];
             double D = a.fD[f];
             double apn = 0.;
-            if (a.hybrid) {
+            if (HYB) {
                 const double anb = cmax(cmax(-RUn, D - 0.5 * RUn), 0.);
                 app += anb;
                 apn = -anb;
@@ -782,6 +784,7 @@ __global__ void k_correct_faces(DomView d, const double *dp, const double *dPdp,
 // ---------------------------------------------------------------------------
 // Scalar transport assembly.  Fluid: navier_scalar.cpp:466-647 (+ the energy
 // wall callback :176-248); solid: HeatConductionSolver.cpp:175-288.
+template <bool HYB>
 __global__ void k_scalar_face(DomView d, ScalarArgs a) {
     int f = blockIdx.x * NB + threadIdx.x;
     if (f >= d.F) return;
@@ -796,7 +799,7 @@ __global__ void k_scalar_face(DomView d, ScalarArgs a) {
     double gz = lambda * a.grad[2 * nc + c1] + lambda2 * a.grad[2 * nc + c2];
     double D = Visc * d.frl[f];
     double fcs = 0.;
-    if (a.bc_mode != SC_SOLID && !a.hybrid) {
+    if (a.bc_mode != SC_SOLID && !HYB) {
         double RU = a.RUFace[f];
         int up = RU > 0. ? c1 : c2;
         double dx0 = d.fx[f] - d.cx[up], dx1 = d.fx[nf + f] - d.cx[nc + up], dx2 = d.fx[2 * nf + f] - d.cx[2 * nc + up];
@@ -863,6 +866,7 @@ __global__ void k_scalar_bnd(DomView d, ScalarArgs a) {
     a.bsrc[b] = fde - fdi - fcs;
 }
 
+template <bool HYB>
 __global__ void k_scalar_cell(DomView d, ScalarArgs a) {
     int i = blockIdx.x * NB + threadIdx.x;
     if (i >= d.nc) return;
@@ -875,7 +879,7 @@ __global__ void k_scalar_cell(DomView d, ScalarArgs a) {
             bool first = d.fc1[f] == i;
             double apn = 0.;
             double D = a.fD[f];
-            if (conv && a.hybrid) {
+            if (conv && HYB) {
                 const double RUn = first ? a.RUFace[f] : -a.RUFace[f];
                 const double anb = cmax(cmax(-RUn, D - 0.5 * RUn), 0.);
                 app += anb;
@@ -1189,9 +1193,15 @@ void launch_limiter(const DomView &d, int limiter, const double *phi, double *gr
 }
 
 void launch_momentum(const DomView &d, const MomArgs &a, cudaStream_t st) {
-    if (d.F) { k_mom_face<<<nblk(d.F), NB, 0, st>>>(d, a); ++::sysu::g_launches; }
+    if (d.F) {
+        if (a.hybrid) k_mom_face<true><<<nblk(d.F), NB, 0, st>>>(d, a);
+        else k_mom_face<false><<<nblk(d.F), NB, 0, st>>>(d, a);
+        ++::sysu::g_launches;
+    }
     if (d.B) { k_mom_bnd<<<nblk(d.B), NB, 0, st>>>(d, a); ++::sysu::g_launches; }
-    { k_mom_cell<<<nblk(d.nc), NB, 0, st>>>(d, a); ++::sysu::g_launches; }
+    if (a.hybrid) k_mom_cell<true><<<nblk(d.nc), NB, 0, st>>>(d, a);
+    else k_mom_cell<false><<<nblk(d.nc), NB, 0, st>>>(d, a);
+    ++::sysu::g_launches;
     CHECK_LAUNCH();
 }
 
@@ -1250,9 +1260,15 @@ void launch_correct_faces(const DomView &d, const double *dp, const double *dPdp
 }
 
 void launch_scalar(const DomView &d, const ScalarArgs &a, cudaStream_t st) {
-    if (d.F) { k_scalar_face<<<nblk(d.F), NB, 0, st>>>(d, a); ++::sysu::g_launches; }
+    if (d.F) {
+        if (a.hybrid) k_scalar_face<true><<<nblk(d.F), NB, 0, st>>>(d, a);
+        else k_scalar_face<false><<<nblk(d.F), NB, 0, st>>>(d, a);
+        ++::sysu::g_launches;
+    }
     if (d.B) { k_scalar_bnd<<<nblk(d.B), NB, 0, st>>>(d, a); ++::sysu::g_launches; }
-    { k_scalar_cell<<<nblk(d.nc), NB, 0, st>>>(d, a); ++::sysu::g_launches; }
+    if (a.hybrid) k_scalar_cell<true><<<nblk(d.nc), NB, 0, st>>>(d, a);
+    else k_scalar_cell<false><<<nblk(d.nc), NB, 0, st>>>(d, a);
+    ++::sysu::g_launches;
     CHECK_LAUNCH();
 }
 
