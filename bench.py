@@ -484,6 +484,24 @@ def learned_form(s, args, to8, field_err):
     return out
 
 
+def max_over_ranks(x: float, w: int) -> float:
+    """The largest per-rank value over the ranks (gloo all-reduce): the timed region
+    of a replica run ends when its slowest replica does."""
+    if w <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_rate(w: int, steps: int, t_max_ms: float) -> float:
+    """Whole-job outer iterations/s of w replicas that each ran `steps` iterations."""
+    return w * steps / (t_max_ms / 1000.0)
+
+
 def run_ours(args, r, w, lr):
     from sysu_cfd_heat_gb300 import _lib
     from sysu_cfd_heat_gb300.solver import NavierStokesSolver
@@ -533,15 +551,10 @@ def run_ours(args, r, w, lr):
 
     def field_err():
         return max(float(np.linalg.norm(s.get(f) - a) / max(np.linalg.norm(a), 1e-300)) for f, a in fields64.items())
-    t_max = s_ms
+    t_max = max_over_ranks(s_ms, w)
     if w > 1:
-        import torch
-
-        t = torch.tensor([s_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
         dist.barrier()
-    value = w * args.steps / (t_max / 1000.0)
+    value = replicas_rate(w, args.steps, t_max)
 
     # end to end through the C ABI with host buffers (page-locked, so the copies are DMA)
     s.reset()
@@ -561,13 +574,7 @@ def run_ours(args, r, w, lr):
         s.iterate(1)
         for f in state:
             s.get(f, out=host[f])
-    e2e_s = time.perf_counter() - t0
-    if w > 1:
-        import torch
-
-        t = torch.tensor([e2e_s], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, w)
 
     peaks = {}
     pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
