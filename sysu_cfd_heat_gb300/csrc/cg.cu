@@ -46,10 +46,10 @@ namespace sysu {
 namespace {
 
 // Threads per CTA (measured on the 2M-cell tet p' system: the FP64 kernel is
-// fastest with 16 warps, 128 registers a thread and 480-row tiles, the FP32
-// one with 24 warps and 736-row tiles).  The last warp produces, the others
+// fastest with 20 warps, 96 registers a thread and 608-row tiles -- 512 and 768
+// threads measured 3-8 % slower -- the FP32 one with 24 warps and 736-row tiles).  The last warp produces, the others
 // consume; a tile has one slice (32 rows) per consumer warp.
-constexpr int CGT64 = 512;
+constexpr int CGT64 = 640;
 constexpr int CGT32 = 768;
 constexpr unsigned CG_SMEM_BUDGET = 200 * 1024;     // dynamic shared memory for the ring
 constexpr int CG_WR = 6;                            // gathers per row held in registers one tile ahead (FP64)
