@@ -333,6 +333,67 @@ __device__ __forceinline__ void issue_matrix_tile(const Part &P, const SellView 
 __device__ __forceinline__ double fma_t(double a, double b, double c) { return __fma_rn(a, b, c); }
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
+// |r| 2^-k as an FP32 number made from r's high word with integer operations only
+// (20 of the 52 mantissa bits, relative error below 2^-20): GB300's FP64 pipe runs
+// at 1/64 of the FP32 rate, and r.r serves only the stopping test.  bias = 1023 +
+// k - 127.  Exponent 0x7FF (inf, NaN) gives NaN; values below FP32's normal range
+// give 0; huge ones are held at 2^50 so that a thread's sum of squares stays finite.
+__device__ __forceinline__ float scaled_abs_f32(double r, int bias) {
+    const int hi = __double2hiint(r);
+    const int e = (hi >> 20) & 0x7FF;
+    if (e == 0x7FF) return __int_as_float(0x7FC00000);
+    const int fe = e - bias;
+    if (fe <= 0) return 0.f;
+    return __int_as_float((min(fe, 127 + 50) << 23) | ((hi & 0xFFFFF) << 3));
+}
+
+// X phase of the FP64 kernel with r.r estimated in FP32 (rr32, in units of 2^-2k);
+// x, r, z and r.z exactly as x_phase computes them.
+template <int NT, int RB>
+__device__ __forceinline__ void x_phase_est(int R0, int R1, double alpha, const double *__restrict__ pv,
+                                            const double *__restrict__ qv, const double *__restrict__ dv,
+                                            double *__restrict__ xv, double *__restrict__ rv,
+                                            double *__restrict__ zv, float &rr32, double &rz, int bias) {
+    int i = R0 + (int)threadIdx.x;
+    for (; i + (RB - 1) * NT < R1; i += RB * NT) {
+        double p[RB], q[RB], x[RB], r[RB], d[RB];
+#pragma unroll
+        for (int u = 0; u < RB; ++u) {
+            const int j = i + u * NT;
+            p[u] = pv[j];
+            q[u] = qv[j];
+            x[u] = xv[j];
+            r[u] = rv[j];
+            d[u] = dv[j];
+        }
+#pragma unroll
+        for (int u = 0; u < RB; ++u) {
+            const int j = i + u * NT;
+            x[u] = fma_t(alpha, p[u], x[u]);
+            r[u] = fma_t(-alpha, q[u], r[u]);
+            const double z = d[u] * r[u];
+            xv[j] = x[u];
+            rv[j] = r[u];
+            zv[j] = z;
+            const float f = scaled_abs_f32(r[u], bias);
+            rr32 = fmaf(f, f, rr32);
+            rz = fma_t(r[u], z, rz);
+        }
+    }
+    for (; i < R1; i += NT) {
+        double pi = pv[i], qi = qv[i], xi = xv[i], ri = rv[i], di = dv[i];
+        xi = fma_t(alpha, pi, xi);
+        ri = fma_t(-alpha, qi, ri);
+        const double zi = di * ri;
+        xv[i] = xi;
+        rv[i] = ri;
+        zv[i] = zi;
+        const float f = scaled_abs_f32(ri, bias);
+        rr32 = fmaf(f, f, rr32);
+        rz = fma_t(ri, zi, rz);
+    }
+}
+
 template <class T, int NT, int RB>
 __device__ __forceinline__ void x_phase(int R0, int R1, T alpha, const T *__restrict__ pv, const T *__restrict__ qv,
                                         const T *__restrict__ dv, T *__restrict__ xv, T *__restrict__ rv,
@@ -516,8 +577,9 @@ __global__ void __launch_bounds__(CGT64, 1) k_cg_pipe(CgPipeArgs a) {
     }
     if (!grid_sum_t0<3>(v3, rc, a.gb, err)) { drain(R); return; }
     // thread-0 scalar state, kept in shared memory (no registers in the other threads)
-    __shared__ double s_state[4];
-    double &bb = s_state[0], &rr = s_state[1], &rho = s_state[2], &thr = s_state[3];
+    __shared__ double s_state[5];
+    double &bb = s_state[0], &rr = s_state[1], &rho = s_state[2], &thr = s_state[3], &est_unit = s_state[4];
+    __shared__ int s_bias, s_rr_est;  // scaling of the r.r estimate (0: exact r.r); rr holds an estimate
     if (tid == 0) {
         bb = v3[0] == 0.0 ? 1.0 : v3[0];
         thr = a.eps * a.eps * bb;
@@ -525,8 +587,20 @@ __global__ void __launch_bounds__(CGT64, 1) k_cg_pipe(CgPipeArgs a) {
         rho = v3[2];
         g_bc[0] = stop_code(rr, thr);
         g_bc[1] = 0.0;
+        // estimate r.r in FP32 in units of 2^2k, 2^2k ~ thr (0: thr unusable, exact r.r)
+        s_bias = 0;
+        s_rr_est = 0;
+        if (thr > 0.0 && isfinite(thr)) {
+            const int e = ilogb(thr);
+            const int k = e >= 0 ? e / 2 : -((1 - e) / 2);  // floor(e / 2)
+            if (k > -900 && k < 900) {
+                s_bias = 1023 + k - 127;
+                est_unit = ldexp(1.0, 2 * k);
+            }
+        }
     }
     __syncthreads();
+    const int rr_bias = s_bias;
 
     long long base = 0;  // job index of the running S phase's first tile
     int it = 0, status = DEV_OK;
@@ -557,18 +631,52 @@ __global__ void __launch_bounds__(CGT64, 1) k_cg_pipe(CgPipeArgs a) {
         // X: the producer first queues the next S phase's tiles
         if (prod) producer_tiles(R, 0, issue, err);
         double v2[2] = {0.0, 0.0};
-        x_phase<double, CGT64, 4>(R0, R1, alpha, a.p, a.q, a.dinv, a.x, a.r, a.z, v2[0], v2[1]);
+        if (rr_bias) {
+            float rr32 = 0.f;
+            x_phase_est<CGT64, 4>(R0, R1, alpha, a.p, a.q, a.dinv, a.x, a.r, a.z, rr32, v2[1], rr_bias);
+            v2[0] = (double)rr32;
+        } else {
+            x_phase<double, CGT64, 4>(R0, R1, alpha, a.p, a.q, a.dinv, a.x, a.r, a.z, v2[0], v2[1]);
+        }
         if (!grid_sum_t0<2>(v2, rc, a.gb, err) || fail_flag()) break;
         stamp(a.ts, it, 2);
         if (tid == 0) {
-            rr = v2[0];
-            g_bc[0] = stop_code(rr, thr);
             g_bc[1] = v2[1] / rho;
             rho = v2[1];
+            if (rr_bias) {
+                // the estimate decides only when it is clearly above the threshold
+                rr = v2[0] * est_unit;
+                s_rr_est = 1;
+                g_bc[5] = rr >= thr * 1.001 ? 0.0 : 1.0;  // 1: take the exact r.r (NaN included)
+                g_bc[0] = 0.0;
+            } else {
+                rr = v2[0];
+                g_bc[0] = stop_code(rr, thr);
+                g_bc[5] = 0.0;
+            }
         }
         __syncthreads();
+        if (g_bc[5] != 0.0) {  // near (or below) the threshold: the exact FP64 r.r
+            double e1[1] = {0.0};
+            for (int i = R0 + tid; i < R1; i += CGT64) e1[0] = fma(a.r[i], a.r[i], e1[0]);
+            if (!grid_sum_t0<1>(e1, rc, a.gb, err)) break;
+            if (tid == 0) {
+                rr = e1[0];
+                s_rr_est = 0;
+                g_bc[0] = stop_code(rr, thr);
+            }
+            __syncthreads();
+        }
     }
     drain(R);
+    // the reported residual is the exact one: recompute r.r if rr holds an estimate
+    // (not after a failed wait, when the blocks no longer meet)
+    if (s_rr_est && !fail_flag() && !(a.info->err)) {
+        double e1[1] = {0.0};
+        for (int i = R0 + tid; i < R1; i += CGT64) e1[0] = fma(a.r[i], a.r[i], e1[0]);
+        if (grid_sum_t0<1>(e1, rc, a.gb, err) && tid == 0) rr = e1[0];
+        __syncthreads();
+    }
     if (blockIdx.x == 0 && tid == 0) {
         double res = sqrt(rr) / sqrt(bb);
         if (status == DEV_OK && !(rr < thr)) status = isfinite(rr) ? DEV_MAXITER : DEV_NONFINITE;
