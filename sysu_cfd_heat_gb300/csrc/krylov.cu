@@ -978,6 +978,18 @@ void jacobi_apply(const SellDev &A, const double *val, double omega, const doubl
 }
 
 
+// Blocks of a BiCGSTAB launch: enough for about BICG_ROWS_PER_THREAD rows a
+// thread, at least one per SM.  Each iteration has five grid barriers; on a
+// small system (256k rows: 608 blocks would give under 2 rows a thread) the
+// barriers of a full grid cost more than its extra parallelism brings -- the
+// momentum solve of the 307k-cell channel measured 3.1 ms on 608 blocks and
+// 2.3 ms on 256.  The 2M-row case keeps the full grid.
+constexpr int BICG_ROWS_PER_THREAD = 4;
+static int bicg_blocks_for(int n, int maxb) {
+    const long want = ((long)n + (long)KB * BICG_ROWS_PER_THREAD - 1) / ((long)KB * BICG_ROWS_PER_THREAD);
+    return (int)std::min<long>(maxb, std::max<long>(num_sms(), want));
+}
+
 static int bicg_max_blocks(int nrhs, bool multi) {
     static int mb[4] = {0, 0, 0, 0};
     if (!mb[0]) {
@@ -1027,7 +1039,7 @@ static void bicg_launch(const SellDev &A, const double *const *vals, bool multi,
     a.maxit = o.maxit;
     a.eps = o.eps;
     void *args[] = {&a};
-    int G = grid_for(n, maxb);
+    int G = grid_for(n, bicg_blocks_for(n, maxb));
     const void *k = nrhs == 1 ? (const void *)k_bicgstab<1, false>
                               : (multi ? (const void *)k_bicgstab<3, true> : (const void *)k_bicgstab<3, false>);
     SYSU_CUDA(cudaMemsetAsync(w.barrier.get(), 0, sizeof(GridBarrier), st));  // grid_sync starts from 0
@@ -1081,7 +1093,7 @@ void bicgstab_solve_mixed(const SellDev &A, const double *val, const double *b, 
     a.eps = o.eps;
     a.inner_tol = o.inner_tol;
     void *args[] = {&a};
-    const int G = grid_for(n, mb);
+    const int G = grid_for(n, bicg_blocks_for(n, mb));
     SYSU_CUDA(cudaMemsetAsync(w.barrier.get(), 0, sizeof(GridBarrier), st));  // grid_sync starts from 0
     SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_bicgstab_mixed, dim3(G), dim3(KB), args, 0, st));
     ++::sysu::g_launches;
