@@ -50,6 +50,13 @@ namespace {
 // threads measured 3-8 % slower -- the FP32 one with 24 warps and 736-row tiles).  The last warp produces, the others
 // consume; a tile has one slice (32 rows) per consumer warp.
 constexpr int CGT64 = 640;
+// the FP64 kernel for rows wider than 5 entries (hex): on a 2.1M-cell hex cavity 640
+// threads measured 84.6 us per CG iteration, 512 threads 88.4 us; 7 gathers held
+// ahead instead of 6 measured the same (and spill)
+constexpr int CGT64_WIDE = 640;
+// threads of the FP64 CG instantiation that holds WR gathers a row ahead
+template <int WR>
+__host__ __device__ constexpr int cg64_threads() { return WR <= 5 ? CGT64 : CGT64_WIDE; }
 constexpr int CGT32 = 768;
 constexpr unsigned CG_SMEM_BUDGET = 200 * 1024;     // dynamic shared memory for the ring
 constexpr int CG_WR = 6;                            // gathers per row held in registers one tile ahead (FP64)
@@ -545,7 +552,8 @@ __device__ __forceinline__ V s_phase(const Part &P, Ring &R, const SellView &A, 
 // ---------------------------------------------------------------------------
 // FP64
 template <int WR>  // gathers per row held one tile ahead: 5 for rows of at most 5 entries (tets), else CG_WR
-__global__ void __launch_bounds__(CGT64, 1) k_cg_pipe(CgPipeArgs a) {
+__global__ void __launch_bounds__(cg64_threads<WR>(), 1) k_cg_pipe(CgPipeArgs a) {
+    constexpr int NT = cg64_threads<WR>();
     if (a.gate && a.gate->status[0] != DEV_STALLED) return;  // the same word for every block
     const int it_before = a.gate ? a.gate->iters[0] : 0;
     const int n = a.A.n;
@@ -565,7 +573,7 @@ __global__ void __launch_bounds__(CGT64, 1) k_cg_pipe(CgPipeArgs a) {
 
     // r = b - A x, z = M^-1 r; ||b||^2, ||r||^2, r.z
     double v3[3] = {0.0, 0.0, 0.0};
-    for (int i = R0 + tid; i < R1; i += CGT64) {
+    for (int i = R0 + tid; i < R1; i += NT) {
         double bi = a.b[i];
         double ri = bi - row_dot(a.A, i, a.x);
         double zi = a.dinv[i] * ri;
@@ -633,10 +641,10 @@ __global__ void __launch_bounds__(CGT64, 1) k_cg_pipe(CgPipeArgs a) {
         double v2[2] = {0.0, 0.0};
         if (rr_bias) {
             float rr32 = 0.f;
-            x_phase_est<CGT64, 4>(R0, R1, alpha, a.p, a.q, a.dinv, a.x, a.r, a.z, rr32, v2[1], rr_bias);
+            x_phase_est<NT, 4>(R0, R1, alpha, a.p, a.q, a.dinv, a.x, a.r, a.z, rr32, v2[1], rr_bias);
             v2[0] = (double)rr32;
         } else {
-            x_phase<double, CGT64, 4>(R0, R1, alpha, a.p, a.q, a.dinv, a.x, a.r, a.z, v2[0], v2[1]);
+            x_phase<double, NT, 4>(R0, R1, alpha, a.p, a.q, a.dinv, a.x, a.r, a.z, v2[0], v2[1]);
         }
         if (!grid_sum_t0<2>(v2, rc, a.gb, err) || fail_flag()) break;
         stamp(a.ts, it, 2);
@@ -658,7 +666,7 @@ __global__ void __launch_bounds__(CGT64, 1) k_cg_pipe(CgPipeArgs a) {
         __syncthreads();
         if (g_bc[5] != 0.0) {  // near (or below) the threshold: the exact FP64 r.r
             double e1[1] = {0.0};
-            for (int i = R0 + tid; i < R1; i += CGT64) e1[0] = fma(a.r[i], a.r[i], e1[0]);
+            for (int i = R0 + tid; i < R1; i += NT) e1[0] = fma(a.r[i], a.r[i], e1[0]);
             if (!grid_sum_t0<1>(e1, rc, a.gb, err)) break;
             if (tid == 0) {
                 rr = e1[0];
@@ -673,7 +681,7 @@ __global__ void __launch_bounds__(CGT64, 1) k_cg_pipe(CgPipeArgs a) {
     // (not after a failed wait, when the blocks no longer meet)
     if (s_rr_est && !fail_flag() && !(a.info->err)) {
         double e1[1] = {0.0};
-        for (int i = R0 + tid; i < R1; i += CGT64) e1[0] = fma(a.r[i], a.r[i], e1[0]);
+        for (int i = R0 + tid; i < R1; i += NT) e1[0] = fma(a.r[i], a.r[i], e1[0]);
         if (grid_sum_t0<1>(e1, rc, a.gb, err) && tid == 0) rr = e1[0];
         __syncthreads();
     }
@@ -987,7 +995,8 @@ static void cg_launch64(const SellDev &A, const double *val, const double *b, do
     auto kern = narrow ? k_cg_pipe<5> : k_cg_pipe<CG_WR>;
     static int maxb5 = 0, maxb6 = 0;
     int &maxb = narrow ? maxb5 : maxb6;
-    if (!maxb) maxb = cg_max_blocks(kern, CGT64);
+    const int nthreads = narrow ? cg64_threads<5>() : cg64_threads<CG_WR>();
+    if (!maxb) maxb = cg_max_blocks(kern, nthreads);
     w.ensure(n, 1, maxb, st);
     check_aligned16({val, A.col.get()});
     SellView V = view(A, val);
@@ -1010,11 +1019,11 @@ static void cg_launch64(const SellDev &A, const double *val, const double *b, do
     a.maxit = o.maxit;
     a.eps = o.eps;
     a.ts = w.phase_ts;
-    a.plan = plan_cg(A.wmax, 8, CGT64 / 32 - 1);
+    a.plan = plan_cg(A.wmax, 8, nthreads / 32 - 1);
     void *args[] = {&a};
     int G = cg_grid(A, a.plan, maxb, w.sm_cap);
     SYSU_CUDA(cudaMemsetAsync(w.barrier.get(), 0, sizeof(GridBarrier), st));  // grid_sync starts from 0
-    { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)kern, dim3(G), dim3(CGT64), args, a.plan.smem, st)); ++::sysu::g_launches; }
+    { SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)kern, dim3(G), dim3(nthreads), args, a.plan.smem, st)); ++::sysu::g_launches; }
 }
 
 void cg_solve(const SellDev &A, const double *val, const double *b, double *x, bool x0_zero,
