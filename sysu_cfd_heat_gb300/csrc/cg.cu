@@ -50,13 +50,14 @@ namespace {
 // threads measured 3-8 % slower -- the FP32 one with 24 warps and 736-row tiles).  The last warp produces, the others
 // consume; a tile has one slice (32 rows) per consumer warp.
 constexpr int CGT64 = 640;
-// the FP64 kernel for rows wider than 5 entries (hex): on a 2.1M-cell hex cavity 640
-// threads measured 84.6 us per CG iteration, 512 threads 88.4 us; 7 gathers held
-// ahead instead of 6 measured the same (and spill)
+// the look-ahead form for rows wider than 5 entries (hex) if it were used: on a 2.1M-cell
+// hex cavity 640 threads measured 84.6 us per CG iteration, 512 threads 88.4 us, 7
+// gathers held ahead the same as 6; the form without look-ahead on 1024 threads
+// measured 82.3 us and is the one wide rows get (cg_solve)
 constexpr int CGT64_WIDE = 640;
 // threads of the FP64 CG instantiation that holds WR gathers a row ahead
-template <int WR>
-__host__ __device__ constexpr int cg64_threads() { return WR <= 5 ? CGT64 : CGT64_WIDE; }
+template <int WR, bool AHEAD = true>
+__host__ __device__ constexpr int cg64_threads() { return !AHEAD ? 1024 : (WR <= 5 ? CGT64 : CGT64_WIDE); }
 constexpr int CGT32 = 768;
 constexpr unsigned CG_SMEM_BUDGET = 200 * 1024;     // dynamic shared memory for the ring
 constexpr int CG_WR = 6;                            // gathers per row held in registers one tile ahead (FP64)
@@ -450,7 +451,7 @@ __device__ __forceinline__ void x_phase(int R0, int R1, T alpha, const T *__rest
 // latency of the next (the warp holds two slots).  val: the matrix values of
 // this precision (read from global memory in direct mode).  The FMAs take a
 // row's entries in order, the first as a product, as tile_row_dot does.
-template <class V, int WR, class Epi>
+template <class V, int WR, class Epi, bool AHEAD = true>
 __device__ __forceinline__ void tiles_ahead(const Part &P, Ring &R, const SellView &A, const V *val, int direct,
                                             const V *pv, const V *qv, const V *__restrict__ zv, bool has_dir,
                                             int *err, Epi &&epi) {
@@ -517,6 +518,15 @@ __device__ __forceinline__ void tiles_ahead(const Part &P, Ring &R, const SellVi
         release_at(rslot);
         if (++rslot == R.depth) rslot = 0;
     };
+    if (!AHEAD) {  // one tile at a time: fetch, then the FMAs (fewer registers)
+        for (int t = 0; t < nt; ++t) {
+            if (!fetch(t, zc, pc, qc, ec, wc)) break;
+            finish(t, zc, pc, qc, ec, wc);
+        }
+        R.cslot = aslot;
+        R.cpar = apar;
+        return;
+    }
     bool ok = nt > 0 && fetch(0, zc, pc, qc, ec, wc);
     for (int t = 0; ok && t < nt; ++t) {
         if (t + 1 < nt && !fetch(t + 1, zn, pn, qn, en, wn)) break;
@@ -534,26 +544,29 @@ __device__ __forceinline__ void tiles_ahead(const Part &P, Ring &R, const SellVi
 
 // S phase of one CG iteration for a consumer warp: w = A z, p = z + beta p,
 // q = w + beta q; returns the thread's partial p.q.
-template <class V, int WR>
+template <class V, int WR, bool AHEAD = true>
 __device__ __forceinline__ V s_phase(const Part &P, Ring &R, const SellView &A, const V *val, int direct,
                                      V *__restrict__ pv, V *__restrict__ qv, const V *__restrict__ zv, V beta,
                                      bool has_dir, int *err) {
     V pq = 0;
-    tiles_ahead<V, WR>(P, R, A, val, direct, pv, qv, zv, has_dir, err, [&](int i, V w, V zi, V pp, V qq) {
+    auto epi = [&](int i, V w, V zi, V pp, V qq) {
         pp = fma_t(beta, pp, zi);
         qq = fma_t(beta, qq, w);
         pv[i] = pp;
         qv[i] = qq;
         pq = fma_t(pp, qq, pq);
-    });
+    };
+    tiles_ahead<V, WR, decltype(epi) &, AHEAD>(P, R, A, val, direct, pv, qv, zv, has_dir, err, epi);
     return pq;
 }
 
 // ---------------------------------------------------------------------------
 // FP64
-template <int WR>  // gathers per row held one tile ahead: 5 for rows of at most 5 entries (tets), else CG_WR
-__global__ void __launch_bounds__(cg64_threads<WR>(), 1) k_cg_pipe(CgPipeArgs a) {
-    constexpr int NT = cg64_threads<WR>();
+// WR: gathers per row held in registers (one tile ahead when AHEAD): 5 for rows of at
+// most 5 entries (tets), else CG_WR
+template <int WR, bool AHEAD = true>
+__global__ void __launch_bounds__(cg64_threads<WR, AHEAD>(), 1) k_cg_pipe(CgPipeArgs a) {
+    constexpr int NT = cg64_threads<WR, AHEAD>();
     if (a.gate && a.gate->status[0] != DEV_STALLED) return;  // the same word for every block
     const int it_before = a.gate ? a.gate->iters[0] : 0;
     const int n = a.A.n;
@@ -624,7 +637,7 @@ __global__ void __launch_bounds__(cg64_threads<WR>(), 1) k_cg_pipe(CgPipeArgs a)
         if (prod) {
             producer_tiles(R, base + nt, issue, err);
         } else {
-            v1[0] = s_phase<double, WR>(P, R, a.A, a.A.val, a.plan.direct, a.p, a.q, a.z, beta, it > 1, err);
+            v1[0] = s_phase<double, WR, AHEAD>(P, R, a.A, a.A.val, a.plan.direct, a.p, a.q, a.z, beta, it > 1, err);
         }
         base += nt;
         if (!grid_sum_t0<1>(v1, rc, a.gb, err) || fail_flag()) break;
@@ -989,13 +1002,14 @@ static void cg_launch64(const SellDev &A, const double *val, const double *b, do
                         cudaStream_t st) {
     int n = A.n;
     if (n == 0) return;
-    // rows of at most 5 entries (tets): 5 gathers held ahead, measured 2.5 % faster than
-    // 6 on the 2M-cell tet p' system; wider rows (hex: 7) keep 6
+    // rows of at most 5 entries (tets): 5 gathers held one tile ahead on 640 threads
+    // (2.5 % faster than 6 on the 2M-cell tet p' system); wider rows (hex: 7): one tile
+    // at a time on 1024 threads (3 % faster there than the look-ahead form)
     const bool narrow = A.wmax <= 5;
-    auto kern = narrow ? k_cg_pipe<5> : k_cg_pipe<CG_WR>;
+    auto kern = narrow ? k_cg_pipe<5, true> : k_cg_pipe<CG_WR, false>;
     static int maxb5 = 0, maxb6 = 0;
     int &maxb = narrow ? maxb5 : maxb6;
-    const int nthreads = narrow ? cg64_threads<5>() : cg64_threads<CG_WR>();
+    const int nthreads = narrow ? cg64_threads<5, true>() : cg64_threads<CG_WR, false>();
     if (!maxb) maxb = cg_max_blocks(kern, nthreads);
     w.ensure(n, 1, maxb, st);
     check_aligned16({val, A.col.get()});
