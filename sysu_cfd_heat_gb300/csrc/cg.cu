@@ -1005,11 +1005,15 @@ static void cg_launch64(const SellDev &A, const double *val, const double *b, do
     // rows of at most 5 entries (tets): 5 gathers held one tile ahead on 640 threads
     // (2.5 % faster than 6 on the 2M-cell tet p' system); wider rows (hex: 7): one tile
     // at a time on 1024 threads (3 % faster there than the look-ahead form)
-    const bool narrow = A.wmax <= 5;
-    auto kern = narrow ? k_cg_pipe<5, true> : k_cg_pipe<CG_WR, false>;
-    static int maxb5 = 0, maxb6 = 0;
-    int &maxb = narrow ? maxb5 : maxb6;
-    const int nthreads = narrow ? cg64_threads<5, true>() : cg64_threads<CG_WR, false>();
+    // (below 1M rows the wide form also looks ahead: the 256k-row hex p' system of the
+    // CHT channel is latency-bound and measured 7.99 ms per solve that way, 8.37 ms
+    // one tile at a time)
+    const bool narrow = A.wmax <= 5, wide_big = !narrow && n >= (1 << 20);
+    auto kern = narrow ? k_cg_pipe<5, true> : (wide_big ? k_cg_pipe<CG_WR, false> : k_cg_pipe<CG_WR, true>);
+    static int maxb5 = 0, maxb6 = 0, maxb6a = 0;
+    int &maxb = narrow ? maxb5 : (wide_big ? maxb6 : maxb6a);
+    const int nthreads = narrow ? cg64_threads<5, true>()
+                                : (wide_big ? cg64_threads<CG_WR, false>() : cg64_threads<CG_WR, true>());
     if (!maxb) maxb = cg_max_blocks(kern, nthreads);
     w.ensure(n, 1, maxb, st);
     check_aligned16({val, A.col.get()});
