@@ -24,7 +24,9 @@
 // at the start of X, so S starts on landed data.  In the FP64 kernel the
 // consumers work one tile ahead (the next tile's gathers in flight during the
 // current tile's FMAs: GB300's FP64 pipe, 1/64 of the FP32 rate, would
-// otherwise idle while every warp waits on its gathers at once).  The matrix is copied with an L2
+// otherwise idle while every warp waits on its gathers at once) -- except for
+// large systems with rows of more than 5 entries, which measured faster one
+// tile at a time on 1024 threads (cg_solve picks the form).  The matrix is copied with an L2
 // evict-first policy so that the Krylov vectors stay in L2.  X runs over the
 // CTA's rows with plain coalesced loads (all 32 warps, no per-tile
 // synchronisation).
