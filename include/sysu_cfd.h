@@ -218,10 +218,17 @@ const char *sysu_csr_last_error(void);
  *   - n must be <= SYSU_NOALLOC_MAX_ROWS, larger systems are rejected
  *     (SYSU_ERR_INPUT, message in sysu_noalloc_last_error());
  *   - every call shares the array; calls that overlap on the GPU race on it;
- *   - the first call on a device looks up the array's address with that device
- *     current -- make it before any stream capture.
- * stream: a cudaStream_t (NULL = default stream); the call waits for the
- * stream to read iters / res / status back. */
+ *   - every call looks the array's address up (cudaGetSymbolAddress, which
+ *     allocates nothing) with the calling thread's device current;
+ *   - every call waits for its stream to read iters / res / status back, so it
+ *     cannot be captured into a CUDA graph: on a capturing stream it returns
+ *     SYSU_ERR_INPUT and queues nothing;
+ *   - the CSR is the caller's responsibility; rows whose pointer decreases,
+ *     columns outside 0..n-1 and rows without a nonzero diagonal are detected
+ *     on the device and returned as SYSU_ERR_INPUT (lowest such row in the
+ *     message) without solving; rowptr[n] must not exceed the length of
+ *     d_col / d_val, which the call cannot check.
+ * stream: a cudaStream_t (NULL = default stream). */
 #define SYSU_NOALLOC_MAX_ROWS 262144
 int sysu_csr_cg_noalloc(int n, const int *d_rowptr, const int *d_col, const double *d_val, const double *d_b,
                         double *d_x, int maxit, double eps, double omega, void *stream, int *iters, double *res,

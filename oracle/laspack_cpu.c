@@ -15,6 +15,9 @@
  *   SYSU_ORACLE_CG_AS      = CG | BiCGSTAB        (what CGIter runs)
  *   SYSU_ORACLE_SSOR_AS    = SSOR | Jacobi | ILU  (what SSORPrecond applies)
  *   SYSU_ORACLE_RTC        = <eps>                (overrides SetRTCAccuracy)
+ *   SYSU_ORACLE_MAXIT      = <n>     replaces every call site's iteration cap
+ *                          (full-size parity runs at tight eps, where the
+ *                          p' cap of 1000 would stop the solve first)
  *   SYSU_ORACLE_GMRES_M    = <restart length>     (default 10)
  *   SYSU_ORACLE_DUMP_DIR   = <dir>   dump A (full CSR), b, x0, x of each solve
  *   SYSU_ORACLE_DUMP_MAX   = <n>     number of solves to dump (default 16)
@@ -624,6 +627,8 @@ static Vector *run_iter(int method, QMatrix *A, Vector *x, Vector *b, int MaxIte
         method = M_BICGSTAB;
     int pc = pc_kind(Precond);
     double eps = effective_eps();
+    const char *mi = getenv("SYSU_ORACLE_MAXIT");
+    if (mi && *mi && atoi(mi) > 0) MaxIter = atoi(mi);
     CsrView *v = build_view(A);
     size_t n = v->n;
     if (x->Dim != n || b->Dim != n) die("dimension mismatch");

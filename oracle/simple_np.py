@@ -317,8 +317,13 @@ def geometry(m: Mesh) -> Geom:
 # --------------------------------------------------------------------------------
 # Krylov -- the LASPack call sites (tools.cpp:56-64) with the restated algorithms
 def _csr_mv(rp, cl, vl, x):
+    """y = A x, each row summed over its entries in storage order (reduceat over the
+    non-empty rows; an empty row gives 0)."""
     y = np.zeros(len(rp) - 1)
-    np.add.at(y, np.repeat(np.arange(len(rp) - 1), np.diff(rp)), vl * x[cl])
+    prod = vl[:rp[-1]] * x[cl[:rp[-1]]]
+    nz = np.flatnonzero(np.diff(rp))
+    if nz.size:
+        y[nz] = np.add.reduceat(prod, np.asarray(rp)[nz])
     return y
 
 

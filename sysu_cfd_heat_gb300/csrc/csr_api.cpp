@@ -14,19 +14,48 @@
 
 namespace {
 thread_local std::string g_csr_err;
+
+// A non-blocking stream that is destroyed on every way out of the call,
+// exceptions included.
+struct OwnedStream {
+    cudaStream_t st = nullptr;
+    OwnedStream() { SYSU_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)); }
+    ~OwnedStream() {
+        if (st) cudaStreamDestroy(st);
+    }
+    OwnedStream(const OwnedStream &) = delete;
+    OwnedStream &operator=(const OwnedStream &) = delete;
+};
+
+// Argument errors (SYSU_ERR_INPUT) as opposed to CUDA/runtime errors.
+struct ArgError {
+    std::string msg;
+};
+
+void check_method(int method, int precond) {
+    if (method < 0 || method > 4) throw ArgError{"method: 0 CG, 1 BiCGSTAB, 2 CG-mixed, 3 GMRES, 4 BiCGSTAB-mixed"};
+    if (precond < 0 || precond > 3) throw ArgError{"precond: 0 none, 1 Jacobi, 2 SSOR, 3 ILU(0)"};
+    if ((method == 1 || method == 4) && precond > 1)
+        throw ArgError{"BiCGSTAB runs with no or the Jacobi preconditioner"};
+    if (method == 2 && precond != 1) throw ArgError{"the mixed-precision CG uses the Jacobi preconditioner"};
 }
+}  // namespace
 
 extern "C" {
 
-// method: 0 CG, 1 BiCGSTAB, 2 CG with FP32 recurrences (Jacobi), 3 GMRES(10);
+// method: 0 CG, 1 BiCGSTAB, 2 CG with FP32 recurrences (Jacobi), 3 GMRES(10),
+// 4 BiCGSTAB with FP32 inner iterations in FP64 defect correction;
 // precond: 0 none, 1 Jacobi (omega D^-1), 2 SSOR(omega), 3 ILU(0).
-// x holds x0 on entry and the solution on return.  Returns 0, or an error.
+// x holds x0 on entry and the solution on return.  Returns 0, SYSU_ERR_INPUT
+// for an argument error (checked before any device work), or SYSU_ERR_CUDA.
 int sysu_csr_solve(int method, int precond, int n, const int *rowptr, const int *col, const double *val,
                    const double *b, double *x, int maxit, double eps, double omega, int *iters, double *res,
                    int *status) {
     try {
-        cudaStream_t st;
-        SYSU_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        check_method(method, precond);
+        if (n < 1 || !rowptr || !col || !val || !b || !x) throw ArgError{"n >= 1 and non-null arrays required"};
+        OwnedStream os;
+        cudaStream_t st = os.st;
         {
             sysu::CsrDevice M;
             M.load(n, rowptr, col, val, st);
@@ -40,8 +69,6 @@ int sysu_csr_solve(int method, int precond, int n, const int *rowptr, const int 
             o.eps = eps;
             o.omega = omega;
             o.jacobi = precond == 1;
-            if (precond < 0 || precond > 3) throw sysu::CaseError{"precond: 0 none, 1 Jacobi, 2 SSOR, 3 ILU(0)"};
-            if (method == 1 && precond > 1) throw sysu::CaseError{"BiCGSTAB runs with no or the Jacobi preconditioner"};
             if (method == 0 && precond > 1) {
                 sysu::pcg_solve(M.A, M.val.get(), db.get(), dx.get(), false, o, precond, w, info.get(), st);
             } else if (method == 0) {
@@ -49,7 +76,6 @@ int sysu_csr_solve(int method, int precond, int n, const int *rowptr, const int 
             } else if (method == 3) {
                 sysu::gmres_solve(M.A, M.val.get(), db.get(), dx.get(), false, o, precond, 10, w, info.get(), st);
             } else if (method == 2) {
-                if (precond != 1) throw sysu::CaseError{"the mixed-precision CG uses the Jacobi preconditioner"};
                 sysu::DevBuf<float> v32(M.A.nnz);
                 sysu::sell_to_fp32(M.A, M.val.get(), v32.get(), st);
                 sysu::cg_solve_mixed(M.A, M.val.get(), v32.get(), db.get(), dx.get(), false, o, w, info.get(), st);
@@ -57,11 +83,8 @@ int sysu_csr_solve(int method, int precond, int n, const int *rowptr, const int 
                 const double *bb[1] = {db.get()};
                 double *xx[1] = {dx.get()};
                 sysu::bicgstab_solve(M.A, M.val.get(), 1, bb, xx, o, w, info.get(), st);
-            } else if (method == 4) {
-                if (precond > 1) throw sysu::CaseError{"BiCGSTAB runs with no or the Jacobi preconditioner"};
+            } else {  // method 4 (check_method admits nothing else)
                 sysu::bicgstab_solve_mixed(M.A, M.val.get(), db.get(), dx.get(), o, w, info.get(), st);
-            } else {
-                throw sysu::CaseError{"method: 0 CG, 1 BiCGSTAB, 2 CG-mixed, 3 GMRES, 4 BiCGSTAB-mixed"};
             }
             sysu::SolveInfo h;
             info.download(&h, 1, st);
@@ -71,8 +94,10 @@ int sysu_csr_solve(int method, int precond, int n, const int *rowptr, const int 
             if (res) *res = h.res[0];
             if (status) *status = h.err ? sysu::DEV_BARRIER_TIMEOUT : h.status[0];
         }
-        cudaStreamDestroy(st);
         return SYSU_OK;
+    } catch (const ArgError &e) {
+        g_csr_err = e.msg;
+        return SYSU_ERR_INPUT;
     } catch (const sysu::CaseError &e) {
         g_csr_err = e.msg;
         return SYSU_ERR_CUDA;
@@ -91,8 +116,8 @@ int sysu_set_spmv_variant(int variant) {
 // y = A x for a host CSR matrix, on the GPU.
 int sysu_csr_spmv(int n, const int *rowptr, const int *col, const double *val, const double *x, double *y) {
     try {
-        cudaStream_t st;
-        SYSU_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        OwnedStream os;
+        cudaStream_t st = os.st;
         {
             sysu::CsrDevice M;
             M.load(n, rowptr, col, val, st);
@@ -108,8 +133,10 @@ int sysu_csr_spmv(int n, const int *rowptr, const int *col, const double *val, c
             SYSU_CUDA(cudaStreamSynchronize(st));
             if (e != 0) throw sysu::CaseError{"sysu_csr_spmv: a bounded wait of the ring SpMV gave up"};
         }
-        cudaStreamDestroy(st);
         return SYSU_OK;
+    } catch (const ArgError &e) {
+        g_csr_err = e.msg;
+        return SYSU_ERR_INPUT;
     } catch (const sysu::CaseError &e) {
         g_csr_err = e.msg;
         return SYSU_ERR_CUDA;
@@ -122,9 +149,9 @@ int sysu_csr_bicgstab_batched3(int n, const int *rowptr, const int *col, const d
                                const double *const *b, double *const *x, int maxit, double eps, int *iters,
                                double *res, int *status) {
     try {
-        if (!vals || !b || !x) throw sysu::CaseError{"null argument"};
-        cudaStream_t st;
-        SYSU_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        if (!vals || !b || !x || n < 1 || !rowptr || !col) throw ArgError{"n >= 1 and non-null arrays required"};
+        OwnedStream os;
+        cudaStream_t st = os.st;
         {
             sysu::CsrDevice M;
             M.load(n, rowptr, col, vals[0], st);
@@ -165,8 +192,10 @@ int sysu_csr_bicgstab_batched3(int n, const int *rowptr, const int *col, const d
                 if (status) status[c] = h.err ? sysu::DEV_BARRIER_TIMEOUT : h.status[c];
             }
         }
-        cudaStreamDestroy(st);
         return SYSU_OK;
+    } catch (const ArgError &e) {
+        g_csr_err = e.msg;
+        return SYSU_ERR_INPUT;
     } catch (const sysu::CaseError &e) {
         g_csr_err = e.msg;
         return SYSU_ERR_CUDA;

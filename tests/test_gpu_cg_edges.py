@@ -157,3 +157,52 @@ def test_cg_many_tiles_per_cta(method):
     r = b - csr_spmv(rp, cl, vl, x)
     assert np.linalg.norm(r) / np.linalg.norm(b) < 2 * eps
     assert np.linalg.norm(x - xo) <= 1e-6 * np.linalg.norm(xo)
+
+
+def grid7(m, seed, dominance):
+    """7-point stencil on an m^3 grid, random symmetric positive couplings, diagonal
+    `dominance` times the row's coupling sum (rows of up to 7 entries)."""
+    rng = np.random.default_rng(seed)
+    n = m ** 3
+    idx = np.arange(n).reshape(m, m, m)
+    Is, Js, Vs = [], [], []
+    for ax in range(3):
+        a = np.take(idx, range(m - 1), axis=ax).ravel()
+        b = np.take(idx, range(1, m), axis=ax).ravel()
+        w = -rng.uniform(0.5, 1.5, a.size)
+        Is += [a, b]
+        Js += [b, a]
+        Vs += [w, w]
+    I, J, V = np.concatenate(Is), np.concatenate(Js), np.concatenate(Vs)
+    diag = np.zeros(n)
+    np.add.at(diag, I, -V)
+    I = np.concatenate([I, np.arange(n)])
+    J = np.concatenate([J, np.arange(n)])
+    V = np.concatenate([V, dominance * diag])
+    o = np.lexsort((J, I))
+    I, J, V = I[o], J[o], V[o]
+    rp = np.zeros(n + 1, np.int64)
+    np.add.at(rp, I + 1, 1)
+    return np.cumsum(rp).astype(np.int32), J.astype(np.int32), V
+
+
+def test_cg_wide_rows_above_one_million():
+    """128^3 = 2,097,152 rows of up to 7 entries: the FP64 kernel's one-tile-at-a-time
+    form on 1024 threads (rows wider than 5 at >= 2^20 rows; the hex-mesh p' systems
+    of the large channel run it), and the FP32 form on the same system."""
+    rp, cl, vl = grid7(128, seed=21, dominance=1.01)
+    n = len(rp) - 1
+    assert np.diff(rp).max() == 7 and n >= 1 << 20
+    b = np.random.default_rng(22).standard_normal(n)
+    eps = 1e-9
+    d = vl[cl == np.repeat(np.arange(n), np.diff(rp))]
+    xo, ito, reso = oracle_cg((rp, cl, vl, d), b, np.zeros(n), 5000, eps, 1.0)
+    assert reso < eps
+    for method in ("CG", "CG-mixed"):
+        x, it, res, st = csr_solve(rp, cl, vl, b, None, method=method, maxit=5000, eps=eps, omega=1.0)
+        assert st == 0 and res < eps, (method, st, it, res)
+        if method == "CG":
+            assert abs(it - ito) <= 1, (it, ito)
+        r = b - csr_spmv(rp, cl, vl, x)
+        assert np.linalg.norm(r) / np.linalg.norm(b) < 2 * eps, method
+        assert np.linalg.norm(x - xo) <= 1e-6 * np.linalg.norm(xo), method
