@@ -181,8 +181,12 @@ long sysu_solver_matrix(sysu_solver *s, const char *which, int *rowptr, int *col
  * any column order).  method: 0 CG, 1 BiCGSTAB, 2 CG with FP32 recurrences and
  * FP64 reliable updates (Jacobi only; iters = FP32 iterations), 3 GMRES(10)
  * right preconditioned, 4 BiCGSTAB with FP32 inner iterations in FP64 defect
- * correction (none or Jacobi; iters = FP32 iterations); precond: 0 none, 1 Jacobi (y = omega D^-1 c), 2 SSOR(omega),
- * 3 ILU(0) (level-scheduled sweeps; not with BiCGSTAB).  Stopping test ||b - A x||_2 / ||b||_2 < eps, as the
+ * correction (none or Jacobi; iters = FP32 iterations), 5 flexible CG with FP32
+ * recurrences and FP64 reliable updates preconditioned by the aggregation-
+ * multigrid V-cycle (symmetric matrices; precond 4, omega = the smoother's
+ * Jacobi weight, 0.8 suits the p' systems; iters = FP32 iterations);
+ * precond: 0 none, 1 Jacobi (y = omega D^-1 c), 2 SSOR(omega),
+ * 3 ILU(0) (level-scheduled sweeps; not with BiCGSTAB), 4 multigrid (method 5 only).  Stopping test ||b - A x||_2 / ||b||_2 < eps, as the
  * reference's SolveLinearEqu (tools.cpp:56-64) expects.  x: x0 in, solution out.
  * status: 0 converged, 1 max iterations, 2 breakdown, 3 barrier timeout,
  * 4 non-finite (a mixed solve whose FP32 refinement stalls is finished by the
@@ -205,6 +209,21 @@ int sysu_csr_bicgstab_batched3(int n, const int *rowptr, const int *col, const d
                                const double *const *b, double *const *x, int maxit, double eps, int *iters,
                                double *res, int *status);
 const char *sysu_csr_last_error(void);
+
+/* ---- aggregation-multigrid hierarchy (host only, no device work) -----------
+ * No counterpart in the reference (its p' solve is CG + SSOR,
+ * navier_pressure.cpp:29).  The hierarchy that p' option precond 4 and method 5
+ * build, for a host CSR matrix: greedy aggregation at strength threshold theta,
+ * Galerkin coarse levels until a level has at most dense_max rows.
+ * sysu_mg_hierarchy: number of levels, rows and entries per level (up to
+ * max_levels).  sysu_mg_level: aggregate of each row of `level` (agg, may be
+ * NULL) and that level's matrix as CSR with the diagonal first (rowptr_out of
+ * rows + 1, col_out / val_out of the level's entry count; may be NULL). */
+int sysu_mg_hierarchy(int n, const int *rowptr, const int *col, const double *val, double theta, int dense_max,
+                      int max_levels, int *nlevels, int *rows, long *nnz);
+int sysu_mg_level(int n, const int *rowptr, const int *col, const double *val, double theta, int dense_max,
+                  int level, int *agg, int *rowptr_out, int *col_out, double *val_out);
+const char *sysu_mg_last_error(void);
 
 /* ---- Jacobi-CG that allocates nothing ----------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc:
@@ -305,6 +324,20 @@ int sysu_gnn_train(sysu_gnn *g, int steps, double lr, int loss_kind, double *los
 int sysu_gnn_fcg(sysu_gnn *g, const double *b, double *x, int x0_zero, int maxit, double eps, double inner_tol,
                  int use_gnn, int stall_max, int *iters, double *res, int *status, int *fallback_at,
                  int *refinements, double *seconds);
+/* Multigrid form (no counterpart in the reference): on = 1 builds the
+ * aggregation-multigrid hierarchy of the handle's matrix (strength theta,
+ * smoother weight omega, coarse-correction scale gamma) and attaches it: from
+ * then on sysu_gnn_fcg is preconditioned by the V-cycle whose finest
+ * post-smoothing step is the network (use_gnn = 1) or Jacobi (use_gnn = 0),
+ * sysu_gnn_set_values refreshes its coarse levels, and pairs added with
+ * sysu_gnn_add_pair become pairs of the post-smoother,
+ * (r, e) -> (r - A z2(r), e - z2(r)) with z2 the cycle before post-smoothing.
+ * levels / rows (up to max_levels; may be NULL) report the hierarchy.
+ * on = 0 detaches it. */
+int sysu_gnn_set_multigrid(sysu_gnn *g, int on, double theta, double omega, double gamma, int *levels, int *rows,
+                           int max_levels);
+/* z = M(r): one application of the attached cycle (host vectors of n values) */
+int sysu_gnn_mg_apply(sysu_gnn *g, const double *r, double *z, int use_gnn);
 /* hidden state h^layer (layer 1..4) of the network on r, FP32 [n][32] */
 int sysu_gnn_hidden(sysu_gnn *g, const double *r, int layer, float *h);
 /* device ms of one network application on r (mean of reps); fwd_per_sm > 0

@@ -104,6 +104,12 @@ def lib() -> C.CDLL:
             "sysu_gnn_hidden": (C.c_int, [vp, dp, C.c_int, fp]),
             "sysu_gnn_time_apply": (C.c_int, [vp, dp, C.c_int, C.c_int, dp]),
             "sysu_gnn_last_error": (cp, []),
+            "sysu_gnn_set_multigrid": (C.c_int, [vp, C.c_int, C.c_double, C.c_double, C.c_double, ip, ip,
+                                                 C.c_int]),
+            "sysu_gnn_mg_apply": (C.c_int, [vp, dp, dp, C.c_int]),
+            "sysu_mg_hierarchy": (C.c_int, [C.c_int, ip, ip, dp, C.c_double, C.c_int, C.c_int, ip, ip, lp]),
+            "sysu_mg_level": (C.c_int, [C.c_int, ip, ip, dp, C.c_double, C.c_int, C.c_int, ip, ip, ip, dp]),
+            "sysu_mg_last_error": (cp, []),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)

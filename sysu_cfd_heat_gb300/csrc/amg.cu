@@ -1,0 +1,383 @@
+// Device part of the aggregation multigrid (see amg.hpp): Galerkin values,
+// smoother weights, the coarsest-level inverse and the V-cycle kernels.
+//
+// Every cycle kernel is a flat grid-stride loop over rows (SELL-32: thread i
+// reads row i's entries at sl_ptr[i/32] + 32 k + i%32, so a warp's loads are
+// coalesced) and returns at once when the flexible CG it serves has finished
+// (*done != 0), so a captured chunk of iterations costs little past convergence.
+#include <algorithm>
+#include <cmath>
+#include <memory>
+
+#include "amg.hpp"
+#include "krylov_dev.cuh"
+
+namespace sysu {
+namespace {
+
+constexpr int MB = 256;  // threads per block of the flat kernels
+constexpr int DENSE_THREADS = 1024;
+
+struct MgView {
+    int n;
+    const int *sl_ptr, *sl_w, *col;
+    const float *val;
+};
+
+int flat_blocks(long n) { return (int)std::max(1L, std::min((n + MB - 1) / MB, (long)num_sms() * 8)); }
+
+// coarse value at stored position q = sum of its fine entries (fixed order)
+__global__ void k_mg_galerkin(long npos, const int *gal_ptr, const int *gal_src, const double *fval, double *cval,
+                              float *cval32) {
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < npos; q += (long)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int k = gal_ptr[q]; k < gal_ptr[q + 1]; ++k) s += fval[gal_src[k]];
+        cval[q] = s;
+        cval32[q] = (float)s;
+    }
+}
+
+// w_i = omega / a_ii (entry 0 of row i is its diagonal)
+__global__ void k_mg_weights(int n, const int *sl_ptr, const double *val, double omega, float *w) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double d = val[sl_ptr[i >> 5] + (i & 31)];
+        w[i] = (float)(d != 0.0 ? omega / d : 0.0);
+    }
+}
+
+__device__ __forceinline__ float row_times(const MgView &A, int i, const float *x) {
+    const int base = A.sl_ptr[i >> 5], wd = A.sl_w[i >> 5], lane = i & 31;
+    float s = 0.f;
+    for (int k = 0; k < wd; ++k) {
+        const int pos = base + k * 32 + lane;
+        s += A.val[pos] * x[A.col[pos]];
+    }
+    return s;
+}
+
+// t = r - A (w r)   (pre-smoothing from zero and its residual)
+__global__ void k_mg_down(MgView A, const float *w, const float *r, float *t, const int *done) {
+    if (done && *done) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x) {
+        const int base = A.sl_ptr[i >> 5], wd = A.sl_w[i >> 5], lane = i & 31;
+        float s = 0.f;
+        for (int k = 0; k < wd; ++k) {
+            const int pos = base + k * 32 + lane;
+            const int j = A.col[pos];
+            s += A.val[pos] * (w[j] * r[j]);
+        }
+        t[i] = r[i] - s;
+    }
+}
+
+// rc[I] = sum of t over the rows of aggregate I (ascending)
+__global__ void k_mg_restrict(int nc, const int *mem_ptr, const int *mem_idx, const float *t, float *rc,
+                              const int *done) {
+    if (done && *done) return;
+    for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < nc; I += gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int k = mem_ptr[I]; k < mem_ptr[I + 1]; ++k) s += t[mem_idx[k]];
+        rc[I] = s;
+    }
+}
+
+// z_i = w_i r_i + gamma zc[agg(i)]
+__global__ void k_mg_prolong(int n, const float *w, const float *r, const int *agg, const float *zc, float gamma,
+                             float *z, const int *done) {
+    if (done && *done) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        z[i] = w[i] * r[i] + gamma * zc[agg[i]];
+}
+
+// zout = z + w (r - A z)
+__global__ void k_mg_post(MgView A, const float *w, const float *r, const float *z, float *zout, const int *done) {
+    if (done && *done) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x)
+        zout[i] = z[i] + w[i] * (r[i] - row_times(A, i, z));
+}
+
+// t = r - A z
+__global__ void k_mg_resid(MgView A, const float *r, const float *z, float *t, const int *done) {
+    if (done && *done) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x)
+        t[i] = r[i] - row_times(A, i, z);
+}
+
+// e -= z (training pair of the post-smoother)
+__global__ void k_mg_sub(int n, float *e, const float *z) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) e[i] -= z[i];
+}
+
+// z = w r (a coarsest level too large for the dense inverse: Jacobi sweeps)
+__global__ void k_mg_scale(int n, const float *w, const float *r, float *z, const int *done) {
+    if (done && *done) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) z[i] = w[i] * r[i];
+}
+
+// z = Minv r on the dense coarsest level (one CTA; a warp per row)
+__global__ void __launch_bounds__(DENSE_THREADS) k_mg_dense_apply(int nd, const float *minv, const float *r,
+                                                                   float *z, const int *done) {
+    if (done && *done) return;
+    __shared__ float rs[MG_DENSE_MAX];
+    for (int j = threadIdx.x; j < nd; j += blockDim.x) rs[j] = r[j];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int i = warp; i < nd; i += nw) {
+        float s = 0.f;
+        for (int j = lane; j < nd; j += 32) s += minv[(size_t)i * nd + j] * rs[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL_MASK, s, o);
+        if (lane == 0) z[i] = s;
+    }
+}
+
+// Dense inverse of the coarsest level (FP32 Gauss-Jordan, no pivoting: the p'
+// operators are weakly diagonally dominant), one CTA, matrix in shared memory.
+// A level whose rows sum to zero (relative 1e-9) gets alpha 1 1^T first,
+// alpha = mean(a_ii) / nd.  *err = 1 if a pivot vanishes.
+__global__ void __launch_bounds__(DENSE_THREADS) k_mg_dense_inverse(int nd, const int *sl_ptr, const int *sl_w,
+                                                                     const int *col, const double *val, float *minv,
+                                                                     int *err) {
+    extern __shared__ float M[];  // nd x nd
+    __shared__ float fcol[MG_DENSE_MAX];
+    __shared__ double s_rowsum, s_diag, s_dsum;
+    __shared__ int s_bad;
+    const int tid = threadIdx.x;
+    for (int q = tid; q < nd * nd; q += blockDim.x) M[q] = 0.f;
+    if (tid == 0) {
+        s_rowsum = 0.0;
+        s_diag = 0.0;
+        s_dsum = 0.0;
+        s_bad = 0;
+    }
+    __syncthreads();
+    if (tid < 32) {
+        // row sums and diagonal in FP64, one lane per row (lane-ordered max/sum)
+        double rmax = 0.0, dmax = 0.0, dsum = 0.0;
+        for (int i = tid; i < nd; i += 32) {
+            const int base = sl_ptr[i >> 5], wd = sl_w[i >> 5], lane = i & 31;
+            double rs = 0.0;
+            for (int k = 0; k < wd; ++k) rs += val[base + k * 32 + lane];
+            const double d = val[base + lane];
+            rmax = fmax(rmax, fabs(rs));
+            dmax = fmax(dmax, fabs(d));
+            dsum += d;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            rmax = fmax(rmax, __shfl_xor_sync(FULL_MASK, rmax, o));
+            dmax = fmax(dmax, __shfl_xor_sync(FULL_MASK, dmax, o));
+            dsum += __shfl_xor_sync(FULL_MASK, dsum, o);
+        }
+        if (tid == 0) {
+            s_rowsum = rmax;
+            s_diag = dmax;
+            s_dsum = dsum;
+        }
+    }
+    __syncthreads();
+    const bool singular = s_rowsum <= 1e-9 * s_diag;
+    const float alpha = singular ? (float)(s_dsum / nd / nd) : 0.f;
+    // scatter the rows (padding entries add 0 to their own diagonal)
+    for (int i = tid; i < nd; i += blockDim.x) {
+        const int base = sl_ptr[i >> 5], wd = sl_w[i >> 5], lane = i & 31;
+        for (int k = 0; k < wd; ++k) {
+            const int pos = base + k * 32 + lane;
+            M[i * nd + col[pos]] += (float)val[pos];
+        }
+    }
+    __syncthreads();
+    if (singular)
+        for (int q = tid; q < nd * nd; q += blockDim.x) M[q] += alpha;
+    __syncthreads();
+    for (int k = 0; k < nd; ++k) {
+        const float p = M[k * nd + k];
+        if (!(fabsf(p) > 0.f) || !isfinite(p)) {
+            if (tid == 0) s_bad = 1;
+            break;  // uniform: every thread read the same pivot
+        }
+        for (int i = tid; i < nd; i += blockDim.x) fcol[i] = i == k ? 0.f : M[i * nd + k];
+        __syncthreads();
+        const float inv = 1.0f / p;
+        for (int j = tid; j < nd; j += blockDim.x) M[k * nd + j] = (j == k ? 1.0f : M[k * nd + j]) * inv;
+        __syncthreads();
+        for (int q = tid; q < nd * nd; q += blockDim.x) {
+            const int i = q / nd, j = q - i * nd;
+            if (i == k) continue;
+            if (j == k) M[q] = -fcol[i] * M[k * nd + k];
+            else M[q] -= fcol[i] * M[k * nd + j];
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    if (s_bad) {
+        if (tid == 0) atomicExch(err, 1);
+        return;
+    }
+    for (int q = tid; q < nd * nd; q += blockDim.x) minv[q] = M[q];
+}
+
+MgView view_of(const SellDev &A, const float *val) { return MgView{A.n, A.sl_ptr.get(), A.sl_w.get(), A.col.get(), val}; }
+
+}  // namespace
+
+void AggMultigrid::setup(const SellDev &A, const SellPattern &pat, const double *val64_dev, double theta,
+                         cudaStream_t st) {
+    A0_ = &A;
+    std::vector<double> hv(pat.nnz);
+    SYSU_CUDA(cudaMemcpyAsync(hv.data(), val64_dev, sizeof(double) * pat.nnz, cudaMemcpyDeviceToHost, st));
+    SYSU_CUDA(cudaStreamSynchronize(st));
+    sgn_ = hv.empty() || hv[0] >= 0.0 ? 1.0f : -1.0f;
+    std::vector<MgHostLevel> H = mg_build_hierarchy(pat, hv, theta, MG_DENSE_MAX);
+    lv_.clear();
+    for (size_t l = 0; l < H.size(); ++l) {
+        auto d = std::make_unique<MgLevelDev>();
+        const MgHostLevel &h = H[l];
+        d->n = h.n;
+        if (l > 0) {
+            d->A.upload(h.pat, st);
+            d->val64.alloc(h.pat.nnz);
+            d->val32.alloc(h.pat.nnz);
+        }
+        d->w.alloc(h.n);
+        d->r.alloc(h.n);
+        d->z.alloc(h.n);
+        d->t.alloc(h.n);
+        if (!h.agg.empty()) {
+            d->agg.upload(h.agg, st);
+            d->mem_ptr.upload(h.mem_ptr, st);
+            d->mem_idx.upload(h.mem_idx, st);
+            d->gal_ptr.upload(h.gal_ptr, st);
+            d->gal_src.upload(h.gal_src, st);
+        }
+        lv_.push_back(std::move(d));
+    }
+    nd_ = lv_.back()->n;
+    if (lv_.size() > 1 && nd_ <= MG_DENSE_MAX) dinv_.alloc((size_t)nd_ * nd_);
+    tmpz_.alloc(A.n);
+    tmpt_.alloc(A.n);
+    err_.alloc(1);
+    err_.zero(st);
+    static bool attr = false;
+    if (!attr) {
+        SYSU_CUDA(cudaFuncSetAttribute(k_mg_dense_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       MG_DENSE_MAX * MG_DENSE_MAX * (int)sizeof(float)));
+        attr = true;
+    }
+    SYSU_CUDA(cudaStreamSynchronize(st));  // the host hierarchy goes out of scope
+}
+
+void AggMultigrid::refresh(const double *val64_dev, const float *val32_dev, cudaStream_t st) {
+    if (!ready()) throw CaseError{"multigrid: no hierarchy"};
+    val0_32_ = val32_dev;
+    const double *fval = val64_dev;
+    for (size_t l = 0; l < lv_.size(); ++l) {
+        MgLevelDev &d = *lv_[l];
+        const SellDev &A = l == 0 ? *A0_ : d.A;
+        const double *v = l == 0 ? val64_dev : d.val64.get();
+        if (l > 0) {
+            const MgLevelDev &f = *lv_[l - 1];
+            k_mg_galerkin<<<flat_blocks(A.nnz), MB, 0, st>>>(A.nnz, f.gal_ptr.get(), f.gal_src.get(), fval,
+                                                              d.val64.get(), d.val32.get());
+            ++g_launches;
+        }
+        k_mg_weights<<<flat_blocks(A.n), MB, 0, st>>>(A.n, A.sl_ptr.get(), v, omega, d.w.get());
+        ++g_launches;
+        fval = v;
+    }
+    if (lv_.size() > 1 && nd_ <= MG_DENSE_MAX) {
+        const MgLevelDev &c = *lv_.back();
+        k_mg_dense_inverse<<<1, DENSE_THREADS, (size_t)nd_ * nd_ * sizeof(float), st>>>(
+            nd_, c.A.sl_ptr.get(), c.A.sl_w.get(), c.A.col.get(), c.val64.get(), dinv_.get(), err_.get());
+        ++g_launches;
+    }
+    SYSU_CUDA(cudaGetLastError());
+}
+
+// level l (l < coarsest): t = r - A (w r) on level l, restricted into level l+1's r
+void AggMultigrid::enqueue_down(int l, const float *r, const int *done, cudaStream_t st) {
+    MgLevelDev &d = *lv_[l];
+    MgLevelDev &c = *lv_[l + 1];
+    const SellDev &A = l == 0 ? *A0_ : d.A;
+    const float *v32 = l == 0 ? val0_32_ : d.val32.get();
+    k_mg_down<<<flat_blocks(A.n), MB, 0, st>>>(view_of(A, v32), d.w.get(), r, d.t.get(), done);
+    k_mg_restrict<<<flat_blocks(c.n), MB, 0, st>>>(c.n, d.mem_ptr.get(), d.mem_idx.get(), d.t.get(), c.r.get(), done);
+    g_launches += 2;
+}
+
+// level l >= 1 (not the coarsest): prolong the coarse correction and post-smooth
+// into zout (level l's z holds the prolonged value)
+void AggMultigrid::enqueue_up(int l, float *zout, const int *done, cudaStream_t st) {
+    MgLevelDev &d = *lv_[l];
+    MgLevelDev &c = *lv_[l + 1];
+    const SellDev &A = d.A;
+    k_mg_prolong<<<flat_blocks(d.n), MB, 0, st>>>(d.n, d.w.get(), d.r.get(), d.agg.get(), c.z.get(), (float)gamma,
+                                                   d.t.get(), done);
+    k_mg_post<<<flat_blocks(d.n), MB, 0, st>>>(view_of(A, d.val32.get()), d.w.get(), d.r.get(), d.t.get(), zout,
+                                                done);
+    g_launches += 2;
+}
+
+// Levels 1.. of the cycle for the residual r at level 0; leaves the prolonged
+// fine correction (w r + gamma P z_1) in z.
+void AggMultigrid::enqueue_cycle_to_fine(const float *r, float *z, const int *done, cudaStream_t st) {
+    const int L = (int)lv_.size();
+    MgLevelDev &f = *lv_[0];
+    if (L == 1) {  // no coarse level: Jacobi
+        k_mg_scale<<<flat_blocks(f.n), MB, 0, st>>>(f.n, f.w.get(), r, z, done);
+        ++g_launches;
+        return;
+    }
+    enqueue_down(0, r, done, st);
+    for (int l = 1; l < L - 1; ++l) enqueue_down(l, lv_[l]->r.get(), done, st);
+    MgLevelDev &c = *lv_[L - 1];
+    if (nd_ <= MG_DENSE_MAX) {
+        k_mg_dense_apply<<<1, DENSE_THREADS, 0, st>>>(nd_, dinv_.get(), c.r.get(), c.z.get(), done);
+        ++g_launches;
+    } else {  // coarsest too large for the dense inverse: three Jacobi steps from zero
+        k_mg_scale<<<flat_blocks(c.n), MB, 0, st>>>(c.n, c.w.get(), c.r.get(), c.z.get(), done);
+        k_mg_post<<<flat_blocks(c.n), MB, 0, st>>>(view_of(c.A, c.val32.get()), c.w.get(), c.r.get(), c.z.get(),
+                                                   c.t.get(), done);
+        k_mg_post<<<flat_blocks(c.n), MB, 0, st>>>(view_of(c.A, c.val32.get()), c.w.get(), c.r.get(), c.t.get(),
+                                                   c.z.get(), done);
+        g_launches += 3;
+    }
+    for (int l = L - 2; l >= 1; --l) enqueue_up(l, lv_[l]->z.get(), done, st);
+    MgLevelDev &c1 = *lv_[1];
+    k_mg_prolong<<<flat_blocks(f.n), MB, 0, st>>>(f.n, f.w.get(), r, f.agg.get(), c1.z.get(), (float)gamma, z, done);
+    ++g_launches;
+}
+
+void AggMultigrid::apply_fixed(const float *r, float *z2, float *t, const int *fs_done, cudaStream_t st) {
+    enqueue_cycle_to_fine(r, z2, fs_done, st);
+    k_mg_resid<<<flat_blocks(A0_->n), MB, 0, st>>>(view_of(*A0_, val0_32_), r, z2, t, fs_done);
+    ++g_launches;
+    SYSU_CUDA(cudaGetLastError());
+}
+
+void AggMultigrid::apply(const float *r, float *z, const int *fs_done, cudaStream_t st) {
+    enqueue_cycle_to_fine(r, tmpz_.get(), fs_done, st);
+    k_mg_post<<<flat_blocks(A0_->n), MB, 0, st>>>(view_of(*A0_, val0_32_), lv_[0]->w.get(), r, tmpz_.get(), z,
+                                                  fs_done);
+    ++g_launches;
+    SYSU_CUDA(cudaGetLastError());
+}
+
+void AggMultigrid::smoother_pair(float *r, float *e, cudaStream_t st) {
+    apply_fixed(r, tmpz_.get(), tmpt_.get(), nullptr, st);
+    const int n = A0_->n;
+    SYSU_CUDA(cudaMemcpyAsync(r, tmpt_.get(), sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+    k_mg_sub<<<flat_blocks(n), MB, 0, st>>>(n, e, tmpz_.get());
+    ++g_launches;
+    SYSU_CUDA(cudaGetLastError());
+}
+
+int AggMultigrid::err_flag(cudaStream_t st) {
+    int e = 0;
+    if (err_.size()) {
+        err_.download(&e, 1, st);
+        SYSU_CUDA(cudaStreamSynchronize(st));
+    }
+    return e;
+}
+
+}  // namespace sysu

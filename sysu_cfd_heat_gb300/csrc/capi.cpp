@@ -233,7 +233,7 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
                     return set_err(SYSU_ERR_INPUT, "mixed precision is available for p, ke, t and ts (not momentum)");
                 if (value != 0.0 && e->kind == sysu::SK_GMRES)
                     return set_err(SYSU_ERR_INPUT, "mixed precision is available for CG and BiCGSTAB solves");
-                if (value != 0.0 && e->kind == sysu::SK_CG && e->precond != sysu::PK_JACOBI)
+                if (value != 0.0 && e->kind == sysu::SK_CG && e->precond != sysu::PK_JACOBI && e->precond != sysu::PK_AMG)
                     return set_err(SYSU_ERR_INPUT, "the mixed-precision CG uses the Jacobi preconditioner");
                 if (value != 0.0 && o.scalars_batched && (e == &o.ke || e == &o.t))
                     return set_err(SYSU_ERR_INPUT, "scalars_batched solves k, eps and T in FP64; turn it off first");
@@ -256,12 +256,16 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
             }
             if (f == "precond") {
                 int pc = (int)value;
-                if (pc < sysu::PK_NONE || pc > sysu::PK_ILU0)
-                    return set_err(SYSU_ERR_INPUT, "precond: 0 none, 1 Jacobi, 2 SSOR, 3 ILU(0)");
+                if (pc < sysu::PK_NONE || pc > sysu::PK_AMG)
+                    return set_err(SYSU_ERR_INPUT, "precond: 0 none, 1 Jacobi, 2 SSOR, 3 ILU(0), 4 multigrid (p')");
+                if (pc == sysu::PK_AMG && (e != &o.p || e->kind != sysu::SK_CG))
+                    return set_err(SYSU_ERR_INPUT, "the multigrid preconditioner is for the p' CG");
                 if (pc > sysu::PK_JACOBI && e->kind == sysu::SK_BICGSTAB)
                     return set_err(SYSU_ERR_INPUT, "BiCGSTAB runs with no or the Jacobi preconditioner");
-                if (pc != sysu::PK_JACOBI && e->mixed)
+                if (pc != sysu::PK_JACOBI && pc != sysu::PK_AMG && e->mixed)
                     return set_err(SYSU_ERR_INPUT, "the mixed-precision CG uses the Jacobi preconditioner");
+                if (e->learned && pc != sysu::PK_JACOBI && pc != sysu::PK_AMG)
+                    return set_err(SYSU_ERR_INPUT, "the learned form runs with the Jacobi or multigrid preconditioner");
                 e->precond = pc;
                 return SYSU_OK;
             }
@@ -272,12 +276,28 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
                 return SYSU_OK;
             }
             if (f == "learned") {
-                if (value != 0.0 && (e != &o.p || e->kind != sysu::SK_CG || e->precond != sysu::PK_JACOBI))
-                    return set_err(SYSU_ERR_INPUT, "the learned preconditioner is for the p' CG (Jacobi mode)");
+                if (value != 0.0 && (e != &o.p || e->kind != sysu::SK_CG ||
+                                     (e->precond != sysu::PK_JACOBI && e->precond != sysu::PK_AMG)))
+                    return set_err(SYSU_ERR_INPUT, "the learned preconditioner is for the p' CG (Jacobi or multigrid mode)");
                 e->learned = value != 0.0;
                 return SYSU_OK;
             }
             if (f == "learn_iters") { e->learn_iters = std::max(0, (int)value); return SYSU_OK; }
+            if (f == "mg_theta") {
+                if (!(value > 0.0 && value < 1.0)) return set_err(SYSU_ERR_INPUT, "mg_theta: strength threshold in (0, 1)");
+                e->mg_theta = value;
+                return SYSU_OK;
+            }
+            if (f == "mg_omega") {
+                if (!(value > 0.0 && value < 2.0)) return set_err(SYSU_ERR_INPUT, "mg_omega: Jacobi weight in (0, 2)");
+                e->mg_omega = value;
+                return SYSU_OK;
+            }
+            if (f == "mg_gamma") {
+                if (!(value > 0.0 && value <= 4.0)) return set_err(SYSU_ERR_INPUT, "mg_gamma: correction scale in (0, 4]");
+                e->mg_gamma = value;
+                return SYSU_OK;
+            }
             if (f == "learn_steps") { e->learn_steps = std::max(0, (int)value); return SYSU_OK; }
             if (f == "learn_lr") { e->learn_lr = value; return SYSU_OK; }
             if (f == "learn_kind") {
@@ -320,6 +340,9 @@ int sysu_solver_get_option(sysu_solver *s, const char *key, double *value) {
             if (f == "inner_tol") { *value = e->inner_tol; return SYSU_OK; }
             if (f == "learned") { *value = e->learned; return SYSU_OK; }
             if (f == "learn_iters") { *value = e->learn_iters; return SYSU_OK; }
+            if (f == "mg_theta") { *value = e->mg_theta; return SYSU_OK; }
+            if (f == "mg_omega") { *value = e->mg_omega; return SYSU_OK; }
+            if (f == "mg_gamma") { *value = e->mg_gamma; return SYSU_OK; }
             if (f == "learn_steps") { *value = e->learn_steps; return SYSU_OK; }
             if (f == "learn_lr") { *value = e->learn_lr; return SYSU_OK; }
             if (f == "learn_kind") { *value = e->learn_kind; return SYSU_OK; }

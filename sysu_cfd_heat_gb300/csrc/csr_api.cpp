@@ -9,6 +9,7 @@
 
 #include "../../include/sysu_cfd.h"
 #include "csr_device.hpp"
+#include "gnn.hpp"
 #include "handles.hpp"
 
 
@@ -33,19 +34,24 @@ struct ArgError {
 };
 
 void check_method(int method, int precond) {
-    if (method < 0 || method > 4) throw ArgError{"method: 0 CG, 1 BiCGSTAB, 2 CG-mixed, 3 GMRES, 4 BiCGSTAB-mixed"};
-    if (precond < 0 || precond > 3) throw ArgError{"precond: 0 none, 1 Jacobi, 2 SSOR, 3 ILU(0)"};
+    if (method < 0 || method > 5)
+        throw ArgError{"method: 0 CG, 1 BiCGSTAB, 2 CG-mixed, 3 GMRES, 4 BiCGSTAB-mixed, 5 CG-multigrid"};
+    if (precond < 0 || precond > 4) throw ArgError{"precond: 0 none, 1 Jacobi, 2 SSOR, 3 ILU(0), 4 multigrid"};
     if ((method == 1 || method == 4) && precond > 1)
         throw ArgError{"BiCGSTAB runs with no or the Jacobi preconditioner"};
     if (method == 2 && precond != 1) throw ArgError{"the mixed-precision CG uses the Jacobi preconditioner"};
+    if (method == 5 && precond != 4) throw ArgError{"the multigrid CG takes precond 4 (multigrid)"};
+    if (method != 5 && precond == 4) throw ArgError{"precond 4 (multigrid) goes with method 5"};
 }
 }  // namespace
 
 extern "C" {
 
 // method: 0 CG, 1 BiCGSTAB, 2 CG with FP32 recurrences (Jacobi), 3 GMRES(10),
-// 4 BiCGSTAB with FP32 inner iterations in FP64 defect correction;
-// precond: 0 none, 1 Jacobi (omega D^-1), 2 SSOR(omega), 3 ILU(0).
+// 4 BiCGSTAB with FP32 inner iterations in FP64 defect correction, 5 flexible
+// CG with FP32 recurrences and FP64 reliable updates preconditioned by the
+// aggregation-multigrid cycle (precond 4; omega = the smoother's Jacobi weight);
+// precond: 0 none, 1 Jacobi (omega D^-1), 2 SSOR(omega), 3 ILU(0), 4 multigrid.
 // x holds x0 on entry and the solution on return.  Returns 0, SYSU_ERR_INPUT
 // for an argument error (checked before any device work), or SYSU_ERR_CUDA.
 int sysu_csr_solve(int method, int precond, int n, const int *rowptr, const int *col, const double *val,
@@ -83,8 +89,29 @@ int sysu_csr_solve(int method, int precond, int n, const int *rowptr, const int 
                 const double *bb[1] = {db.get()};
                 double *xx[1] = {dx.get()};
                 sysu::bicgstab_solve(M.A, M.val.get(), 1, bb, xx, o, w, info.get(), st);
-            } else {  // method 4 (check_method admits nothing else)
+            } else if (method == 4) {
                 sysu::bicgstab_solve_mixed(M.A, M.val.get(), db.get(), dx.get(), o, w, info.get(), st);
+            } else {  // method 5 (check_method admits nothing else)
+                sysu::DevBuf<float> v32(M.A.nnz);
+                sysu::sell_to_fp32(M.A, M.val.get(), v32.get(), st);
+                sysu::AggMultigrid mg;
+                mg.omega = omega;
+                mg.setup(M.A, M.pat, M.val.get(), 0.25, st);
+                mg.refresh(M.val.get(), v32.get(), st);
+                sysu::GnnPrecond fcg;
+                fcg.bind(M.A, M.val.get(), v32.get(), st);
+                fcg.attach_multigrid(&mg);
+                o.inner_tol = 0.1;
+                fcg.fcg(db.get(), dx.get(), false, o, false, info.get(), st);
+                if (mg.err_flag(st)) throw sysu::CaseError{"multigrid: the coarsest level is singular"};
+                sysu::SolveInfo h;
+                info.download(&h, 1, st);
+                dx.download(x, n, st);
+                SYSU_CUDA(cudaStreamSynchronize(st));
+                if (iters) *iters = h.iters[0];
+                if (res) *res = h.res[0];
+                if (status) *status = h.err ? sysu::DEV_BARRIER_TIMEOUT : h.status[0];
+                return SYSU_OK;
             }
             sysu::SolveInfo h;
             info.download(&h, 1, st);

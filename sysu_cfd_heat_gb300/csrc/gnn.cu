@@ -101,6 +101,7 @@ struct NetArgs {
     uint32_t *mask;
     float *aw;
     float *z;
+    const float *zbase;  // multigrid form: z = zbase + network output
     const float *qprev;
     FcgState *fs;
     double *part;
@@ -284,6 +285,7 @@ __global__ void __launch_bounds__(GT) k_gnn_fwd(NetArgs a) {
                 for (int c = 0; c < 32; c += 2) acc += sprm[96 + c] * bf_lo(ho[c >> 1]) + sprm[97 + c] * bf_hi(ho[c >> 1]);
                 float u = di * a.r[row] * inv_s;
                 float zi = s * (u + acc);
+                if (a.zbase) zi += a.zbase[row];
                 a.z[row] = zi;
                 if (a.qprev) zq += (double)zi * (double)a.qprev[row];
             }
@@ -718,6 +720,11 @@ __global__ void k_to_f32(int n, const double *a, float *b) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) b[i] = (float)a[i];
 }
+__global__ void k_post_jacobi(int n, const float *z2, const float *w, const float *t, float *z) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) z[i] = z2[i] + w[i] * t[i];
+}
+
 __global__ void k_to_f64(int n, const float *a, double *b) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) b[i] = (double)a[i];
@@ -796,6 +803,35 @@ __global__ void k_fcg_jacobi(FcgArgs a) {
     const bool rs = a.fs->restart;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.g.n; i += gridDim.x * blockDim.x) {
         float zi = a.g.dinv[i] * a.r[i];
+        a.z[i] = zi;
+        if (!rs) v[0] += (double)zi * a.q[i];
+    }
+    if (grid_sums<1>(v, a.part, &a.fs->cnt[0])) a.fs->zq = v[0];
+}
+
+// multigrid form with the network: scale s2 = rms(D^-1 t) of the post-smoother's input
+__global__ void k_fcg_tscale(FcgArgs a, const float *t) {
+    if (a.fs->done || !a.fs->use_gnn) return;
+    double v[1] = {0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.g.n; i += gridDim.x * blockDim.x) {
+        double u = (double)a.g.dinv[i] * t[i];
+        v[0] += u * u;
+    }
+    if (grid_sums<1>(v, a.part, &a.fs->cnt[3])) {
+        double s = sqrt(v[0] / (double)a.g.n);
+        a.fs->s2 = (float)s;
+        a.fs->inv_s2 = s > 0.0 ? (float)(1.0 / s) : 0.f;
+    }
+}
+
+// multigrid form, Jacobi post-smoothing (also the fallback when the network is
+// off): z = z2 + w t, and z.q_prev for the flexible beta
+__global__ void k_fcg_mgpost(FcgArgs a, const float *z2, const float *t, const float *w) {
+    if (a.fs->done || a.fs->use_gnn) return;
+    double v[1] = {0.0};
+    const bool rs = a.fs->restart;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.g.n; i += gridDim.x * blockDim.x) {
+        float zi = z2[i] + w[i] * t[i];
         a.z[i] = zi;
         if (!rs) v[0] += (double)zi * a.q[i];
     }
@@ -939,11 +975,32 @@ int blocks_flat(int n) { return std::max(1, std::min((n + FB - 1) / FB, num_sms(
 
 }  // namespace
 
-void GnnPrecond::bind(const SellDev &A, const double *val64, const float *val32, cudaStream_t st) {
+void GnnPrecond::drop_graphs() {
     for (ChunkGraph &g : graphs_) {
         if (g.exec) cudaGraphExecDestroy(g.exec);
         g = ChunkGraph{};
     }
+}
+
+void GnnPrecond::attach_multigrid(AggMultigrid *mg) {
+    if (mg && (!mg->ready() || !bound() || mg->level_rows(0) != n_))
+        throw CaseError{"multigrid: hierarchy not built for the bound matrix"};
+    drop_graphs();
+    mg_ = mg;
+    if (mg_ && z2_.size() < (size_t)n_) {
+        z2_.alloc(n_);
+        t_.alloc(n_);
+    }
+}
+
+void GnnPrecond::transform_pair(int k, cudaStream_t st) {
+    if (!mg_) return;
+    mg_->smoother_pair(pr_.get() + (size_t)k * n_, pe_.get() + (size_t)k * n_, st);
+}
+
+void GnnPrecond::bind(const SellDev &A, const double *val64, const float *val32, cudaStream_t st) {
+    drop_graphs();
+    mg_ = nullptr;
     A_ = &A;
     val64_ = val64;
     val32_ = val32;
@@ -1062,12 +1119,14 @@ void GnnPrecond::scale_of(const float *r32, cudaStream_t st) {
     SYSU_CUDA(cudaGetLastError());
 }
 
-void GnnPrecond::forward(const float *r32, float *z32, bool train, FcgState *fs, const float *qprev, cudaStream_t st) {
+void GnnPrecond::forward(const float *r32, float *z32, bool train, FcgState *fs, const float *qprev, cudaStream_t st,
+                         const float *zbase) {
     NetArgs a{};
     a.g = gview(*A_, val32_, dinv_.get());
     a.r = r32;
-    a.inv_s_p = fs ? &fs->inv_s : &sc_.get()->inv_s;
-    a.s_p = fs ? &fs->s : &sc_.get()->s;
+    a.inv_s_p = fs ? (zbase ? &fs->inv_s2 : &fs->inv_s) : &sc_.get()->inv_s;
+    a.s_p = fs ? (zbase ? &fs->s2 : &fs->s) : &sc_.get()->s;
+    a.zbase = zbase;
     a.prm = p_.get();
     a.aw = aw_.get();
     a.z = z32;
@@ -1156,6 +1215,25 @@ void GnnPrecond::apply(const double *r, double *z, cudaStream_t st) {
     check_err(st);
 }
 
+void GnnPrecond::apply_mg(const double *r, double *z, bool use_gnn, cudaStream_t st) {
+    if (!bound() || !mg_) throw CaseError{"multigrid form: no matrix bound or no hierarchy attached"};
+    int nb = (n_ + FB - 1) / FB;
+    k_to_f32<<<nb, FB, 0, st>>>(n_, r, r32_.get());
+    ++g_launches;
+    mg_->apply_fixed(r32_.get(), z2_.get(), t_.get(), nullptr, st);
+    if (use_gnn) {
+        scale_of(t_.get(), st);
+        forward(t_.get(), z32_.get(), false, nullptr, nullptr, st, z2_.get());
+    } else {
+        k_post_jacobi<<<nb, FB, 0, st>>>(n_, z2_.get(), mg_->w0(), t_.get(), z32_.get());
+        ++g_launches;
+    }
+    k_to_f64<<<nb, FB, 0, st>>>(n_, z32_.get(), z);
+    ++g_launches;
+    SYSU_CUDA(cudaGetLastError());
+    check_err(st);
+}
+
 double GnnPrecond::time_apply(const double *r, int reps, cudaStream_t st) {
     int nb = (n_ + FB - 1) / FB;
     k_to_f32<<<nb, FB, 0, st>>>(n_, r, r32_.get());
@@ -1195,6 +1273,7 @@ void GnnPrecond::add_pair(const double *r, const double *e, cudaStream_t st) {
     k_to_f32<<<nb, FB, 0, st>>>(n_, e, pe_.get() + off);
     g_launches += 2;
     SYSU_CUDA(cudaGetLastError());
+    transform_pair(next_, st);
     next_ = (next_ + 1) % capacity_;
     count_ = std::min(count_ + 1, capacity_);
 }
@@ -1206,6 +1285,7 @@ void GnnPrecond::add_pair_from(const double *b, const double *x1, const double *
                                                   pr_.get() + off, pe_.get() + off);
     ++g_launches;
     SYSU_CUDA(cudaGetLastError());
+    transform_pair(next_, st);
     next_ = (next_ + 1) % capacity_;
     count_ = std::min(count_ + 1, capacity_);
 }
@@ -1264,8 +1344,18 @@ void GnnPrecond::last_losses(std::vector<double> &out, int count, cudaStream_t s
 // update, conditional reliable update) enqueued on st.
 void GnnPrecond::fcg_iteration(const void *args, bool use_gnn, cudaStream_t st) {
     const FcgArgs &a = *static_cast<const FcgArgs *>(args);
-    if (use_gnn) forward(a.r, a.z, false, a.fs, a.q, st);
-    k_fcg_jacobi<<<gflat_, FB, 0, st>>>(a);
+    if (mg_) {
+        mg_->apply_fixed(a.r, z2_.get(), t_.get(), &a.fs->done, st);
+        if (use_gnn) {
+            k_fcg_tscale<<<gflat_, FB, 0, st>>>(a, t_.get());
+            ++g_launches;
+            forward(t_.get(), a.z, false, a.fs, a.q, st, z2_.get());
+        }
+        k_fcg_mgpost<<<gflat_, FB, 0, st>>>(a, z2_.get(), t_.get(), mg_->w0());
+    } else {
+        if (use_gnn) forward(a.r, a.z, false, a.fs, a.q, st);
+        k_fcg_jacobi<<<gflat_, FB, 0, st>>>(a);
+    }
     k_fcg_dir<<<gflat_, FB, 0, st>>>(a);
     k_fcg_upd<<<gflat_, FB, 0, st>>>(a);
     k_fcg_rel1<<<gflat_, FB, 0, st>>>(a);
@@ -1307,9 +1397,9 @@ void GnnPrecond::fcg(const double *b, double *x, bool x0_zero, const KrylovOpts 
     ++g_launches;
     SYSU_CUDA(cudaGetLastError());
     // (re)capture the chunk graph when its arguments changed
-    ChunkGraph &cg = graphs_[use_gnn ? 1 : 0];
+    ChunkGraph &cg = graphs_[(mg_ ? 2 : 0) + (use_gnn ? 1 : 0)];
     if (!cg.exec || cg.inner_tol != o.inner_tol || cg.stall_max != stall_max || cg.chunk != check_every ||
-        cg.val32 != val32_ || cg.dinv != dinv_.get()) {
+        cg.val32 != val32_ || cg.dinv != dinv_.get() || cg.mg != mg_) {
         if (cg.exec) cudaGraphExecDestroy(cg.exec);
         cg.exec = nullptr;
         long before = g_launches.load();
@@ -1326,6 +1416,7 @@ void GnnPrecond::fcg(const double *b, double *x, bool x0_zero, const KrylovOpts 
         cg.chunk = check_every;
         cg.val32 = val32_;
         cg.dinv = dinv_.get();
+        cg.mg = mg_;
     }
     int done = 0;
     for (int it = 0; it < o.maxit && !done; it += check_every) {
@@ -1341,10 +1432,7 @@ void GnnPrecond::fcg(const double *b, double *x, bool x0_zero, const KrylovOpts 
     check_err(st);
 }
 
-GnnPrecond::~GnnPrecond() {
-    for (ChunkGraph &g : graphs_)
-        if (g.exec) cudaGraphExecDestroy(g.exec);
-}
+GnnPrecond::~GnnPrecond() { drop_graphs(); }
 
 __global__ void k_bf16_to_f32(long n, const uint16_t *a, float *b) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;

@@ -23,6 +23,7 @@
 #include <cstdint>
 #include <vector>
 
+#include "amg.hpp"
 #include "krylov.hpp"
 
 namespace sysu {
@@ -44,6 +45,7 @@ struct FcgState {
     double res;
     int iters, refinements, done, status, use_gnn, stall, restart, need_update, fallback_at, maxit;
     float inv_s, s;
+    float inv_s2, s2;  // multigrid form: scale of the post-smoother's input
     unsigned cnt[4];
 };
 
@@ -100,10 +102,25 @@ class GnnPrecond {
     // (layer 1..4) as FP32 [n][32] to the host.
     void hidden(const double *r, int layer, float *host, cudaStream_t st);
 
+    // Multigrid form: with a hierarchy attached (built for the bound matrix and
+    // refreshed with its values by the caller), the preconditioner of fcg() is
+    // the aggregation-multigrid V-cycle, whose finest post-smoothing step is the
+    // network applied to the residual t = r - A z2 after pre-smoothing and
+    // coarse correction (use_gnn), or Jacobi.  Training pairs added while a
+    // hierarchy is attached are turned into pairs of that post-smoother,
+    // (r, e) -> (r - A z2(r), e - z2(r)).  nullptr detaches.
+    void attach_multigrid(AggMultigrid *mg);
+    AggMultigrid *multigrid() const { return mg_; }
+    // z = M(r) of the attached cycle once (FP64 device vectors): z2 + N(t) with
+    // the network (use_gnn), z2 + w t (Jacobi) without.
+    void apply_mg(const double *r, double *z, bool use_gnn, cudaStream_t st);
+
     // Flexible CG (Notay's FCG(1)) with FP32 recurrences and FP64 reliable
-    // updates, preconditioned by the network (use_gnn) or by Jacobi; when the
-    // network fails to reduce the residual for `stall_max` iterations, or a
-    // direction loses positivity, Jacobi takes over for the rest of the solve.
+    // updates, preconditioned by the network (use_gnn) or by Jacobi -- or by
+    // the multigrid cycle, with or without the network, when one is attached;
+    // when the network fails to reduce the residual for `stall_max` iterations,
+    // or a direction loses positivity, the same preconditioner without the
+    // network takes over for the rest of the solve.
     // Stops on the FP64 residual ||b - A x|| / ||b|| < eps.
     void fcg(const double *b, double *x, bool x0_zero, const KrylovOpts &o, bool use_gnn, SolveInfo *info_dev,
              cudaStream_t st);
@@ -112,7 +129,8 @@ class GnnPrecond {
     FcgState last_state(cudaStream_t st);
 
   private:
-    void forward(const float *r32, float *z32, bool train, FcgState *fs, const float *qprev, cudaStream_t st);
+    void forward(const float *r32, float *z32, bool train, FcgState *fs, const float *qprev, cudaStream_t st,
+                 const float *zbase = nullptr);
     void backward(const float *r32, cudaStream_t st);
     void refresh_bf16(cudaStream_t st);
     void scale_of(const float *r32, cudaStream_t st);
@@ -120,14 +138,21 @@ class GnnPrecond {
     void fcg_iteration(const void *args, bool use_gnn, cudaStream_t st);
 
     // a captured chunk of check_every flexible-CG iterations
+    // (index: 2 * multigrid attached + network on)
     struct ChunkGraph {
         cudaGraphExec_t exec = nullptr;
         double inner_tol = 0.0;
         int stall_max = 0, chunk = 0;
         long launches = 0;
         const float *val32 = nullptr, *dinv = nullptr;
+        const AggMultigrid *mg = nullptr;
     };
-    ChunkGraph graphs_[2];
+    ChunkGraph graphs_[4];
+    void drop_graphs();
+    void transform_pair(int k, cudaStream_t st);
+
+    AggMultigrid *mg_ = nullptr;
+    DevBuf<float> z2_, t_;      // multigrid form: fixed part of the cycle and its residual
 
     const SellDev *A_ = nullptr;
     const double *val64_ = nullptr;

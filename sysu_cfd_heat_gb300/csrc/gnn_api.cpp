@@ -12,6 +12,7 @@ struct sysu_gnn {
     cudaStream_t st = nullptr;
     sysu::CsrDevice M;
     sysu::DevBuf<float> val32;
+    sysu::AggMultigrid mg;  // declared before net: net refers to it and goes first
     sysu::GnnPrecond net;
     sysu::DevBuf<double> v0, v1;
     sysu::DevBuf<sysu::SolveInfo> info;
@@ -77,6 +78,7 @@ int sysu_gnn_set_values(sysu_gnn *g, const int *rowptr, const int *col, const do
         g->M.reload_values(g->net.n(), rowptr, col, val, g->st);
         sysu::sell_to_fp32(g->M.A, g->M.val.get(), g->val32.get(), g->st);
         g->net.refresh(g->st);
+        if (g->net.multigrid()) g->mg.refresh(g->M.val.get(), g->val32.get(), g->st);
     });
 }
 
@@ -205,6 +207,39 @@ int sysu_gnn_time_apply(sysu_gnn *g, const double *r, int reps, int fwd_per_sm, 
             g->net.bind(g->M.A, g->M.val.get(), g->val32.get(), g->st);
         }
         *ms = g->net.time_apply(g->v0.get(), reps, g->st);
+    });
+}
+
+int sysu_gnn_set_multigrid(sysu_gnn *g, int on, double theta, double omega, double gamma, int *levels, int *rows,
+                           int max_levels) {
+    if (!g || (on && (!(theta > 0.0 && theta < 1.0) || !(omega > 0.0 && omega < 2.0) || !(gamma > 0.0 && gamma <= 4.0)))) {
+        g_gnn_err = "sysu_gnn_set_multigrid: theta in (0, 1), omega in (0, 2), gamma in (0, 4]";
+        return SYSU_ERR_INPUT;
+    }
+    return guarded([&] {
+        g->net.attach_multigrid(nullptr);
+        if (!on) return;
+        g->mg.omega = omega;
+        g->mg.gamma = gamma;
+        g->mg.setup(g->M.A, g->M.pat, g->M.val.get(), theta, g->st);
+        g->mg.refresh(g->M.val.get(), g->val32.get(), g->st);
+        g->net.attach_multigrid(&g->mg);
+        if (g->mg.err_flag(g->st)) throw sysu::CaseError{"multigrid: the coarsest level is singular"};
+        if (levels) *levels = g->mg.levels();
+        if (rows)
+            for (int l = 0; l < g->mg.levels() && l < max_levels; ++l) rows[l] = g->mg.level_rows(l);
+        SYSU_CUDA(cudaStreamSynchronize(g->st));
+    });
+}
+
+int sysu_gnn_mg_apply(sysu_gnn *g, const double *r, double *z, int use_gnn) {
+    if (!g || !r || !z) return SYSU_ERR_INPUT;
+    return guarded([&] {
+        int n = g->net.n();
+        g->v0.upload(r, n, g->st);
+        g->net.apply_mg(g->v0.get(), g->v1.get(), use_gnn != 0, g->st);
+        g->v1.download(z, n, g->st);
+        SYSU_CUDA(cudaStreamSynchronize(g->st));
     });
 }
 

@@ -97,8 +97,10 @@ struct KrylovOpts {
 };
 
 // Preconditioners of the general solvers (LASPack's JacobiPrecond, SSORPrecond,
-// ILUPrecond; none = identity).
-enum PrecondKind { PK_NONE = 0, PK_JACOBI = 1, PK_SSOR = 2, PK_ILU0 = 3 };
+// ILUPrecond; none = identity).  PK_AMG (the symmetric p' systems only):
+// flexible CG with FP32 recurrences and FP64 reliable updates, preconditioned
+// by the aggregation-multigrid V-cycle of amg.hpp.
+enum PrecondKind { PK_NONE = 0, PK_JACOBI = 1, PK_SSOR = 2, PK_ILU0 = 3, PK_AMG = 4 };
 constexpr int GMRES_MAX_RESTART = 30;
 
 // Restarted GMRES(m), right preconditioned (the oracle's LASPack restatement:

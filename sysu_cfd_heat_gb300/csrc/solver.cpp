@@ -416,7 +416,7 @@ void SimpleSolver::solve(int slot, const EqOpts &o, const SellDev &A, const doub
                         nrhs == 1 ? info : infos.get() + SLOT_N + c, st);
         return;
     }
-    if (o.kind == SK_CG && o.learned && &A == &fd.A) {
+    if (o.kind == SK_CG && (o.learned || o.precond == PK_AMG) && &A == &fd.A) {
         if (nrhs != 1) throw CaseError{"CG solves one right-hand side"};
         solve_learned(o, val, b[0], x[0], x0_zero, info);
         return;
@@ -454,13 +454,19 @@ void SimpleSolver::solve(int slot, const EqOpts &o, const SellDev &A, const doub
     bicgstab_solve(A, val, nrhs, b, x, ko, kw, info, st);
 }
 
-// p' solve of the learned form.  Training window: a loose plain solve (1e-2)
-// from zero, then the solve to eps from there; the pairs (b, x*) and
-// (b - A x1, x* - x1) go into the network's ring and learn_steps Adam steps
-// follow.  After the window: flexible CG with the network.
+// p' solve of the learned and multigrid forms.  With precond PK_AMG the
+// flexible CG is preconditioned by the aggregation-multigrid cycle (hierarchy
+// built at the first solve, values refreshed at every solve); with learned set,
+// the network is that cycle's finest post-smoother (without PK_AMG: the whole
+// preconditioner).  Training window of the learned form: a loose plain solve
+// (1e-2) from zero, then the solve to eps from there; the pairs (b, x*) and
+// (b - A x1, x* - x1) go into the network's ring (as post-smoother pairs in the
+// multigrid form) and learn_steps Adam steps follow.  After the window: flexible
+// CG with the network.
 void SimpleSolver::solve_learned(const EqOpts &o, const double *val, const double *b, double *x, bool x0_zero,
                                  SolveInfo *info) {
     const SellDev &A = fd.A;
+    const bool use_mg = o.precond == PK_AMG;
     if (f.Ap32.size() < (size_t)A.nnz) f.Ap32.alloc(A.nnz);
     sell_to_fp32(A, val, f.Ap32.get(), st);
     if (!gnn.bound()) {
@@ -471,12 +477,29 @@ void SimpleSolver::solve_learned(const EqOpts &o, const double *val, const doubl
     } else {
         gnn.refresh(st);
     }
+    if (use_mg) {
+        if (!mg.ready() || mg_theta_built != o.mg_theta) {
+            gnn.attach_multigrid(nullptr);
+            mg.setup(A, fd.pat, val, o.mg_theta, st);
+            mg_theta_built = o.mg_theta;
+        }
+        mg.omega = o.mg_omega;
+        mg.gamma = o.mg_gamma;
+        mg.refresh(val, f.Ap32.get(), st);
+        if (gnn.multigrid() != &mg) gnn.attach_multigrid(&mg);
+    } else if (gnn.multigrid()) {
+        gnn.attach_multigrid(nullptr);
+    }
     KrylovOpts ko;
     ko.maxit = o.maxit;
     ko.eps = o.eps;
     ko.omega = o.omega;
     ko.jacobi = true;
     ko.inner_tol = o.inner_tol;
+    if (!o.learned) {
+        gnn.fcg(b, x, x0_zero, ko, false, info, st);
+        return;
+    }
     if (p_solves++ >= o.learn_iters) {
         gnn.fcg(b, x, x0_zero, ko, true, info, st);
         return;
@@ -484,7 +507,8 @@ void SimpleSolver::solve_learned(const EqOpts &o, const double *val, const doubl
     auto plain = [&](double eps, bool zero) {
         KrylovOpts k = ko;
         k.eps = eps;
-        if (o.mixed) cg_solve_mixed(A, val, f.Ap32.get(), b, x, zero, k, kw, info, st);
+        if (use_mg) gnn.fcg(b, x, zero, k, false, info, st);
+        else if (o.mixed) cg_solve_mixed(A, val, f.Ap32.get(), b, x, zero, k, kw, info, st);
         else cg_solve(A, val, b, x, zero, k, kw, info, st);
     };
     if (gnn_x1.size() < (size_t)A.n) gnn_x1.alloc(A.n);

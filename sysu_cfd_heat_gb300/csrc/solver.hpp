@@ -53,6 +53,11 @@ struct EqOpts {
     int learn_steps = 64;
     double learn_lr = 1e-3;
     int learn_kind = 1;       // loss: 0 energy norm of the error, 1 residual norm
+    // precond PK_AMG: strength threshold of the aggregation, Jacobi weight of the
+    // smoother, scale of the prolonged coarse correction
+    double mg_theta = 0.25;
+    double mg_omega = 0.8;
+    double mg_gamma = 1.8;
 };
 
 struct SolverOptions {
@@ -135,7 +140,9 @@ class SimpleSolver {
     DomainDev fd, sd;
     FieldSet f, s;
     KrylovWork kw;
-    GnnPrecond gnn;             // learned p' preconditioner (option p.learned)
+    GnnPrecond gnn;             // learned p' preconditioner (option p.learned); flexible CG driver
+    AggMultigrid mg;            // p' multigrid hierarchy (option p.precond 4)
+    double mg_theta_built = 0.0;
     int p_solves = 0;           // p' solves so far (training window of the learned form)
     DevBuf<double> gnn_x1;      // partial solution of a training solve
     DevBuf<double> io_stage;    // staging for reordered field transfers

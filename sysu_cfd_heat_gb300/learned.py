@@ -88,6 +88,24 @@ class LearnedPreconditioner:
         self._check(_lib.lib().sysu_gnn_apply(self.h, _dp(r), _dp(z)))
         return z
 
+    def set_multigrid(self, on: bool = True, theta: float = 0.25, omega: float = 0.8, gamma: float = 1.8):
+        """Attach (or detach) the aggregation-multigrid cycle: fcg() is then
+        preconditioned by the V-cycle whose finest post-smoother is the network
+        (use_gnn) or Jacobi, and add_pair() stores post-smoother pairs.  Returns
+        the rows of each level."""
+        lev = C.c_int()
+        rows = (C.c_int * 16)()
+        self._check(_lib.lib().sysu_gnn_set_multigrid(self.h, 1 if on else 0, theta, omega, gamma, C.byref(lev),
+                                                      rows, 16))
+        return [rows[i] for i in range(lev.value)] if on else []
+
+    def mg_apply(self, r, use_gnn: bool = False) -> np.ndarray:
+        """One application of the attached cycle, z = M(r)."""
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        z = np.zeros(self.n)
+        self._check(_lib.lib().sysu_gnn_mg_apply(self.h, _dp(r), _dp(z), 1 if use_gnn else 0))
+        return z
+
     def hidden(self, r, layer: int) -> np.ndarray:
         r = np.ascontiguousarray(r, dtype=np.float64)
         h = np.zeros((self.n, WIDTH), np.float32)

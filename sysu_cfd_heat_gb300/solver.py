@@ -234,8 +234,10 @@ def csr_solve(rowptr, col, val, b, x0=None, method: str = "CG", precond: str = "
     n = len(rowptr) - 1
     x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64)
     it, rs, stt = C.c_int(), C.c_double(), C.c_int()
-    code = fn({"CG": 0, "BiCGSTAB": 1, "CG-mixed": 2, "GMRES": 3, "BiCGSTAB-mixed": 4}[method],
-              {"none": 0, "Jacobi": 1, "SSOR": 2, "ILU": 3}[precond], n,
+    if method == "CG-multigrid":
+        precond = "multigrid"
+    code = fn({"CG": 0, "BiCGSTAB": 1, "CG-mixed": 2, "GMRES": 3, "BiCGSTAB-mixed": 4, "CG-multigrid": 5}[method],
+              {"none": 0, "Jacobi": 1, "SSOR": 2, "ILU": 3, "multigrid": 4}[precond], n,
               rowptr.ctypes.data_as(ip), col.ctypes.data_as(ip), _dptr(val), _dptr(b), _dptr(x), maxit, eps, omega,
               C.byref(it), C.byref(rs), C.byref(stt))
     if code != 0:
