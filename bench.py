@@ -15,9 +15,10 @@ are the same iterations the CPU sample times.  ``e2e`` runs the same iterations
 through the C ABI with host buffers: every step uploads U, V, W, P and the face
 fluxes from host memory and reads U, V, W, P back.
 
-``--impl reference`` times the reference's own CPU code (oracle/_ref/cycas_ref: the
-reference's src/*.cpp + the LASPack restatement) on the same case, single-threaded as
-the reference is, for as many outer iterations as fit in a time budget.
+``--impl reference`` times the reference's own CPU code (oracle/_ref/cycas_ref_o3: the
+reference's src/*.cpp + the LASPack restatement at -O3 -march=native) on the same case,
+single-threaded as the reference is and pinned to one core, for the same --steps outer
+iterations (stopping early only past --ref-budget seconds).
 
 With torchrun (N > 1) every rank runs an independent replica on its own GPU
 (the path has no data-parallel exchange); value = total iterations / max time.
@@ -52,6 +53,7 @@ FP64_PEAK_TFLOPS = 1.25
 LEARN_ITERS = 10   # outer iterations that train the learned preconditioner
 LEARN_STEPS = 64   # Adam steps per training outer iteration
 LEARN_C5_ITERS = 40  # training outer iterations of the --learned-c5 run
+LEARN_C5_MG = 10     # training outer iterations of its learned multigrid form
 
 
 def rank_info():
@@ -143,18 +145,56 @@ def cg_flops_per_iter(n: int, nnz_true: int) -> float:
     return 2.0 * nnz_true + 13.0 * n
 
 
-def cpu_reference_run(param: str, iters: int, budget_s: float, timeout_s: float):
-    """Run the reference binary on the case; returns (per-iteration seconds, setup s, info)."""
-    exe = os.path.join(ROOT, "oracle", "_ref", "cycas_ref")
+def host_cpu() -> dict:
+    """Host cores and CPU model of this machine (the CPU baseline's record)."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if model is None and os.path.exists("/proc/cpuinfo"):
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                model = line.split(":", 1)[1].strip()
+                break
+    return {"nproc": os.cpu_count(), "cpu_model": model or "unknown"}
+
+
+def cpu_reference_run(param: str, iters: int, budget_s: float, timeout_s: float, build: str = "o3",
+                      env_extra: dict | None = None):
+    """Run the reference binary on the case, single-threaded and pinned to one core
+    (the last core this process may use); stops after `iters` outer iterations or
+    once they add up to more than budget_s.  build: "o3" (-O3 -march=native, the
+    primary CPU baseline), "o2" (the parity build) or "g" (the reference's shipped
+    flags, -g without optimisation).  Returns (per-iteration seconds, setup s,
+    error or None, record)."""
+    exe = os.path.join(ROOT, "oracle", "_ref", {"o3": "cycas_ref_o3", "o2": "cycas_ref", "g": "cycas_ref_g"}[build])
     if not os.path.exists(exe):
-        return None, None, "oracle/_ref/cycas_ref not built (no reference sources on this machine)"
+        return None, None, f"oracle/_ref/{os.path.basename(exe)} not built (no reference sources on this machine)", {}
     d = os.path.dirname(param)
     env = dict(os.environ, SYSU_ORACLE_GMRES_AS="BiCGSTAB", SYSU_ORACLE_SSOR_AS="Jacobi", SYSU_ORACLE_RTC=str(RTC))
+    env.update(env_extra or {})
+    try:
+        core = max(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        core = None
+    rec = dict(host_cpu(), binary="oracle/_ref/" + os.path.basename(exe), pinned_core=core,
+               flags={"o3": "-O3 -march=native", "o2": "-O2", "g": "-g (the reference makefile's flags)"}[build])
+
+    def pin():
+        if core is not None:
+            os.sched_setaffinity(0, {core})
+
     with tempfile.TemporaryDirectory() as tmp:
         tfile = os.path.join(tmp, "timing.txt")
         cmd = [exe, "-paramfile", os.path.basename(param), "-iters", str(iters), "-quiet", "-timing", tfile]
         t0 = time.time()
-        p = subprocess.Popen(cmd, cwd=d, env=env, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        p = subprocess.Popen(cmd, cwd=d, env=env, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL,
+                             preexec_fn=pin)
         setup, its = None, []
         while p.poll() is None:
             time.sleep(0.5)
@@ -165,7 +205,15 @@ def cpu_reference_run(param: str, iters: int, budget_s: float, timeout_s: float)
                 p.wait()
                 break
         setup, its = _read_timing(tfile)
-        return its, setup, None
+        return its, setup, None, rec
+
+
+def cpu_rate(its):
+    """(iterations/s, description): the mean over outer iterations 2.. when more
+    than one finished, else iteration 1."""
+    if len(its) >= 2:
+        return (len(its) - 1) / sum(its[1:]), f"mean over outer iterations 2..{len(its)}"
+    return 1.0 / its[0], "outer iteration 1"
 
 
 def _read_timing(path):
@@ -188,7 +236,7 @@ def run_reference(args, r, w):
         return
     param = case_dir(args.workload)
     nx, ny, nz = WORKLOADS[args.workload]
-    its, setup, err = cpu_reference_run(param, max(1, args.steps), args.ref_budget, args.ref_budget + 600)
+    its, setup, err, rec = cpu_reference_run(param, max(1, args.steps), args.ref_budget, args.ref_budget + 600)
     base = {"impl": "reference", "metric": METRIC, "unit": "iters/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": config_of(args)}
@@ -199,9 +247,10 @@ def run_reference(args, r, w):
     tot = sum(its)
     v = len(its) / tot
     sample = (f"outer iterations 1..{len(its)} of the {args.workload} case ({6 * nx * ny * nz} cells), "
-              f"set-up ({setup:.1f} s) excluded, bounded to ~{args.ref_budget:.0f} s of iterations")
+              f"set-up ({setup:.1f} s) excluded, {rec['flags']}, 1 thread pinned to core {rec['pinned_core']}")
     base.update({"value": v, "ms_per_step": 1000 * tot / len(its), "steps": len(its),
-                 "cpu_baseline": {"value": v, "unit": "iters/s", "cores": 1, "kind": "reference", "sample": sample},
+                 "cpu_baseline": {"value": v, "unit": "iters/s", "cores": 1, "kind": "reference", "sample": sample,
+                                  "host": rec},
                  "e2e": {"value": v, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
     print(json.dumps(base))
 
@@ -385,7 +434,10 @@ def c5_learned_run(args):
     up, fluid 320 x 80 x 160 hexes (4,096,000 cells) + solid 320 x 16 x 160 (819,200).
     The learned p' form trains during the first LEARN_C5_ITERS outer iterations, then the
     p' system of the next outer iteration is solved to 1e-8 by flexible CG with the
-    network and, from the same state, by plain FP64 Jacobi-CG and the mixed FP32 CG."""
+    network and, from the same state, by plain FP64 Jacobi-CG, the mixed FP32 CG, the
+    multigrid flexible CG and the multigrid flexible CG with the network as its
+    post-smoother (trained from that state for LEARN_C5_MG outer iterations); each
+    method's fields after that outer iteration against the FP64 CG's."""
     from sysu_cfd_heat_gb300 import meshgen as mg
     from sysu_cfd_heat_gb300.solver import NavierStokesSolver
 
@@ -409,9 +461,25 @@ def c5_learned_run(args):
         s.sync()
         out["training_s"] = time.perf_counter() - t0
         state = {f: s.get(f) for f in ("U", "V", "W", "P", "RUFace", "TE", "ED", "VisTur", "T", "solid_T")}
-        res = {}
-        for name, opts in (("learned_fcg", {"p.learned": 1}), ("fp64_cg", {"p.learned": 0, "p.mixed": 0}),
-                           ("mixed_cg", {"p.learned": 0, "p.mixed": 1})):
+        res, fields = {}, {}
+        forms = (("fp64_cg", {"p.learned": 0, "p.mixed": 0, "p.precond": 1}),
+                 ("mixed_cg", {"p.learned": 0, "p.mixed": 1, "p.precond": 1}),
+                 ("multigrid_fcg", {"p.learned": 0, "p.mixed": 0, "p.precond": 4}),
+                 ("learned_fcg", {"p.learned": 1, "p.mixed": 0, "p.precond": 1}),
+                 ("learned_multigrid_fcg", {"p.learned": 1, "p.mixed": 0, "p.precond": 4}))
+        for name, opts in forms:
+            if name == "learned_multigrid_fcg":
+                # train the post-smoother from the same state: LEARN_C5_MG outer iterations
+                for k, v in opts.items():
+                    s.set_option(k, v)
+                s.set_option("p.learn_reset", 1)
+                s.set_option("p.learn_iters", LEARN_C5_MG)
+                for f, a in state.items():
+                    s.set(f, a)
+                t0 = time.perf_counter()
+                s.iterate(LEARN_C5_MG)
+                s.sync()
+                out["training_multigrid_s"] = time.perf_counter() - t0
             for f, a in state.items():
                 s.set(f, a)
             for k, v in opts.items():
@@ -422,66 +490,150 @@ def c5_learned_run(args):
             st = s.solve_stats()["p"]
             res[name] = {"ms": s.timing()[0], "iters": st["iters"][0], "rel_residual": st["res"][0],
                          "converged": st["status"][0] == 0}
+            fields[name] = {f: s.get(f) for f in ("U", "V", "W", "P")}
+        for name in res:
+            res[name]["field_rel_l2_vs_fp64_cg"] = max(
+                float(np.linalg.norm(fields[name][f] - fields["fp64_cg"][f]) /
+                      max(np.linalg.norm(fields["fp64_cg"][f]), 1e-300)) for f in fields[name])
         out["p_solve_to_1e-8_after_training"] = res
         out["training_outer_iterations"] = LEARN_C5_ITERS
     return out
 
 
-def learned_form(s, args, to8, field_err):
-    """The learned + FP32 form: p' by flexible CG preconditioned by the message-passing
-    network (FP32 recurrences, FP64 reliable updates, Jacobi fallback).  The network
-    is trained on the GPU during the first LEARN_ITERS outer iterations (plain p'
-    solves generating the residual/correction pairs); then the fields are reset
-    (the trained network is kept) and the same timed iterations run with it."""
-    s.set_option("p.learned", 1)
-    s.set_option("p.learn_iters", LEARN_ITERS)
-    s.set_option("p.learn_steps", LEARN_STEPS)
+# The forms of the p' solve timed side by side at a matched residual: every form
+# starts from the same initial state and runs the same outer iterations with p'
+# solved to the 1e-8 relative residual (no iteration cap).
+P_FORMS = (
+    ("fp64", {}, "Jacobi-CG, FP64 (the drop-in's method without the reference's 1000-iteration cap)"),
+    ("mixed_fp32_fp64", {"p.mixed": 1}, "Jacobi-CG, FP32 recurrences + FP64 reliable updates"),
+    ("multigrid_fp32_fp64", {"p.precond": 4},
+     "flexible CG, FP32 recurrences + FP64 reliable updates, aggregation-multigrid V-cycle"),
+    ("learned_multigrid_fp32_fp64", {"p.precond": 4, "p.learned": 1},
+     "as multigrid_fp32_fp64 with the trained message-passing network as the finest post-smoother"),
+    ("learned_network_fp32_fp64", {"p.learned": 1},
+     "flexible CG, FP32 recurrences + FP64 reliable updates, the trained network as the whole preconditioner"),
+)
+P_OPTION_DEFAULTS = {"p.mixed": 0, "p.learned": 0, "p.precond": 1}
+
+
+def matched_forms(s, args, n, nnz, hbm):
+    """Outer iterations/s of every p' form at a matched 1e-8 residual, the p' solve
+    time and iterations, and the fields' relative L2 difference from the FP64
+    form's after the same iterations.  The learned forms first train during
+    LEARN_ITERS outer iterations (plain solves generating the pairs, LEARN_STEPS
+    Adam steps each); the fields are then reset and the same iterations timed
+    with the trained network (training is not in the timed region)."""
     s.set_option("p.maxit", 100000)
-    s.reset()
-    t0 = time.perf_counter()
-    s.iterate(LEARN_ITERS)
-    s.sync()
-    train_s = time.perf_counter() - t0
-    # p' solve of outer iteration 1 to 1e-8 with the trained network
-    s.reset()
-    s.CalculateVelocity()
-    s.CalculatePressure()
-    s.check()
-    st = s.solve_stats()["p"]
-    first = {"ms": s.timing()[0], "iters": st["iters"][0], "rel_residual": st["res"][0],
-             "converged": st["status"][0] == 0}
+    out, ref = {}, None
+    for name, opts, what in P_FORMS:
+        for k, v in P_OPTION_DEFAULTS.items():
+            s.set_option(k, v)
+        for k, v in opts.items():
+            s.set_option(k, v)
+        entry = {"method": what}
+        if opts.get("p.learned"):
+            s.set_option("p.learn_reset", 1)
+            s.set_option("p.learn_iters", LEARN_ITERS)
+            s.set_option("p.learn_steps", LEARN_STEPS)
+            s.reset()
+            t0 = time.perf_counter()
+            s.iterate(LEARN_ITERS)
+            s.sync()
+            entry["training"] = {"outer_iterations": LEARN_ITERS, "adam_steps_per_iteration": LEARN_STEPS,
+                                 "seconds_incl_plain_solves": time.perf_counter() - t0,
+                                 "pairs": "(b, x*) and (b - A x1, x* - x1) per p' solve, x1 = solve to 1e-2"
+                                          + (", as post-smoother pairs (r - A z2, e - z2)" if opts.get("p.precond") else ""),
+                                 "loss": "residual norm ||A(z - e)||^2 / ||A e||^2"}
+        else:
+            s.reset()
+            s.iterate(1)  # warm-up: hierarchy set-up, graph capture
+        s.reset()
+        tot, pm, pit = 0.0, [], []
+        for k in range(args.steps):
+            s.timer_start()
+            s.iterate(1)
+            tot += s.timer_stop()
+            pm.append(s.timing()[0])
+            st = s.solve_stats()["p"]
+            pit.append(st["iters"][0])
+            if st["status"][0] != 0:
+                entry["p_status_not_converged"] = st["status"][0]
+        fields = {f: s.get(f) for f in ("U", "V", "W", "P")}
+        if ref is None:
+            ref = fields
+        entry.update({"iters_per_s": args.steps / (tot / 1000.0), "ms_per_step": tot / args.steps,
+                      "p_solve_ms_mean": statistics.mean(pm), "p_iters_mean": statistics.mean(pit),
+                      "field_rel_l2_vs_fp64": max(float(np.linalg.norm(fields[f] - ref[f]) /
+                                                        max(np.linalg.norm(ref[f]), 1e-300)) for f in fields)})
+        if name == "mixed_fp32_fp64":
+            b32 = cg_bytes_per_iter(n, nnz, fp32=True)
+            init32 = nnz * 12 + 40 * n
+            ach32 = statistics.mean([(it * b32 + init32) / (ms / 1000.0) / 1e9 for it, ms in zip(pit, pm) if ms > 0])
+            entry["roofline"] = {"bound": "hbm", "kernel": "k_cg_mixed_pipe", "achieved": ach32, "peak": hbm,
+                                 "unit": "GB/s", "frac": ach32 / hbm, "algorithmic_bytes_per_cg_iteration": b32}
+        out[name] = entry
+    for k, v in P_OPTION_DEFAULTS.items():
+        s.set_option(k, v)
     s.set_option("p.maxit", 1000)
-    s.reset()
-    l_ms, l_p, l_it = 0.0, [], []
-    for k in range(args.steps):
-        s.timer_start()
-        s.iterate(1)
-        l_ms += s.timer_stop()
-        l_p.append(s.timing()[0])
-        l_it.append(s.solve_stats()["p"]["iters"][0])
-    fl = {f: s.get(f) for f in ("U", "V", "W", "P")}
-    # error against the plain FP64 form with every p' solve taken to 1e-8 as well
-    # (the timed FP64 loop stops p' at the reference's 1000-iteration cap)
-    s.set_option("p.learned", 0)
-    s.set_option("p.maxit", 100000)
-    s.reset()
-    s.iterate(args.steps)
-    err = max(float(np.linalg.norm(a - s.get(f)) / max(np.linalg.norm(s.get(f)), 1e-300)) for f, a in fl.items())
-    s.set_option("p.maxit", 1000)
-    out = {"iters_per_s": args.steps / (l_ms / 1000.0), "ms_per_step": l_ms / args.steps,
-           "field_rel_l2_vs_fp64_uncapped": err, "field_rel_l2_vs_fp64_timed_form": field_err(),
-           "p_solve_ms_mean": statistics.mean(l_p),
-           "p_fcg_iters_mean": statistics.mean(l_it),
-           "p_solve_to_1e-8_outer_iteration_1": first,
-           "p_solve_speedup_vs_fp64_to_1e-8": (to8["fp64"]["ms"] / first["ms"]) if first["ms"] > 0 else None,
-           "cg_iteration_reduction_vs_fp64": (to8["fp64"]["iters"] / first["iters"]) if first["iters"] else None,
-           "training": {"outer_iterations": LEARN_ITERS, "adam_steps_per_iteration": LEARN_STEPS,
-                        "seconds_incl_plain_solves": train_s,
-                        "pairs": "(b, x*) and (b - A x1, x* - x1) per p' solve, x1 = solve to 1e-2",
-                        "loss": "residual norm ||A(z - e)||^2 / ||A e||^2"},
-           "network": "4 message-passing layers, width 32, BF16 weights/activations, FP32 accumulation "
-                      "(tcgen05 MMA, 128-row tiles)"}
-    s.set_option("p.learned", 0)
+    base = out["fp64"]["iters_per_s"]
+    for name in out:
+        out[name]["speedup_vs_fp64"] = out[name]["iters_per_s"] / base
+    out["steps"] = args.steps
+    out["p_eps"] = RTC
+    out["target"] = ("learned + mixed-precision form at >= 3x the FP64 form's outer iterations/s, fields within "
+                     "1e-6 relative L2")
+    return out
+
+
+def cpu_survey(args) -> dict:
+    """--cpu-survey (not part of the default run; minutes of CPU time): the
+    reference's CPU build on configurations 1-3 next to the GPU path on the same
+    cases, 1 core pinned, the measurement SURVEY-style:
+    * C1, the 24^3 hex cavity at Re 100: all 300 outer iterations;
+    * C2, the k-epsilon CHT channel (256,000 + 51,200 cells) without the solid's
+      volumetric source, which the reference cannot express: mean over outer
+      iterations 2..20;
+    * C3, the 2M-cell tet cavity: mean over outer iterations 2..10 of the -O3
+      build, and outer iteration 1 of the reference's shipped -g build.
+    Every solve at the configurations' 1e-8 with BiCGSTAB + Jacobi for momentum
+    and scalars and Jacobi-CG for p' and the solid (both codes)."""
+    from sysu_cfd_heat_gb300 import meshgen as mg
+    from sysu_cfd_heat_gb300.solver import NavierStokesSolver
+
+    out = {"host": host_cpu()}
+
+    def gpu_rate(param, iters, skip_first):
+        with NavierStokesSolver(param, {"rtc": RTC}) as s:
+            s.iterate(1)
+            s.reset()
+            if skip_first:
+                s.iterate(1)
+            s.timer_start()
+            done = s.iterate(iters - (1 if skip_first else 0))
+            ms = s.timer_stop()
+        return done / (ms / 1000.0)
+
+    with tempfile.TemporaryDirectory() as tmp:
+        c1 = mg.write_case(os.path.join(tmp, "c1"), mg.lid_cavity_hex(24), mg.cavity_param("x", 300, mu=0.01))
+        its, setup, err, rec = cpu_reference_run(c1, 300, 1e9, 3600)
+        out["c1_cavity_24"] = {"cells": 13824, "cpu_iters_per_s": (len(its) / sum(its)) if its else None,
+                               "cpu_sample": f"all {len(its) if its else 0} outer iterations", "cpu": rec,
+                               "gpu_iters_per_s": gpu_rate(c1, 300, False), "error": err}
+        c2 = mg.write_case(os.path.join(tmp, "c2"), mg.cht_channel(160, 40, 8, 40),
+                           mg.cht_param("x", 20, nu=1e-5, k_solid=15.0))
+        its, setup, err, rec = cpu_reference_run(c2, 20, 1e9, 3600)
+        v, which = cpu_rate(its) if its else (None, "none")
+        out["c2_cht_channel"] = {"cells": {"fluid": 256000, "solid": 51200}, "cpu_iters_per_s": v,
+                                 "cpu_sample": which, "cpu": rec, "gpu_iters_per_s": gpu_rate(c2, 20, True),
+                                 "gpu_sample": "mean over outer iterations 2..20", "error": err}
+    c3 = case_dir("c3")
+    its, setup, err, rec = cpu_reference_run(c3, 10, 1e9, 3600)
+    v, which = cpu_rate(its) if its else (None, "none")
+    itg, setup_g, errg, recg = cpu_reference_run(c3, 1, 1e9, 3600, build="g")
+    out["c3_tet_cavity_2m"] = {"cells": 1996800, "cpu_iters_per_s": v, "cpu_sample": which, "cpu": rec,
+                               "cpu_iteration_seconds": its, "reference_setup_s": setup,
+                               "as_shipped_g_iters_per_s": (1.0 / itg[0]) if itg else None,
+                               "as_shipped_g": recg, "error": err or errg}
     return out
 
 
@@ -548,10 +700,6 @@ def run_ours(args, r, w, lr):
         mom_it.append(st["mom"]["iters"])
     launches = L.sysu_kernel_launches() - l0
     clocks = clk.stop()
-    fields64 = {f: s.get(f) for f in ("U", "V", "W", "P")}
-
-    def field_err():
-        return max(float(np.linalg.norm(s.get(f) - a) / max(np.linalg.norm(a), 1e-300)) for f, a in fields64.items())
     t_max = max_over_ranks(s_ms, w)
     if w > 1:
         dist.barrier()
@@ -601,46 +749,11 @@ def run_ours(args, r, w, lr):
         if per_iter:
             traffic = per_iter * statistics.mean(cg_it)
 
-    # the mixed-precision form (FP32 inner CG in FP64 defect correction) on the same iterations
     forms = {"fp64": {"iters_per_s": value, "ms_per_step": t_max / args.steps,
-                      "p_solve_ms_mean": statistics.mean(p_ms), "p_cg_iters_mean": statistics.mean(cg_it)}}
+                      "p_solve_ms_mean": statistics.mean(p_ms), "p_cg_iters_mean": statistics.mean(cg_it),
+                      "p_maxit": 1000}}
     if not args.p_maxit and not args.p_mixed:
-        s.set_option("p.mixed", 1)
-        s.reset()
-        m_ms, m_p, m_it = 0.0, [], []
-        for k in range(args.steps):
-            s.timer_start()
-            s.iterate(1)
-            m_ms += s.timer_stop()
-            m_p.append(s.timing()[0])
-            m_it.append(s.solve_stats()["p"]["iters"][0])
-        b32 = cg_bytes_per_iter(n, nnz, fp32=True)
-        init32 = nnz * 12 + 40 * n
-        ach32 = statistics.mean([(it * b32 + init32) / (ms / 1000.0) / 1e9 for it, ms in zip(m_it, m_p) if ms > 0])
-        forms["mixed_fp32_fp64"] = {"iters_per_s": args.steps / (m_ms / 1000.0), "ms_per_step": m_ms / args.steps,
-                                    "field_rel_l2_vs_fp64": field_err(),
-                                    "p_solve_ms_mean": statistics.mean(m_p),
-                                    "p_cg_inner_iters_mean": statistics.mean(m_it),
-                                    "roofline": {"bound": "hbm", "kernel": "k_cg_mixed_pipe", "achieved": ach32,
-                                                 "peak": hbm, "unit": "GB/s", "frac": ach32 / hbm,
-                                                 "algorithmic_bytes_per_cg_iteration": b32}}
-        s.set_option("p.mixed", 0)
-        # p' solve of outer iteration 1 to the 1e-8 relative residual, without the 1000 cap
-        to8 = {}
-        for name, mixed in (("fp64", 0), ("mixed_fp32_fp64", 1)):
-            s.set_option("p.mixed", mixed)
-            s.set_option("p.maxit", 100000)
-            s.reset()
-            s.CalculateVelocity()
-            s.CalculatePressure()
-            s.check()
-            st = s.solve_stats()["p"]
-            to8[name] = {"ms": s.timing()[0], "iters": st["iters"][0], "rel_residual": st["res"][0],
-                         "converged": st["status"][0] == 0}
-        s.set_option("p.mixed", 0)
-        s.set_option("p.maxit", 1000)
-        forms["p_solve_to_1e-8_outer_iteration_1"] = to8
-        forms["learned_fp32"] = learned_form(s, args, to8, field_err)
+        forms["matched_1e-8"] = matched_forms(s, args, n, nnz, hbm)
 
     # the reference's own solver mode (GMRES(10) + SSOR, CG + SSOR), outer iteration 1
     if not args.p_maxit and not args.p_mixed:
@@ -689,15 +802,17 @@ def run_ours(args, r, w, lr):
     }
     s.close()
     if r == 0 and w == 1 and not args.no_cpu_baseline:
-        its, setup, err = cpu_reference_run(param, 1, args.cpu_budget, args.cpu_budget + 600)
+        its, setup, err, rec = cpu_reference_run(param, 3, args.cpu_budget, args.cpu_budget + 600)
         if setup is not None:
             out["setup"]["reference_setup_s"] = setup
         if its:
             nx, ny, nz = WORKLOADS[args.workload]
-            out["cpu_baseline"] = {"value": 1.0 / its[0], "unit": "iters/s", "cores": 1, "kind": "reference",
-                                   "sample": f"outer iteration 1 of the same {6 * nx * ny * nz}-cell case, "
-                                             f"reference C++ + LASPack restatement, 1 thread, set-up "
-                                             f"({setup:.1f} s) excluded"}
+            v, which = cpu_rate(its)
+            out["cpu_baseline"] = {"value": v, "unit": "iters/s", "cores": 1, "kind": "reference",
+                                   "sample": f"{which} of the same {6 * nx * ny * nz}-cell case (reference C++ + "
+                                             f"LASPack restatement, {rec['flags']}, 1 thread pinned to core "
+                                             f"{rec['pinned_core']}, set-up {setup:.1f} s excluded)",
+                                   "iteration_seconds": its, "host": rec}
         else:
             out["cpu_baseline"] = {"value": None, "unit": "iters/s", "cores": 1, "kind": "reference",
                                    "sample": err or "no iteration finished within the budget"}
@@ -716,8 +831,12 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the 48-cavity batch form")
     ap.add_argument("--learned-c5", action="store_true",
                     help="only the configuration-5 learned-preconditioner run (4.9 M cells; minutes)")
-    ap.add_argument("--cpu-budget", type=float, default=240.0)
-    ap.add_argument("--ref-budget", type=float, default=150.0)
+    ap.add_argument("--cpu-survey", action="store_true",
+                    help="only the CPU baseline of configurations 1-3 next to the GPU (minutes of CPU time)")
+    ap.add_argument("--cpu-budget", type=float, default=60.0,
+                    help="seconds of reference outer iterations for the cpu_baseline sample (at most 3 iterations)")
+    ap.add_argument("--ref-budget", type=float, default=900.0,
+                    help="reference arm: stop early once its outer iterations add up to this many seconds")
     ap.add_argument("--p-maxit", type=int, default=0,
                     help="cap the p' CG iterations (short profiling runs only; not a bench setting)")
     ap.add_argument("--p-mixed", action="store_true",
@@ -729,7 +848,10 @@ def main():
         import torch.distributed as dist
 
         dist.init_process_group("gloo")
-    if args.learned_c5:
+    if args.cpu_survey:
+        if r == 0:
+            print(json.dumps({"cpu_survey": cpu_survey(args)}))
+    elif args.learned_c5:
         if r == 0:
             print(json.dumps({"learned_c5": c5_learned_run(args)}))
     elif args.impl == "reference":

@@ -218,6 +218,120 @@ __global__ void __launch_bounds__(DENSE_THREADS) k_mg_dense_inverse(int nd, cons
 
 MgView view_of(const SellDev &A, const float *val) { return MgView{A.n, A.sl_ptr.get(), A.sl_w.get(), A.col.get(), val}; }
 
+// ---- the coarse levels in one persistent cooperative launch ------------------
+// Phases (each closed by a grid barrier): restriction of the finest level's t into
+// level 1; for l = 1 .. L-2: t_l = r_l - A_l (w_l r_l), restriction into l+1; the
+// coarsest solve; for l = L-2 .. 1: prolongation w_l r_l + gamma z_{l+1}[agg] into
+// t_l, post-smoothing into z_l; finally the finest prolongation
+// z0 = w0 r0 + gamma z_1[agg0].  Every row is computed by the same arithmetic in
+// the same order as the one-kernel-per-phase path, so both give the same bits.
+// Vectors written inside the launch are read with ld.global.cg (L2, not L1): t is
+// gathered again after other blocks rewrote it.
+constexpr int MGP_THREADS = 1024;
+
+struct MgLvl {
+    int n;
+    const int *sl_ptr, *sl_w, *col;
+    const float *val, *w;
+    float *r, *z, *t;
+    const int *agg, *mem_ptr, *mem_idx;  // to the next level
+};
+
+struct MgPersistArgs {
+    int nlev;
+    MgLvl lv[MG_MAX_LEVELS];
+    const float *r0, *t0;
+    float *z0;
+    int nd;              // rows of the coarsest level if it is dense, else 0
+    const float *minv;
+    float gamma;
+    GridBarrier *gb;
+    int *err;
+    const int *done;
+};
+
+__device__ __forceinline__ float lvl_row(const MgLvl &L, int i, const float *x) {
+    const int base = L.sl_ptr[i >> 5], wd = L.sl_w[i >> 5], lane = i & 31;
+    float s = 0.f;
+    for (int k = 0; k < wd; ++k) {
+        const int pos = base + k * 32 + lane;
+        s += L.val[pos] * __ldcg(x + L.col[pos]);
+    }
+    return s;
+}
+
+__device__ __forceinline__ float lvl_row_wr(const MgLvl &L, int i) {
+    const int base = L.sl_ptr[i >> 5], wd = L.sl_w[i >> 5], lane = i & 31;
+    float s = 0.f;
+    for (int k = 0; k < wd; ++k) {
+        const int pos = base + k * 32 + lane;
+        const int j = L.col[pos];
+        s += L.val[pos] * (L.w[j] * __ldcg(L.r + j));
+    }
+    return s;
+}
+
+__global__ void __launch_bounds__(MGP_THREADS, 1) k_mg_coarse(MgPersistArgs a) {
+    if (a.done && *a.done) return;  // written by earlier launches: every block sees the same value
+    const int T = gridDim.x * blockDim.x, t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    const int L = a.nlev;
+    // restriction of the finest level's t into level 1
+    {
+        const MgLvl &f = a.lv[0];
+        const MgLvl &c = a.lv[1];
+        for (int I = t0; I < c.n; I += T) {
+            float s = 0.f;
+            for (int k = f.mem_ptr[I]; k < f.mem_ptr[I + 1]; ++k) s += __ldcg(a.t0 + f.mem_idx[k]);
+            c.r[I] = s;
+        }
+    }
+    if (!grid_sync(a.gb, a.err)) return;
+    for (int l = 1; l < L - 1; ++l) {
+        const MgLvl &f = a.lv[l];
+        for (int i = t0; i < f.n; i += T) f.t[i] = __ldcg(f.r + i) - lvl_row_wr(f, i);
+        if (!grid_sync(a.gb, a.err)) return;
+        const MgLvl &c = a.lv[l + 1];
+        for (int I = t0; I < c.n; I += T) {
+            float s = 0.f;
+            for (int k = f.mem_ptr[I]; k < f.mem_ptr[I + 1]; ++k) s += __ldcg(f.t + f.mem_idx[k]);
+            c.r[I] = s;
+        }
+        if (!grid_sync(a.gb, a.err)) return;
+    }
+    const MgLvl &c = a.lv[L - 1];
+    if (a.nd > 0) {
+        const int warp = t0 >> 5, lane = threadIdx.x & 31, nw = T >> 5;
+        for (int i = warp; i < a.nd; i += nw) {
+            float s = 0.f;
+            for (int j = lane; j < a.nd; j += 32) s += a.minv[(size_t)i * a.nd + j] * __ldcg(c.r + j);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL_MASK, s, o);
+            if (lane == 0) c.z[i] = s;
+        }
+        if (!grid_sync(a.gb, a.err)) return;
+    } else {  // three Jacobi steps from zero
+        for (int i = t0; i < c.n; i += T) c.z[i] = c.w[i] * __ldcg(c.r + i);
+        if (!grid_sync(a.gb, a.err)) return;
+        for (int i = t0; i < c.n; i += T) c.t[i] = __ldcg(c.z + i) + c.w[i] * (__ldcg(c.r + i) - lvl_row(c, i, c.z));
+        if (!grid_sync(a.gb, a.err)) return;
+        for (int i = t0; i < c.n; i += T) c.z[i] = __ldcg(c.t + i) + c.w[i] * (__ldcg(c.r + i) - lvl_row(c, i, c.t));
+        if (!grid_sync(a.gb, a.err)) return;
+    }
+    for (int l = L - 2; l >= 1; --l) {
+        const MgLvl &f = a.lv[l];
+        const MgLvl &cc = a.lv[l + 1];
+        for (int i = t0; i < f.n; i += T) f.t[i] = f.w[i] * __ldcg(f.r + i) + a.gamma * __ldcg(cc.z + f.agg[i]);
+        if (!grid_sync(a.gb, a.err)) return;
+        for (int i = t0; i < f.n; i += T) f.z[i] = __ldcg(f.t + i) + f.w[i] * (__ldcg(f.r + i) - lvl_row(f, i, f.t));
+        if (!grid_sync(a.gb, a.err)) return;
+    }
+    {
+        const MgLvl &f = a.lv[0];
+        const MgLvl &c1 = a.lv[1];
+        for (int i = t0; i < f.n; i += T) a.z0[i] = f.w[i] * a.r0[i] + a.gamma * __ldcg(c1.z + f.agg[i]);
+    }
+}
+
 }  // namespace
 
 void AggMultigrid::setup(const SellDev &A, const SellPattern &pat, const double *val64_dev, double theta,
@@ -257,6 +371,13 @@ void AggMultigrid::setup(const SellDev &A, const SellPattern &pat, const double 
     tmpt_.alloc(A.n);
     err_.alloc(1);
     err_.zero(st);
+    gb_.alloc(1);
+    gb_.zero(st);  // the barrier's counter returns to 0 or 2^31 after every completed launch
+    if (pblocks_ == 0) {
+        int per_sm = 0;
+        SYSU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mg_coarse, MGP_THREADS, 0));
+        pblocks_ = std::max(1, std::min(per_sm, 1)) * num_sms();
+    }
     static bool attr = false;
     if (!attr) {
         SYSU_CUDA(cudaFuncSetAttribute(k_mg_dense_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -268,6 +389,7 @@ void AggMultigrid::setup(const SellDev &A, const SellPattern &pat, const double 
 
 void AggMultigrid::refresh(const double *val64_dev, const float *val32_dev, cudaStream_t st) {
     if (!ready()) throw CaseError{"multigrid: no hierarchy"};
+    gb_.zero(st);  // a barrier that timed out in an earlier solve starts clean
     val0_32_ = val32_dev;
     const double *fval = val64_dev;
     for (size_t l = 0; l < lv_.size(); ++l) {
@@ -327,6 +449,34 @@ void AggMultigrid::enqueue_cycle_to_fine(const float *r, float *z, const int *do
         ++g_launches;
         return;
     }
+    if (persistent) {
+        MgLevelDev &d0 = *lv_[0];
+        k_mg_down<<<flat_blocks(f.n), MB, 0, st>>>(view_of(*A0_, val0_32_), d0.w.get(), r, d0.t.get(), done);
+        ++g_launches;
+        MgPersistArgs pa{};
+        pa.nlev = L;
+        for (int l = 0; l < L; ++l) {
+            MgLevelDev &d = *lv_[l];
+            const SellDev &A = l == 0 ? *A0_ : d.A;
+            pa.lv[l] = MgLvl{d.n, A.sl_ptr.get(), A.sl_w.get(), A.col.get(), l == 0 ? val0_32_ : d.val32.get(),
+                             d.w.get(), d.r.get(), d.z.get(), d.t.get(), d.agg.get(), d.mem_ptr.get(),
+                             d.mem_idx.get()};
+        }
+        pa.r0 = r;
+        pa.t0 = d0.t.get();
+        pa.z0 = z;
+        pa.nd = nd_ <= MG_DENSE_MAX ? nd_ : 0;
+        pa.minv = dinv_.get();
+        pa.gamma = (float)gamma;
+        pa.gb = gb_.get();
+        pa.err = err_.get();
+        pa.done = done;
+        void *args[] = {&pa};
+        SYSU_CUDA(cudaLaunchCooperativeKernel((const void *)k_mg_coarse, dim3(pblocks_), dim3(MGP_THREADS), args, 0,
+                                              st));
+        ++g_launches;
+        return;
+    }
     enqueue_down(0, r, done, st);
     for (int l = 1; l < L - 1; ++l) enqueue_down(l, lv_[l]->r.get(), done, st);
     MgLevelDev &c = *lv_[L - 1];
@@ -345,6 +495,11 @@ void AggMultigrid::enqueue_cycle_to_fine(const float *r, float *z, const int *do
     MgLevelDev &c1 = *lv_[1];
     k_mg_prolong<<<flat_blocks(f.n), MB, 0, st>>>(f.n, f.w.get(), r, f.agg.get(), c1.z.get(), (float)gamma, z, done);
     ++g_launches;
+}
+
+void AggMultigrid::apply_to_fine(const float *r, float *z2, const int *fs_done, cudaStream_t st) {
+    enqueue_cycle_to_fine(r, z2, fs_done, st);
+    SYSU_CUDA(cudaGetLastError());
 }
 
 void AggMultigrid::apply_fixed(const float *r, float *z2, float *t, const int *fs_done, cudaStream_t st) {

@@ -89,6 +89,11 @@ class AggMultigrid {
     // The fixed part of the cycle at the finest level: z2 = pre-smoothing + coarse
     // correction, t = r - A z2 (the input of the finest post-smoother).
     void apply_fixed(const float *r, float *z2, float *t, const int *fs_done, cudaStream_t st);
+    // z2 alone (the caller forms t = r - A z2 itself, fused with what follows).
+    void apply_to_fine(const float *r, float *z2, const int *fs_done, cudaStream_t st);
+    // true: the coarse levels run as one persistent cooperative launch (grid
+    // barriers between phases); false: one launch per phase.  Same results.
+    bool persistent = true;
     // Training pair for the post-smoother from a pair (r, e = A^-1 r), in place:
     // r <- r - A z2(r), e <- e - z2(r).
     void smoother_pair(float *r, float *e, cudaStream_t st);
@@ -117,6 +122,8 @@ class AggMultigrid {
     DevBuf<float> tmpz_;            // fine-level scratch for apply_fixed / smoother_pair
     DevBuf<float> tmpt_;
     DevBuf<int> err_;
+    DevBuf<GridBarrier> gb_;
+    int pblocks_ = 0;
 };
 
 }  // namespace sysu

@@ -283,6 +283,20 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
                 return SYSU_OK;
             }
             if (f == "learn_iters") { e->learn_iters = std::max(0, (int)value); return SYSU_OK; }
+            if (f == "learn_reset") {
+                // start the learned form over: fresh network, empty pair ring, new training window
+                if (e != &o.p) return set_err(SYSU_ERR_INPUT, "learn_reset is a p' option");
+                return guarded([&] {
+                    sysu::SimpleSolver &S = *s->impl;
+                    S.p_solves = 0;
+                    if (S.gnn.bound()) {
+                        S.gnn.init_params(20261203ULL, S.st);
+                        S.gnn.reset_adam(S.st);
+                        S.gnn.clear_pairs();
+                    }
+                    return SYSU_OK;
+                });
+            }
             if (f == "mg_theta") {
                 if (!(value > 0.0 && value < 1.0)) return set_err(SYSU_ERR_INPUT, "mg_theta: strength threshold in (0, 1)");
                 e->mg_theta = value;

@@ -809,33 +809,41 @@ __global__ void k_fcg_jacobi(FcgArgs a) {
     if (grid_sums<1>(v, a.part, &a.fs->cnt[0])) a.fs->zq = v[0];
 }
 
-// multigrid form with the network: scale s2 = rms(D^-1 t) of the post-smoother's input
-__global__ void k_fcg_tscale(FcgArgs a, const float *t) {
-    if (a.fs->done || !a.fs->use_gnn) return;
+// multigrid form, finest level after the coarse correction z2: t = r - A z2, then
+// either (network off) z = z2 + w t and z.q_prev for the flexible beta, or
+// (network on) t for the network and its scale s2 = rms(D^-1 t)
+__global__ void k_fcg_mgfine(FcgArgs a, const float *z2, float *t, const float *w) {
+    if (a.fs->done) return;
+    const bool net = a.fs->use_gnn, rs = a.fs->restart;
     double v[1] = {0.0};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.g.n; i += gridDim.x * blockDim.x) {
-        double u = (double)a.g.dinv[i] * t[i];
-        v[0] += u * u;
+        const int sl = i >> 5, lane = i & 31;
+        const int base = a.g.sl_ptr[sl], wd = a.g.sl_w[sl];
+        float az = 0.f;
+        for (int k = 0; k < wd; ++k) {
+            int pos = base + k * 32 + lane;
+            az += a.g.val[pos] * z2[a.g.col[pos]];
+        }
+        const float ti = a.r[i] - az;
+        if (net) {
+            t[i] = ti;
+            double u = (double)a.g.dinv[i] * ti;
+            v[0] += u * u;
+        } else {
+            const float zi = z2[i] + w[i] * ti;
+            a.z[i] = zi;
+            if (!rs) v[0] += (double)zi * a.q[i];
+        }
     }
-    if (grid_sums<1>(v, a.part, &a.fs->cnt[3])) {
-        double s = sqrt(v[0] / (double)a.g.n);
-        a.fs->s2 = (float)s;
-        a.fs->inv_s2 = s > 0.0 ? (float)(1.0 / s) : 0.f;
+    if (grid_sums<1>(v, a.part, &a.fs->cnt[0])) {
+        if (net) {
+            double s = sqrt(v[0] / (double)a.g.n);
+            a.fs->s2 = (float)s;
+            a.fs->inv_s2 = s > 0.0 ? (float)(1.0 / s) : 0.f;
+        } else {
+            a.fs->zq = v[0];
+        }
     }
-}
-
-// multigrid form, Jacobi post-smoothing (also the fallback when the network is
-// off): z = z2 + w t, and z.q_prev for the flexible beta
-__global__ void k_fcg_mgpost(FcgArgs a, const float *z2, const float *t, const float *w) {
-    if (a.fs->done || a.fs->use_gnn) return;
-    double v[1] = {0.0};
-    const bool rs = a.fs->restart;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.g.n; i += gridDim.x * blockDim.x) {
-        float zi = z2[i] + w[i] * t[i];
-        a.z[i] = zi;
-        if (!rs) v[0] += (double)zi * a.q[i];
-    }
-    if (grid_sums<1>(v, a.part, &a.fs->cnt[0])) a.fs->zq = v[0];
 }
 
 __global__ void k_fcg_dir(FcgArgs a) {
@@ -1345,13 +1353,10 @@ void GnnPrecond::last_losses(std::vector<double> &out, int count, cudaStream_t s
 void GnnPrecond::fcg_iteration(const void *args, bool use_gnn, cudaStream_t st) {
     const FcgArgs &a = *static_cast<const FcgArgs *>(args);
     if (mg_) {
-        mg_->apply_fixed(a.r, z2_.get(), t_.get(), &a.fs->done, st);
-        if (use_gnn) {
-            k_fcg_tscale<<<gflat_, FB, 0, st>>>(a, t_.get());
-            ++g_launches;
-            forward(t_.get(), a.z, false, a.fs, a.q, st, z2_.get());
-        }
-        k_fcg_mgpost<<<gflat_, FB, 0, st>>>(a, z2_.get(), t_.get(), mg_->w0());
+        mg_->apply_to_fine(a.r, z2_.get(), &a.fs->done, st);
+        k_fcg_mgfine<<<gflat_, FB, 0, st>>>(a, z2_.get(), t_.get(), mg_->w0());
+        ++g_launches;
+        if (use_gnn) forward(t_.get(), a.z, false, a.fs, a.q, st, z2_.get());
     } else {
         if (use_gnn) forward(a.r, a.z, false, a.fs, a.q, st);
         k_fcg_jacobi<<<gflat_, FB, 0, st>>>(a);
@@ -1360,7 +1365,7 @@ void GnnPrecond::fcg_iteration(const void *args, bool use_gnn, cudaStream_t st) 
     k_fcg_upd<<<gflat_, FB, 0, st>>>(a);
     k_fcg_rel1<<<gflat_, FB, 0, st>>>(a);
     k_fcg_rel2<<<gflat_, FB, 0, st>>>(a);
-    g_launches += 5;
+    g_launches += mg_ ? 4 : 5;
     SYSU_CUDA(cudaGetLastError());
 }
 

@@ -496,12 +496,17 @@ void SimpleSolver::solve_learned(const EqOpts &o, const double *val, const doubl
     ko.omega = o.omega;
     ko.jacobi = true;
     ko.inner_tol = o.inner_tol;
+    auto mg_check = [&] {
+        if (use_mg && mg.err_flag(st)) throw CaseError{"p' multigrid: a bounded wait timed out or the coarsest level is singular"};
+    };
     if (!o.learned) {
         gnn.fcg(b, x, x0_zero, ko, false, info, st);
+        mg_check();
         return;
     }
     if (p_solves++ >= o.learn_iters) {
         gnn.fcg(b, x, x0_zero, ko, true, info, st);
+        mg_check();
         return;
     }
     auto plain = [&](double eps, bool zero) {
