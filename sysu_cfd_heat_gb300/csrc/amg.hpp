@@ -93,7 +93,7 @@ class AggMultigrid {
     void apply_to_fine(const float *r, float *z2, const int *fs_done, cudaStream_t st);
     // true: the coarse levels run as one persistent cooperative launch (grid
     // barriers between phases); false: one launch per phase.  Same results.
-    bool persistent = true;
+    bool persistent = false;
     // Training pair for the post-smoother from a pair (r, e = A^-1 r), in place:
     // r <- r - A z2(r), e <- e - z2(r).
     void smoother_pair(float *r, float *e, cudaStream_t st);

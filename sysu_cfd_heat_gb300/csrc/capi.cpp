@@ -312,6 +312,7 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
                 e->mg_gamma = value;
                 return SYSU_OK;
             }
+            if (f == "mg_persistent") { e->mg_persistent = value != 0.0; return SYSU_OK; }
             if (f == "learn_steps") { e->learn_steps = std::max(0, (int)value); return SYSU_OK; }
             if (f == "learn_lr") { e->learn_lr = value; return SYSU_OK; }
             if (f == "learn_kind") {
@@ -357,6 +358,7 @@ int sysu_solver_get_option(sysu_solver *s, const char *key, double *value) {
             if (f == "mg_theta") { *value = e->mg_theta; return SYSU_OK; }
             if (f == "mg_omega") { *value = e->mg_omega; return SYSU_OK; }
             if (f == "mg_gamma") { *value = e->mg_gamma; return SYSU_OK; }
+            if (f == "mg_persistent") { *value = e->mg_persistent; return SYSU_OK; }
             if (f == "learn_steps") { *value = e->learn_steps; return SYSU_OK; }
             if (f == "learn_lr") { *value = e->learn_lr; return SYSU_OK; }
             if (f == "learn_kind") { *value = e->learn_kind; return SYSU_OK; }

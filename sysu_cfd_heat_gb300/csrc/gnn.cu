@@ -54,6 +54,10 @@ __device__ __forceinline__ uint32_t bf_pack(float a, float b) {
 }
 __device__ __forceinline__ float bf_round(float a) { return __bfloat162float(__float2bfloat16_rn(a)); }
 
+// The flexible-CG kernels accumulate each thread's rows (a handful) in FP32 and
+// hand those partials to grid_sums in FP64: per-row FP64 arithmetic and
+// conversions run on GB300's FP64 pipe (1/64 of the FP32 rate) and took half of
+// these kernels' time.  Convergence is decided on the FP64 residual b - A x.
 // Block partial sums of NV values -> part[block][NV]; the last block to arrive
 // adds them up (every thread of that block loads a strided share, then a block
 // reduction in a fixed order).  Returns true in exactly one thread (thread 0 of
@@ -799,13 +803,14 @@ __global__ void k_fcg_zero(int n, double *x) {
 
 __global__ void k_fcg_jacobi(FcgArgs a) {
     if (a.fs->done || a.fs->use_gnn) return;
-    double v[1] = {0.0};
+    float f0 = 0.f;
     const bool rs = a.fs->restart;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.g.n; i += gridDim.x * blockDim.x) {
         float zi = a.g.dinv[i] * a.r[i];
         a.z[i] = zi;
-        if (!rs) v[0] += (double)zi * a.q[i];
+        if (!rs) f0 += zi * a.q[i];
     }
+    double v[1] = {f0};
     if (grid_sums<1>(v, a.part, &a.fs->cnt[0])) a.fs->zq = v[0];
 }
 
@@ -815,7 +820,7 @@ __global__ void k_fcg_jacobi(FcgArgs a) {
 __global__ void k_fcg_mgfine(FcgArgs a, const float *z2, float *t, const float *w) {
     if (a.fs->done) return;
     const bool net = a.fs->use_gnn, rs = a.fs->restart;
-    double v[1] = {0.0};
+    float f0 = 0.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.g.n; i += gridDim.x * blockDim.x) {
         const int sl = i >> 5, lane = i & 31;
         const int base = a.g.sl_ptr[sl], wd = a.g.sl_w[sl];
@@ -827,14 +832,15 @@ __global__ void k_fcg_mgfine(FcgArgs a, const float *z2, float *t, const float *
         const float ti = a.r[i] - az;
         if (net) {
             t[i] = ti;
-            double u = (double)a.g.dinv[i] * ti;
-            v[0] += u * u;
+            const float u = a.g.dinv[i] * ti;
+            f0 += u * u;
         } else {
             const float zi = z2[i] + w[i] * ti;
             a.z[i] = zi;
-            if (!rs) v[0] += (double)zi * a.q[i];
+            if (!rs) f0 += zi * a.q[i];
         }
     }
+    double v[1] = {f0};
     if (grid_sums<1>(v, a.part, &a.fs->cnt[0])) {
         if (net) {
             double s = sqrt(v[0] / (double)a.g.n);
@@ -851,7 +857,7 @@ __global__ void k_fcg_dir(FcgArgs a) {
     const bool rs = a.fs->restart;
     const double beta = rs ? 0.0 : a.fs->zq / a.fs->pq_prev;
     const float bf = (float)beta;
-    double v[2] = {0.0, 0.0};
+    float f0 = 0.f, f1 = 0.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.g.n; i += gridDim.x * blockDim.x) {
         const int sl = i >> 5, lane = i & 31;
         const int base = a.g.sl_ptr[sl], w = a.g.sl_w[sl];
@@ -864,9 +870,10 @@ __global__ void k_fcg_dir(FcgArgs a) {
         float pi = rs ? a.z[i] : a.z[i] - bf * a.p[i];
         a.q[i] = qi;
         a.p[i] = pi;
-        v[0] += (double)pi * qi;
-        v[1] += (double)pi * a.r[i];
+        f0 += pi * qi;
+        f1 += pi * a.r[i];
     }
+    double v[2] = {f0, f1};
     if (grid_sums<2>(v, a.part, &a.fs->cnt[1])) {
         FcgState *f = a.fs;
         double pq = v[0], pr = v[1];
@@ -894,7 +901,7 @@ __global__ void k_fcg_dir(FcgArgs a) {
 __global__ void k_fcg_upd(FcgArgs a) {
     if (a.fs->done) return;
     const float al = (float)a.fs->alpha;
-    double v[2] = {0.0, 0.0};
+    float f0 = 0.f, f1 = 0.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.g.n; i += gridDim.x * blockDim.x) {
         float ri = a.r[i];
         if (al != 0.f) {
@@ -902,10 +909,11 @@ __global__ void k_fcg_upd(FcgArgs a) {
             ri -= al * a.q[i];
             a.r[i] = ri;
         }
-        double u = (double)a.g.dinv[i] * ri;
-        v[0] += (double)ri * ri;
-        v[1] += u * u;
+        const float u = a.g.dinv[i] * ri;
+        f0 += ri * ri;
+        f1 += u * u;
     }
+    double v[2] = {f0, f1};
     if (grid_sums<2>(v, a.part, &a.fs->cnt[2])) {
         FcgState *f = a.fs;
         f->iters += 1;
@@ -1404,7 +1412,8 @@ void GnnPrecond::fcg(const double *b, double *x, bool x0_zero, const KrylovOpts 
     // (re)capture the chunk graph when its arguments changed
     ChunkGraph &cg = graphs_[(mg_ ? 2 : 0) + (use_gnn ? 1 : 0)];
     if (!cg.exec || cg.inner_tol != o.inner_tol || cg.stall_max != stall_max || cg.chunk != check_every ||
-        cg.val32 != val32_ || cg.dinv != dinv_.get() || cg.mg != mg_) {
+        cg.val32 != val32_ || cg.dinv != dinv_.get() || cg.mg != mg_ ||
+        (mg_ && (cg.mg_gamma != mg_->gamma || cg.mg_persistent != mg_->persistent))) {
         if (cg.exec) cudaGraphExecDestroy(cg.exec);
         cg.exec = nullptr;
         long before = g_launches.load();
@@ -1422,6 +1431,8 @@ void GnnPrecond::fcg(const double *b, double *x, bool x0_zero, const KrylovOpts 
         cg.val32 = val32_;
         cg.dinv = dinv_.get();
         cg.mg = mg_;
+        cg.mg_gamma = mg_ ? mg_->gamma : 0.0;
+        cg.mg_persistent = mg_ ? mg_->persistent : false;
     }
     int done = 0;
     for (int it = 0; it < o.maxit && !done; it += check_every) {

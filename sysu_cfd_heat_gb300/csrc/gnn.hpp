@@ -146,6 +146,8 @@ class GnnPrecond {
         long launches = 0;
         const float *val32 = nullptr, *dinv = nullptr;
         const AggMultigrid *mg = nullptr;
+        double mg_gamma = 0.0;  // a kernel argument of the captured cycle
+        bool mg_persistent = false;
     };
     ChunkGraph graphs_[4];
     void drop_graphs();

@@ -485,6 +485,7 @@ void SimpleSolver::solve_learned(const EqOpts &o, const double *val, const doubl
         }
         mg.omega = o.mg_omega;
         mg.gamma = o.mg_gamma;
+        mg.persistent = o.mg_persistent != 0;  // part of the captured iterations' key
         mg.refresh(val, f.Ap32.get(), st);
         if (gnn.multigrid() != &mg) gnn.attach_multigrid(&mg);
     } else if (gnn.multigrid()) {

@@ -58,6 +58,7 @@ struct EqOpts {
     double mg_theta = 0.25;
     double mg_omega = 0.8;
     double mg_gamma = 1.8;
+    int mg_persistent = 0;    // 1: the coarse levels as one persistent cooperative launch
 };
 
 struct SolverOptions {
