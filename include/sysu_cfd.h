@@ -171,6 +171,16 @@ long sysu_solver_field_size(sysu_solver *s, const char *name);
 int sysu_solver_get_field(sysu_solver *s, const char *name, double *out, long n);
 int sysu_solver_set_field(sysu_solver *s, const char *name, const double *in, long n);
 int sysu_solver_sync(sysu_solver *s);
+/* The p' multigrid form (option p.precond 4; no counterpart in the reference,
+ * whose p' solve is CG + SSOR, navier_pressure.cpp:29).  sysu_solver_p_cycle:
+ * z = M r, one application of the cycle as the last p' solve left it (its
+ * matrix values, and its network on its level when use_net).
+ * sysu_solver_p_network: the level of the p' network (0 the finest, >= 1 a
+ * coarse level of the cycle) and, when params is not NULL, its np =
+ * sysu_gnn_num_params() parameters; sysu_solver_p_set_network replaces them. */
+int sysu_solver_p_cycle(sysu_solver *s, const double *r, double *z, int use_net);
+int sysu_solver_p_network(sysu_solver *s, int *level, float *params, int np);
+int sysu_solver_p_set_network(sysu_solver *s, const float *params, int np);
 /* Assembled matrix "mom", "p", "scalar" (last k/eps/T) or "solid" as CSR,
  * diagonal first in each row.  With rowptr == NULL returns the entry count;
  * otherwise fills rowptr[n+1], col[], val[] and returns the count (-1: error). */

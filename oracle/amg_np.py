@@ -163,8 +163,10 @@ def _coarsest(L: Level, r, omega, dense_max):
     return z
 
 
-def _prolonged(levels, l, r, omega, gamma, dense_max):
-    """Level l's correction before its post-smoothing step: w r + gamma P z_{l+1}."""
+def _prolonged(levels, l, r, omega, gamma, dense_max, post=None):
+    """Level l's correction before its post-smoothing step: w r + gamma P z_{l+1}.
+    post: {level: f(r, zp) -> z} replaces that coarse level's post-smoothing step
+    (the learned form's network on a coarse level)."""
     L = levels[l]
     w = omega / L.diag
     t = r - L.matvec(w * r)
@@ -174,24 +176,27 @@ def _prolonged(levels, l, r, omega, gamma, dense_max):
         zc = _coarsest(levels[l + 1], rc, omega, dense_max)
     else:
         C = levels[l + 1]
-        zc = _prolonged(levels, l + 1, rc, omega, gamma, dense_max)
-        zc = zc + omega / C.diag * (rc - C.matvec(zc))
+        zc = _prolonged(levels, l + 1, rc, omega, gamma, dense_max, post)
+        if post and (l + 1) in post:
+            zc = post[l + 1](rc, zc)
+        else:
+            zc = zc + omega / C.diag * (rc - C.matvec(zc))
     return w * r + gamma * zc[L.agg]
 
 
-def cycle_fixed(levels, r, omega=0.8, gamma=1.8, dense_max=200):
+def cycle_fixed(levels, r, omega=0.8, gamma=1.8, dense_max=200, post=None):
     """Pre-smoothing and coarse correction at the finest level: z2, and t = r - A z2."""
     L0 = levels[0]
     if len(levels) == 1:
         z2 = omega / L0.diag * r
     else:
-        z2 = _prolonged(levels, 0, r, omega, gamma, dense_max)
+        z2 = _prolonged(levels, 0, r, omega, gamma, dense_max, post)
     return z2, r - L0.matvec(z2)
 
 
-def vcycle(levels, r, omega=0.8, gamma=1.8, dense_max=200):
+def vcycle(levels, r, omega=0.8, gamma=1.8, dense_max=200, post=None):
     """z = M r with the Jacobi post-smoother at the finest level."""
-    z2, t = cycle_fixed(levels, r, omega, gamma, dense_max)
+    z2, t = cycle_fixed(levels, r, omega, gamma, dense_max, post)
     return z2 + omega / levels[0].diag * t
 
 

@@ -84,7 +84,7 @@ class Graph:
         return (self.off(x) + (self.diag.reshape((-1,) + (1,) * (np.ndim(x) - 1)) * x)).astype(self.dtype)
 
 
-def forward(p, g: Graph, r, exact=False):
+def forward(p, g: Graph, r, exact=False, skip=1.0):
     dt = np.float64 if exact else np.float32
     rnd = (lambda x: np.asarray(x, dtype=dt)) if exact else bf16
     e, c, Ws, bs, wd, bd = [np.asarray(a, dtype=dt) if np.ndim(a) else dt(a) for a in unpack(p)]
@@ -108,15 +108,15 @@ def forward(p, g: Graph, r, exact=False):
         cache["X"].append(X)
         cache["pre"].append(pre)
         cache["h"].append(h)
-    z = s * (u + (h.astype(np.float64) @ wd.astype(np.float64)).astype(dt) + bd)
+    z = s * (dt(skip) * u + (h.astype(np.float64) @ wd.astype(np.float64)).astype(dt) + bd)
     return z.astype(dt), cache
 
 
-def loss_and_grad(p, g: Graph, r, e_true, kind=0, exact=False):
+def loss_and_grad(p, g: Graph, r, e_true, kind=0, exact=False, skip=1.0):
     """Loss of one pair and its gradient with respect to the flat parameters."""
     dt = np.float64 if exact else np.float32
     rnd = (lambda x: np.asarray(x, dtype=dt)) if exact else bf16
-    z, C = forward(p, g, r, exact)
+    z, C = forward(p, g, r, exact, skip)
     e_true = np.asarray(e_true, dtype=dt)
     t = z - e_true
     St = g.sgn * g.matvec(t).astype(np.float64)

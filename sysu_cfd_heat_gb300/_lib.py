@@ -58,6 +58,9 @@ def lib() -> C.CDLL:
             "sysu_solver_get_field": (C.c_int, [vp, cp, dp, C.c_long]),
             "sysu_solver_set_field": (C.c_int, [vp, cp, dp, C.c_long]),
             "sysu_solver_sync": (C.c_int, [vp]),
+            "sysu_solver_p_cycle": (C.c_int, [vp, dp, dp, C.c_int]),
+            "sysu_solver_p_network": (C.c_int, [vp, ip, C.POINTER(C.c_float), C.c_int]),
+            "sysu_solver_p_set_network": (C.c_int, [vp, C.POINTER(C.c_float), C.c_int]),
             "sysu_solver_reset": (C.c_int, [vp]),
             "sysu_solver_timer_start": (C.c_int, [vp]),
             "sysu_solver_timer_stop": (C.c_int, [vp, dp]),

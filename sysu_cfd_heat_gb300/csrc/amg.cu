@@ -108,6 +108,10 @@ __global__ void k_mg_sub(int n, float *e, const float *z) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) e[i] -= z[i];
 }
 
+__global__ void k_mg_to_f64(int n, const float *a, double *b) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = a[i];
+}
+
 // z = w r (a coarsest level too large for the dense inverse: Jacobi sweeps)
 __global__ void k_mg_scale(int n, const float *w, const float *r, float *z, const int *done) {
     if (done && *done) return;
@@ -338,6 +342,12 @@ __global__ void __launch_bounds__(MGP_THREADS, 1) k_mg_coarse(MgPersistArgs a) {
 
 }  // namespace
 
+void mg_to_f64(const float *a, double *b, int n, cudaStream_t st) {
+    k_mg_to_f64<<<flat_blocks(n), MB, 0, st>>>(n, a, b);
+    ++g_launches;
+    SYSU_CUDA(cudaGetLastError());
+}
+
 void AggMultigrid::setup(const SellDev &A, const SellPattern &pat, const double *val64_dev, double theta,
                          cudaStream_t st) {
     A0_ = &A;
@@ -347,6 +357,8 @@ void AggMultigrid::setup(const SellDev &A, const SellPattern &pat, const double 
     sgn_ = hv.empty() || hv[0] >= 0.0 ? 1.0f : -1.0f;
     std::vector<MgHostLevel> H = mg_build_hierarchy(pat, hv, theta, MG_DENSE_MAX);
     lv_.clear();
+    hpat_.assign(H.size(), SellPattern{});
+    for (size_t l = 1; l < H.size(); ++l) hpat_[l] = H[l].pat;
     for (size_t l = 0; l < H.size(); ++l) {
         auto d = std::make_unique<MgLevelDev>();
         const MgHostLevel &h = H[l];
@@ -438,9 +450,21 @@ void AggMultigrid::enqueue_up(int l, float *zout, const int *done, cudaStream_t 
     const SellDev &A = d.A;
     k_mg_prolong<<<flat_blocks(d.n), MB, 0, st>>>(d.n, d.w.get(), d.r.get(), d.agg.get(), c.z.get(), (float)gamma,
                                                    d.t.get(), done);
+    ++g_launches;
+    if (post_hook && l == post_level) {
+        post_hook(l, d.r.get(), d.t.get(), zout, done, st);
+        return;
+    }
     k_mg_post<<<flat_blocks(d.n), MB, 0, st>>>(view_of(A, d.val32.get()), d.w.get(), d.r.get(), d.t.get(), zout,
                                                 done);
-    g_launches += 2;
+    ++g_launches;
+}
+
+void AggMultigrid::level_rhs(int l, const float *r0, float *out, cudaStream_t st) {
+    if (l < 1 || l >= levels()) throw CaseError{"multigrid: no such coarse level"};
+    enqueue_down(0, r0, nullptr, st);
+    for (int k = 1; k < l; ++k) enqueue_down(k, lv_[k]->r.get(), nullptr, st);
+    SYSU_CUDA(cudaMemcpyAsync(out, lv_[l]->r.get(), sizeof(float) * lv_[l]->n, cudaMemcpyDeviceToDevice, st));
 }
 
 // Levels 1.. of the cycle for the residual r at level 0; leaves the prolonged
@@ -453,7 +477,7 @@ void AggMultigrid::enqueue_cycle_to_fine(const float *r, float *z, const int *do
         ++g_launches;
         return;
     }
-    if (persistent) {
+    if (persistent && !(post_hook && post_level >= 1)) {
         MgLevelDev &d0 = *lv_[0];
         k_mg_down<<<flat_blocks(f.n), MB, 0, st>>>(view_of(*A0_, val0_32_), d0.w.get(), r, d0.t.get(), done);
         ++g_launches;

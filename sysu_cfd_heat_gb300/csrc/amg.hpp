@@ -34,6 +34,7 @@
 // the network applied to t = r - A z:  z += N(t).
 #pragma once
 
+#include <functional>
 #include <memory>
 #include <vector>
 
@@ -69,6 +70,9 @@ struct MgLevelDev {
     DevBuf<int> agg, mem_ptr, mem_idx, gal_ptr, gal_src;  // to the next level
 };
 
+// b = a in FP64 (n values on the device)
+void mg_to_f64(const float *a, double *b, int n, cudaStream_t st);
+
 class AggMultigrid {
   public:
     AggMultigrid() = default;
@@ -98,6 +102,26 @@ class AggMultigrid {
     // r <- r - A z2(r), e <- e - z2(r).
     void smoother_pair(float *r, float *e, cudaStream_t st);
 
+    // The post-smoothing step of one coarse level, post_level (1 <= post_level <
+    // levels() - 1), replaced by post_hook: called while the cycle is enqueued,
+    // with the level, its right-hand side r, the prolonged correction
+    // zp = w r + gamma P z_{l+1}, the output z and the done flag; it enqueues
+    // z = zp + (a smoothing step for r - A zp).  Kernels enqueued from it run
+    // inside the flexible CG's captured iterations.  The persistent form does
+    // not take a hook (the one-launch-per-phase form runs then).
+    std::function<void(int, const float *, const float *, float *, const int *, cudaStream_t)> post_hook;
+    int post_level = -1;
+    // Level l >= 1: its matrix (device pattern, FP64 and FP32 values), host
+    // pattern and smoother weights w = omega / a_ii.
+    const SellDev &level_matrix(int l) const { return lv_[l]->A; }
+    const double *level_val64(int l) const { return lv_[l]->val64.get(); }
+    const float *level_val32(int l) const { return lv_[l]->val32.get(); }
+    const SellPattern &level_pattern(int l) const { return hpat_[l]; }
+    const float *level_w(int l) const { return lv_[l]->w.get(); }
+    // The right-hand side the cycle hands level l >= 1 for the finest-level
+    // residual r0 (l times pre-smoothing residual and restriction), into out.
+    void level_rhs(int l, const float *r0, float *out, cudaStream_t st);
+
     int levels() const { return (int)lv_.size(); }
     int level_rows(int l) const { return lv_[l]->n; }
     long level_nnz(int l) const { return l == 0 ? A0_->nnz_true : lv_[l]->A.nnz_true; }
@@ -117,6 +141,7 @@ class AggMultigrid {
     const float *val0_32_ = nullptr;
     float sgn_ = 1.0f;
     std::vector<std::unique_ptr<MgLevelDev>> lv_;
+    std::vector<SellPattern> hpat_;  // host patterns of levels >= 1 (level 0: empty)
     int nd_ = 0;                    // rows of the dense coarsest level
     DevBuf<float> dinv_;            // coarsest inverse, nd_ x nd_
     DevBuf<float> tmpz_;            // fine-level scratch for apply_fixed / smoother_pair

@@ -289,10 +289,11 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
                 return guarded([&] {
                     sysu::SimpleSolver &S = *s->impl;
                     S.p_solves = 0;
-                    if (S.gnn.bound()) {
-                        S.gnn.init_params(20261203ULL, S.st);
-                        S.gnn.reset_adam(S.st);
-                        S.gnn.clear_pairs();
+                    for (sysu::GnnPrecond *g : {&S.gnn, &S.gnn_c}) {
+                        if (!g->bound()) continue;
+                        g->init_params(20261203ULL, S.st);
+                        g->reset_adam(S.st);
+                        g->clear_pairs();
                     }
                     return SYSU_OK;
                 });
@@ -313,6 +314,11 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
                 return SYSU_OK;
             }
             if (f == "mg_persistent") { e->mg_persistent = value != 0.0; return SYSU_OK; }
+            if (f == "learn_level") {
+                if (value < 0.0 || value > 15.0) return set_err(SYSU_ERR_INPUT, "learn_level: multigrid level 0..15");
+                e->learn_level = (int)value;
+                return SYSU_OK;
+            }
             if (f == "learn_steps") { e->learn_steps = std::max(0, (int)value); return SYSU_OK; }
             if (f == "learn_lr") { e->learn_lr = value; return SYSU_OK; }
             if (f == "learn_kind") {
@@ -359,6 +365,7 @@ int sysu_solver_get_option(sysu_solver *s, const char *key, double *value) {
             if (f == "mg_omega") { *value = e->mg_omega; return SYSU_OK; }
             if (f == "mg_gamma") { *value = e->mg_gamma; return SYSU_OK; }
             if (f == "mg_persistent") { *value = e->mg_persistent; return SYSU_OK; }
+            if (f == "learn_level") { *value = e->learn_level; return SYSU_OK; }
             if (f == "learn_steps") { *value = e->learn_steps; return SYSU_OK; }
             if (f == "learn_lr") { *value = e->learn_lr; return SYSU_OK; }
             if (f == "learn_kind") { *value = e->learn_kind; return SYSU_OK; }
@@ -601,6 +608,42 @@ int sysu_solver_solve_stats(sysu_solver *s, int *iters, double *res, int *status
             if (status) status[k * 3 + c] = I.status[c];
         }
     return SYSU_OK;
+}
+
+int sysu_solver_p_cycle(sysu_solver *s, const double *r, double *z, int use_net) {
+    if (!s || !r || !z) return set_err(SYSU_ERR_INPUT, "null argument");
+    return guarded([&] {
+        s->impl->p_cycle(r, z, use_net != 0);
+        return SYSU_OK;
+    });
+}
+
+int sysu_solver_p_network(sysu_solver *s, int *level, float *params, int np) {
+    if (!s || !level) return set_err(SYSU_ERR_INPUT, "null argument");
+    return guarded([&] {
+        sysu::SimpleSolver &S = *s->impl;
+        const bool coarse = S.gnn.multigrid() == &S.mg && S.gnn.net_level >= 1;
+        *level = coarse ? S.gnn.net_level : 0;
+        sysu::GnnPrecond &g = coarse ? S.gnn_c : S.gnn;
+        if (params) {
+            if (np != sysu::GNN_NPARAM) throw sysu::CaseError{"sysu_solver_p_network: need sysu_gnn_num_params() values"};
+            if (!g.bound()) throw sysu::CaseError{"sysu_solver_p_network: no network yet"};
+            g.get_params(params, S.st);
+        }
+        return SYSU_OK;
+    });
+}
+
+int sysu_solver_p_set_network(sysu_solver *s, const float *params, int np) {
+    if (!s || !params || np != sysu::GNN_NPARAM) return set_err(SYSU_ERR_INPUT, "need sysu_gnn_num_params() values");
+    return guarded([&] {
+        sysu::SimpleSolver &S = *s->impl;
+        const bool coarse = S.gnn.multigrid() == &S.mg && S.gnn.net_level >= 1;
+        sysu::GnnPrecond &g = coarse ? S.gnn_c : S.gnn;
+        if (!g.bound()) throw sysu::CaseError{"sysu_solver_p_set_network: no network yet"};
+        g.set_params(params, S.st);
+        return SYSU_OK;
+    });
 }
 
 int sysu_solver_timing(sysu_solver *s, double *p_ms, double *mom_ms) {

@@ -106,6 +106,7 @@ struct NetArgs {
     float *aw;
     float *z;
     const float *zbase;  // multigrid form: z = zbase + network output
+    float skip;          // weight of the Jacobi term u in the decoder (1 as a whole preconditioner)
     const float *qprev;
     FcgState *fs;
     double *part;
@@ -288,7 +289,7 @@ __global__ void __launch_bounds__(GT) k_gnn_fwd(NetArgs a) {
 #pragma unroll
                 for (int c = 0; c < 32; c += 2) acc += sprm[96 + c] * bf_lo(ho[c >> 1]) + sprm[97 + c] * bf_hi(ho[c >> 1]);
                 float u = di * a.r[row] * inv_s;
-                float zi = s * (u + acc);
+                float zi = s * (a.skip * u + acc);
                 if (a.zbase) zi += a.zbase[row];
                 a.z[row] = zi;
                 if (a.qprev) zq += (double)zi * (double)a.qprev[row];
@@ -817,9 +818,9 @@ __global__ void k_fcg_jacobi(FcgArgs a) {
 // multigrid form, finest level after the coarse correction z2: t = r - A z2, then
 // either (network off) z = z2 + w t and z.q_prev for the flexible beta, or
 // (network on) t for the network and its scale s2 = rms(D^-1 t)
-__global__ void k_fcg_mgfine(FcgArgs a, const float *z2, float *t, const float *w) {
+__global__ void k_fcg_mgfine(FcgArgs a, const float *z2, float *t, const float *w, int fine_net) {
     if (a.fs->done) return;
-    const bool net = a.fs->use_gnn, rs = a.fs->restart;
+    const bool net = fine_net && a.fs->use_gnn, rs = a.fs->restart;
     float f0 = 0.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.g.n; i += gridDim.x * blockDim.x) {
         const int sl = i >> 5, lane = i & 31;
@@ -849,6 +850,57 @@ __global__ void k_fcg_mgfine(FcgArgs a, const float *z2, float *t, const float *
         } else {
             a.fs->zq = v[0];
         }
+    }
+}
+
+// network as a coarse level's post-smoother: t = r - A zp on that level, and
+// (network on) the network's input scale s2 = rms(D^-1 t) into the finest-level
+// flexible CG's state
+__global__ void k_lvl_resid(GView g, const float *r, const float *zp, float *t, FcgState *fs, double *part) {
+    if (fs->done) return;
+    const bool net = fs->use_gnn;  // written by other launches only: uniform here
+    float f0 = 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x) {
+        const int base = g.sl_ptr[i >> 5], wd = g.sl_w[i >> 5], lane = i & 31;
+        float az = 0.f;
+        for (int k = 0; k < wd; ++k) {
+            int pos = base + k * 32 + lane;
+            az += g.val[pos] * zp[g.col[pos]];
+        }
+        const float ti = r[i] - az;
+        t[i] = ti;
+        if (net) {
+            const float u = g.dinv[i] * ti;
+            f0 += u * u;
+        }
+    }
+    if (!net) return;
+    double v[1] = {f0};
+    if (grid_sums<1>(v, part, &fs->cnt[3])) {
+        double s = sqrt(v[0] / (double)g.n);
+        fs->s2 = (float)s;
+        fs->inv_s2 = s > 0.0 ? (float)(1.0 / s) : 0.f;
+    }
+}
+
+// the Jacobi post-smoothing step of that level while the network is off
+__global__ void k_lvl_jacobi(int n, const float *zp, const float *w, const float *t, float *z, const FcgState *fs) {
+    if (fs->done || fs->use_gnn) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) z[i] = zp[i] + w[i] * t[i];
+}
+
+// r = b - A x1 (FP64) rounded to FP32; x1 == nullptr: r = b
+__global__ void k_res32(GView g, const double *val64, const double *b, const double *x1, float *r) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x) {
+        double ri = b[i];
+        if (x1) {
+            const int base = g.sl_ptr[i >> 5], wd = g.sl_w[i >> 5], lane = i & 31;
+            for (int k = 0; k < wd; ++k) {
+                int pos = base + k * 32 + lane;
+                ri -= val64[pos] * x1[g.col[pos]];
+            }
+        }
+        r[i] = (float)ri;
     }
 }
 
@@ -1143,6 +1195,7 @@ void GnnPrecond::forward(const float *r32, float *z32, bool train, FcgState *fs,
     a.inv_s_p = fs ? (zbase ? &fs->inv_s2 : &fs->inv_s) : &sc_.get()->inv_s;
     a.s_p = fs ? (zbase ? &fs->s2 : &fs->s) : &sc_.get()->s;
     a.zbase = zbase;
+    a.skip = skip;
     a.prm = p_.get();
     a.aw = aw_.get();
     a.z = z32;
@@ -1229,6 +1282,24 @@ void GnnPrecond::apply(const double *r, double *z, cudaStream_t st) {
     ++g_launches;
     SYSU_CUDA(cudaGetLastError());
     check_err(st);
+}
+
+void GnnPrecond::post_smooth(const float *r, const float *zp, float *z, FcgState *fs, const float *w, cudaStream_t st) {
+    if (!bound()) throw CaseError{"coarse-level network: no matrix bound"};
+    if (t_.size() < (size_t)n_) t_.alloc(n_);
+    k_lvl_resid<<<gflat_, FB, 0, st>>>(gview(*A_, val32_, dinv_.get()), r, zp, t_.get(), fs, part_.get());
+    ++g_launches;
+    forward(t_.get(), z, false, fs, nullptr, st, zp);
+    k_lvl_jacobi<<<gflat_, FB, 0, st>>>(n_, zp, w, t_.get(), z, fs);
+    ++g_launches;
+    SYSU_CUDA(cudaGetLastError());
+}
+
+void GnnPrecond::residual32(const double *b, const double *x1, float *r, cudaStream_t st) {
+    if (!bound()) throw CaseError{"learned preconditioner: no matrix bound"};
+    k_res32<<<gflat_, FB, 0, st>>>(gview(*A_, val32_, dinv_.get()), val64_, b, x1, r);
+    ++g_launches;
+    SYSU_CUDA(cudaGetLastError());
 }
 
 void GnnPrecond::apply_mg(const double *r, double *z, bool use_gnn, cudaStream_t st) {
@@ -1362,9 +1433,9 @@ void GnnPrecond::fcg_iteration(const void *args, bool use_gnn, cudaStream_t st) 
     const FcgArgs &a = *static_cast<const FcgArgs *>(args);
     if (mg_) {
         mg_->apply_to_fine(a.r, z2_.get(), &a.fs->done, st);
-        k_fcg_mgfine<<<gflat_, FB, 0, st>>>(a, z2_.get(), t_.get(), mg_->w0());
+        k_fcg_mgfine<<<gflat_, FB, 0, st>>>(a, z2_.get(), t_.get(), mg_->w0(), net_level == 0 ? 1 : 0);
         ++g_launches;
-        if (use_gnn) forward(t_.get(), a.z, false, a.fs, a.q, st, z2_.get());
+        if (use_gnn && net_level == 0) forward(t_.get(), a.z, false, a.fs, a.q, st, z2_.get());
     } else {
         if (use_gnn) forward(a.r, a.z, false, a.fs, a.q, st);
         k_fcg_jacobi<<<gflat_, FB, 0, st>>>(a);
@@ -1413,7 +1484,7 @@ void GnnPrecond::fcg(const double *b, double *x, bool x0_zero, const KrylovOpts 
     ChunkGraph &cg = graphs_[(mg_ ? 2 : 0) + (use_gnn ? 1 : 0)];
     if (!cg.exec || cg.inner_tol != o.inner_tol || cg.stall_max != stall_max || cg.chunk != check_every ||
         cg.val32 != val32_ || cg.dinv != dinv_.get() || cg.mg != mg_ ||
-        (mg_ && (cg.mg_gamma != mg_->gamma || cg.mg_persistent != mg_->persistent))) {
+        (mg_ && (cg.mg_gamma != mg_->gamma || cg.mg_persistent != mg_->persistent || cg.net_level != net_level))) {
         if (cg.exec) cudaGraphExecDestroy(cg.exec);
         cg.exec = nullptr;
         long before = g_launches.load();
@@ -1433,6 +1504,7 @@ void GnnPrecond::fcg(const double *b, double *x, bool x0_zero, const KrylovOpts 
         cg.mg = mg_;
         cg.mg_gamma = mg_ ? mg_->gamma : 0.0;
         cg.mg_persistent = mg_ ? mg_->persistent : false;
+        cg.net_level = net_level;
     }
     int done = 0;
     for (int it = 0; it < o.maxit && !done; it += check_every) {

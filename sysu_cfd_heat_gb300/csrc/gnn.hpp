@@ -10,8 +10,9 @@
 //   h0_i   = u_i e + c                                     encoder (e, c in R^32)
 //   m^l_i  = sum_{j != i} w_ij h^{l-1}_j                  aggregation over the row's neighbours
 //   h^l_i  = h^{l-1}_i + relu(W_l^T [h^{l-1}_i ; m^l_i] + b_l)     l = 1..4, W_l 64 x 32
-//   z_i    = s (u_i + w_d . h4_i + b_d)                    decoder (Jacobi plus a learned correction)
-// With w_d = b_d = 0 the network is exactly the Jacobi preconditioner.
+//   z_i    = s (k u_i + w_d . h4_i + b_d)                  decoder (Jacobi plus a learned correction)
+// With w_d = b_d = 0 the network is exactly the Jacobi preconditioner (k = 1),
+// or the weighted-Jacobi smoothing step of the multigrid cycle (k = omega).
 // Activations h, m are stored in BF16; the 64 x 32 dense products run as
 // tcgen05 MMAs (M = 128 rows per tile).
 //
@@ -81,6 +82,11 @@ class GnnPrecond {
     // device time of one network application (ms), averaged over reps
     double time_apply(const double *r, int reps, cudaStream_t st);
     int fwd_per_sm = 0;   // forward CTAs per SM (0: from registers and shared memory); applied at bind
+    // Weight of the Jacobi term in the decoder, z = s (skip u + w_d . h4 + b_d):
+    // 1 as a whole preconditioner; the smoother's omega as a multigrid
+    // post-smoother, so that the untrained network (zero decoder) is exactly the
+    // cycle's Jacobi post-smoothing step and training learns a correction to it.
+    float skip = 1.0f;
 
     // Training pairs: a ring of `capacity` FP32 pairs.
     void set_capacity(int pairs) { capacity_ = pairs; }
@@ -114,6 +120,18 @@ class GnnPrecond {
     // z = M(r) of the attached cycle once (FP64 device vectors): z2 + N(t) with
     // the network (use_gnn), z2 + w t (Jacobi) without.
     void apply_mg(const double *r, double *z, bool use_gnn, cudaStream_t st);
+    // Level of the attached cycle whose post-smoother the network is: 0 the
+    // finest (this handle's own network), >= 1 a coarse level, whose network is
+    // another handle bound to that level's matrix and called through the
+    // cycle's post_hook (this handle's finest post-smoothing is then Jacobi).
+    int net_level = 0;
+    // As the network of a coarse level (this handle bound to that level's
+    // matrix): z = zp + N(r - A zp) while fs->use_gnn, else the Jacobi step
+    // zp + w (r - A zp); fs is the finest-level flexible CG's state.
+    void post_smooth(const float *r, const float *zp, float *z, FcgState *fs, const float *w, cudaStream_t st);
+    FcgState *fcg_state() { return fs_.get(); }
+    // r = b - A x1 in FP32 (x1 == nullptr: r = b), FP64 device vectors in
+    void residual32(const double *b, const double *x1, float *r, cudaStream_t st);
 
     // Flexible CG (Notay's FCG(1)) with FP32 recurrences and FP64 reliable
     // updates, preconditioned by the network (use_gnn) or by Jacobi -- or by
@@ -148,6 +166,7 @@ class GnnPrecond {
         const AggMultigrid *mg = nullptr;
         double mg_gamma = 0.0;  // a kernel argument of the captured cycle
         bool mg_persistent = false;
+        int net_level = 0;
     };
     ChunkGraph graphs_[4];
     void drop_graphs();

@@ -477,19 +477,52 @@ void SimpleSolver::solve_learned(const EqOpts &o, const double *val, const doubl
     } else {
         gnn.refresh(st);
     }
+    int lvl = 0;  // level of the network in the multigrid form
     if (use_mg) {
         if (!mg.ready() || mg_theta_built != o.mg_theta) {
             gnn.attach_multigrid(nullptr);
             mg.setup(A, fd.pat, val, o.mg_theta, st);
             mg_theta_built = o.mg_theta;
+            learn_level_built = -1;
         }
         mg.omega = o.mg_omega;
         mg.gamma = o.mg_gamma;
         mg.persistent = o.mg_persistent != 0;  // part of the captured iterations' key
         mg.refresh(val, f.Ap32.get(), st);
+        if (o.learned) lvl = std::max(0, std::min(o.learn_level, mg.levels() - 2));
+        if (lvl >= 1) {
+            if (learn_level_built != lvl) {
+                gnn.attach_multigrid(nullptr);  // the captured iterations change
+                gnn_c.set_capacity(std::max(8, 2 * std::min(o.learn_iters, 32)));
+                gnn_c.bind(mg.level_matrix(lvl), mg.level_val64(lvl), mg.level_val32(lvl), st);
+                gnn_c.init_params(20261203ULL, st);
+                mg_c.omega = o.mg_omega;
+                mg_c.gamma = o.mg_gamma;
+                mg_c.setup(mg.level_matrix(lvl), mg.level_pattern(lvl), mg.level_val64(lvl), o.mg_theta, st);
+                learn_level_built = lvl;
+            }
+            gnn_c.loss_kind = o.learn_kind;
+            gnn_c.skip = (float)o.mg_omega;
+            mg_c.omega = o.mg_omega;
+            mg_c.gamma = o.mg_gamma;
+            mg_c.refresh(mg.level_val64(lvl), mg.level_val32(lvl), st);
+            gnn_c.refresh(st);
+            if (gnn_c.multigrid() != &mg_c) gnn_c.attach_multigrid(&mg_c);
+            mg.post_level = lvl;
+            mg.post_hook = [this](int l, const float *r, const float *zp, float *z, const int *, cudaStream_t s) {
+                gnn_c.post_smooth(r, zp, z, gnn.fcg_state(), mg.level_w(l), s);
+            };
+        } else {
+            mg.post_level = -1;
+            mg.post_hook = nullptr;
+        }
+        gnn.net_level = lvl;
+        gnn.skip = (float)o.mg_omega;  // the finest-level network as the cycle's post-smoother
         if (gnn.multigrid() != &mg) gnn.attach_multigrid(&mg);
-    } else if (gnn.multigrid()) {
-        gnn.attach_multigrid(nullptr);
+    } else {
+        if (gnn.multigrid()) gnn.attach_multigrid(nullptr);
+        gnn.net_level = 0;
+        gnn.skip = 1.0f;  // the network as the whole preconditioner
     }
     KrylovOpts ko;
     ko.maxit = o.maxit;
@@ -521,9 +554,58 @@ void SimpleSolver::solve_learned(const EqOpts &o, const double *val, const doubl
     plain(std::max(o.eps, 1e-2), x0_zero);
     SYSU_CUDA(cudaMemcpyAsync(gnn_x1.get(), x, sizeof(double) * A.n, cudaMemcpyDeviceToDevice, st));
     plain(o.eps, false);
+    if (lvl >= 1) {
+        // pairs of the coarse level: the right-hand side the cycle hands that level
+        // for the finest residuals b and b - A x1, and the level's own solution of
+        // it (flexible CG with the hierarchy below the level); add_pair turns them
+        // into post-smoother pairs of that level
+        const int nl = mg.level_rows(lvl);
+        if (mg_r32.size() < (size_t)A.n) mg_r32.alloc(A.n);
+        if (mg_rl32.size() < (size_t)nl) {
+            mg_rl32.alloc(nl);
+            mg_rl64.alloc(nl);
+            mg_el64.alloc(nl);
+        }
+        if (!mg_info.size()) mg_info.alloc(1);
+        KrylovOpts kl = ko;
+        kl.eps = 1e-6;
+        kl.maxit = 1000;
+        for (const double *x1 : {static_cast<const double *>(nullptr), static_cast<const double *>(gnn_x1.get())}) {
+            gnn.residual32(b, x1, mg_r32.get(), st);
+            mg.level_rhs(lvl, mg_r32.get(), mg_rl32.get(), st);
+            mg_to_f64(mg_rl32.get(), mg_rl64.get(), nl, st);
+            gnn_c.fcg(mg_rl64.get(), mg_el64.get(), true, kl, false, mg_info.get(), st);
+            gnn_c.add_pair(mg_rl64.get(), mg_el64.get(), st);
+        }
+        for (int k = 0; k < o.learn_steps; ++k) gnn_c.train_step(k % gnn_c.pairs(), o.learn_lr, st);
+        return;
+    }
     gnn.add_pair_from(b, nullptr, x, st);
     gnn.add_pair_from(b, gnn_x1.get(), x, st);
     for (int k = 0; k < o.learn_steps; ++k) gnn.train_step(k % gnn.pairs(), o.learn_lr, st);
+}
+
+void SimpleSolver::p_cycle(const double *r, double *z, bool use_net) {
+    if (!mg.ready() || gnn.multigrid() != &mg) throw CaseError{"p' multigrid: no p' solve with precond 4 yet"};
+    const int n = fd.A.n;
+    if (mg_r32.size() < (size_t)n) mg_r32.alloc(n);
+    DevBuf<double> d(n);
+    DevBuf<float> z32(n);
+    d.upload(r, n, st);
+    gnn.residual32(d.get(), nullptr, mg_r32.get(), st);
+    // the cycle's network kernels read the flexible CG's flags: running, network on or off
+    FcgState *fs = gnn.fcg_state();
+    const int flags[2] = {0, use_net ? 1 : 0};
+    SYSU_CUDA(cudaMemcpyAsync(&fs->done, &flags[0], sizeof(int), cudaMemcpyHostToDevice, st));
+    SYSU_CUDA(cudaMemcpyAsync(&fs->use_gnn, &flags[1], sizeof(int), cudaMemcpyHostToDevice, st));
+    if (gnn.net_level == 0 && use_net) {
+        gnn.apply_mg(d.get(), d.get(), true, st);
+    } else {
+        mg.apply(mg_r32.get(), z32.get(), &fs->done, st);
+        mg_to_f64(z32.get(), d.get(), n, st);
+    }
+    d.download(z, n, st);
+    SYSU_CUDA(cudaStreamSynchronize(st));
 }
 
 // CalculateVelocity + BuildVelocityMatrix, navier_velocity.cpp:12-357

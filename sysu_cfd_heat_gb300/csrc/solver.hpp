@@ -59,6 +59,9 @@ struct EqOpts {
     double mg_omega = 0.8;
     double mg_gamma = 1.8;
     int mg_persistent = 0;    // 1: the coarse levels as one persistent cooperative launch
+    // learned form with precond PK_AMG: the multigrid level whose post-smoother
+    // the network is (0 the finest; deeper than the last coarse level clamps)
+    int learn_level = 2;
 };
 
 struct SolverOptions {
@@ -144,6 +147,15 @@ class SimpleSolver {
     GnnPrecond gnn;             // learned p' preconditioner (option p.learned); flexible CG driver
     AggMultigrid mg;            // p' multigrid hierarchy (option p.precond 4)
     double mg_theta_built = 0.0;
+    // learned multigrid form with the network on a coarse level: the network
+    // bound to that level's matrix, the hierarchy below that level (for the
+    // level's own solves that give its training pairs), scratch
+    GnnPrecond gnn_c;
+    AggMultigrid mg_c;
+    int learn_level_built = -1;
+    DevBuf<float> mg_r32, mg_rl32;
+    DevBuf<double> mg_rl64, mg_el64;
+    DevBuf<SolveInfo> mg_info;
     int p_solves = 0;           // p' solves so far (training window of the learned form)
     DevBuf<double> gnn_x1;      // partial solution of a training solve
     DevBuf<double> io_stage;    // staging for reordered field transfers
@@ -192,6 +204,9 @@ class SimpleSolver {
     void sync();
     // back to the state after InitFlowField (fields, residuals, counters)
     void reset();
+    // One application of the p' multigrid cycle as the last p' solve left it
+    // (hierarchy, values, the network on its level when use_net), host vectors
+    void p_cycle(const double *r, double *z, bool use_net);
     // CUDA events on the solver's stream around a region of work
     void timer_start();
     double timer_stop();  // ms; synchronises
@@ -209,6 +224,7 @@ class SimpleSolver {
   private:
     void alloc_fields(FieldSet &fs, const DomainDev &d, bool solid);
     void solve_learned(const EqOpts &o, const double *val, const double *b, double *x, bool x0_zero, SolveInfo *info);
+
     void solve(int slot, const EqOpts &o, const SellDev &A, const double *val, int nrhs, const double *const *b,
                double *const *x, bool x0_zero);
     void grad_limited(DomainDev &d, FieldSet &fs, int nfield, const double *const *phi, const double *const *Bphi,

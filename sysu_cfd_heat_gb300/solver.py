@@ -197,6 +197,27 @@ class NavierStokesSolver:
         check(lib().sysu_solver_get_field(self._h, name.encode(), _dptr(out), n))
         return out
 
+    def p_cycle(self, r, use_net: bool = True) -> np.ndarray:
+        """One application of the p' multigrid cycle (option p.precond 4) as the
+        last p' solve left it, z = M r."""
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        z = np.zeros_like(r)
+        check(lib().sysu_solver_p_cycle(self._h, _dptr(r), _dptr(z), 1 if use_net else 0))
+        return z
+
+    def p_network(self):
+        """(level, parameters) of the p' network: level 0 the finest, >= 1 a
+        coarse level of the multigrid cycle."""
+        lvl = C.c_int()
+        n = lib().sysu_gnn_num_params()
+        prm = np.zeros(n, np.float32)
+        check(lib().sysu_solver_p_network(self._h, C.byref(lvl), prm.ctypes.data_as(C.POINTER(C.c_float)), n))
+        return lvl.value, prm
+
+    def p_set_network(self, params) -> None:
+        prm = np.ascontiguousarray(params, dtype=np.float32)
+        check(lib().sysu_solver_p_set_network(self._h, prm.ctypes.data_as(C.POINTER(C.c_float)), len(prm)))
+
     def set(self, name: str, values) -> None:
         a = np.ascontiguousarray(values, dtype=np.float64).ravel()
         check(lib().sysu_solver_set_field(self._h, name.encode(), _dptr(a), a.size))

@@ -11,7 +11,9 @@
 * the learned form: the network trained on the solver's own pairs (turned into
   post-smoother pairs) needs fewer iterations than the same cycle with the
   untrained network, and a useless network falls back to the Jacobi
-  post-smoother and still converges.
+  post-smoother and still converges -- with the network at the finest level
+  (CSR handle) and on a coarse level of the SIMPLE p' solve (option
+  p.learn_level), where the untrained network is exactly the plain cycle.
 """
 import os
 import sys
@@ -184,3 +186,82 @@ def test_useless_network_falls_back_to_the_jacobi_post_smoother():
     A = sp.csr_matrix((vl, cl, rp), shape=(n, n))
     assert np.linalg.norm(b - A @ x) / np.linalg.norm(b) < 1e-8
     assert plain["fallback_at"] == -1 and plain["status"] == 0
+
+
+def _learned_cavity(tmp, level, learn_iters=6, steps=64):
+    p = mg.write_case(tmp, mg.lid_cavity_tet(18, 18, 12, jitter=0.2, seed=5), mg.cavity_param("x", 100, mu=0.0025))
+    s = NavierStokesSolver(p, {"rtc": 1e-8, "p.maxit": 100000, "p.precond": 4, "p.learned": 1, "p.learn_level": level,
+                               "p.learn_iters": learn_iters, "p.learn_steps": steps})
+    return s
+
+
+@pytest.mark.parametrize("level", [1, 2])
+def test_coarse_level_network_cycle_matches_oracle(level):
+    with tempfile.TemporaryDirectory() as tmp:
+        with _learned_cavity(tmp, level, learn_iters=1, steps=8) as s:
+            s.iterate(2)
+            lvl, prm = s.p_network()
+            assert lvl == level
+            rng = np.random.default_rng(6)
+            prm = prm.copy()
+            prm[G.OFF_DEC:G.OFF_DEC + 33] = rng.uniform(-0.3, 0.3, 33)  # make the network's part visible
+            s.p_set_network(prm)
+            rp, cl, vl = s.matrix("p")
+            r = rng.standard_normal(len(rp) - 1)
+            r -= r.mean()
+            z = s.p_cycle(r, use_net=True)
+            zj = s.p_cycle(r, use_net=False)
+    lv = amg_np.hierarchy(rp, cl, vl, dense_max=DENSE_MAX)
+    L = lv[level]
+    g = G.Graph(L.rp, L.col, L.val)
+
+    def post(rl, zp):
+        zn, _ = G.forward(prm, g, rl - L.matvec(zp), exact=False, skip=0.8)
+        return zp + zn
+    zo = amg_np.vcycle(lv, r, post={level: post})
+    assert _rel(zj, amg_np.vcycle(lv, r)) < 5e-5
+    assert _rel(z, zo) < 5e-3, _rel(z, zo)
+    assert _rel(z, zj) > 1e-3  # the network did change the cycle
+
+
+def test_coarse_level_network_gains_over_the_plain_cycle():
+    """Trained during the first outer iterations (pairs: the right-hand sides the
+    cycle hands the network's level, solved on that level), the network cuts the
+    p' iterations below the plain cycle's from the same state; with its zero
+    decoder the untrained network is the plain cycle."""
+    fields = ("U", "V", "W", "P", "RUFace")
+    with tempfile.TemporaryDirectory() as tmp:
+        with _learned_cavity(tmp, 1) as s:
+            assert s.iterate(6) == 6
+            state = {f: s.get(f) for f in fields}
+            its = {}
+            for name, opts in (("plain", {"p.learned": 0}), ("trained", {"p.learned": 1}),
+                               ("untrained", {"p.learned": 1, "p.learn_reset": 1, "p.learn_iters": 0})):
+                for k, v in opts.items():
+                    s.set_option(k, v)
+                for f, a in state.items():
+                    s.set(f, a)
+                s.CalculateVelocity()
+                s.CalculatePressure()
+                s.check()
+                st = s.solve_stats()["p"]
+                assert st["status"][0] == 0 and st["res"][0] < 1e-8, (name, st)
+                its[name] = st["iters"][0]
+    assert abs(its["untrained"] - its["plain"]) <= 1, its
+    assert its["trained"] < its["plain"], its
+    print("p' iterations from the same state:", its)
+
+
+def test_useless_coarse_level_network_still_converges():
+    with tempfile.TemporaryDirectory() as tmp:
+        with _learned_cavity(tmp, 1, learn_iters=1, steps=4) as s:
+            s.iterate(2)
+            _, prm = s.p_network()
+            prm = prm.copy()
+            prm[G.OFF_DEC:G.OFF_DEC + 33] = np.random.default_rng(0).uniform(-50, 50, 33)
+            s.p_set_network(prm)
+            s.CalculateVelocity()
+            s.CalculatePressure()
+            s.check()
+            st = s.solve_stats()["p"]
+    assert st["status"][0] == 0 and st["res"][0] < 1e-8, st
