@@ -508,12 +508,29 @@ P_FORMS = (
     ("mixed_fp32_fp64", {"p.mixed": 1}, "Jacobi-CG, FP32 recurrences + FP64 reliable updates"),
     ("multigrid_fp32_fp64", {"p.precond": 4},
      "flexible CG, FP32 recurrences + FP64 reliable updates, aggregation-multigrid V-cycle"),
-    ("learned_multigrid_fp32_fp64", {"p.precond": 4, "p.learned": 1},
-     "as multigrid_fp32_fp64 with the trained message-passing network as the finest post-smoother"),
+    ("learned_multigrid_fp32_fp64", {"p.precond": 4, "p.learned": 1, "p.learn_level": 2},
+     "as multigrid_fp32_fp64 with the trained message-passing network as the post-smoother of the cycle's "
+     "second coarse level"),
+    ("learned_multigrid_level1_fp32_fp64", {"p.precond": 4, "p.learned": 1, "p.learn_level": 1},
+     "the same with the network on the first coarse level"),
+    ("learned_multigrid_level0_fp32_fp64", {"p.precond": 4, "p.learned": 1, "p.learn_level": 0},
+     "the same with the network as the finest level's post-smoother"),
     ("learned_network_fp32_fp64", {"p.learned": 1},
      "flexible CG, FP32 recurrences + FP64 reliable updates, the trained network as the whole preconditioner"),
 )
-P_OPTION_DEFAULTS = {"p.mixed": 0, "p.learned": 0, "p.precond": 1}
+P_OPTION_DEFAULTS = {"p.mixed": 0, "p.learned": 0, "p.precond": 1, "p.learn_level": 2}
+
+
+def pair_text(opts) -> str:
+    """How a learned form's training pairs are made."""
+    if not opts.get("p.precond"):
+        return "(b, x*) and (b - A x1, x* - x1) per p' solve, x1 = solve to 1e-2"
+    if opts.get("p.learn_level", 2) == 0:
+        return ("(b, x*) and (b - A x1, x* - x1) per p' solve, x1 = solve to 1e-2, as post-smoother pairs "
+                "(r - A z2, e - z2) of the finest level")
+    return ("per p' solve, the right-hand sides r_l the cycle hands the network's level for the finest residuals "
+            "b and b - A x1 (x1 = solve to 1e-2), their solutions e_l on that level (flexible CG with the "
+            "hierarchy below it, to 1e-6), as post-smoother pairs (r_l - A_l z_l, e_l - z_l) of that level")
 
 
 def matched_forms(s, args, n, nnz, hbm):
@@ -541,8 +558,7 @@ def matched_forms(s, args, n, nnz, hbm):
             s.sync()
             entry["training"] = {"outer_iterations": LEARN_ITERS, "adam_steps_per_iteration": LEARN_STEPS,
                                  "seconds_incl_plain_solves": time.perf_counter() - t0,
-                                 "pairs": "(b, x*) and (b - A x1, x* - x1) per p' solve, x1 = solve to 1e-2"
-                                          + (", as post-smoother pairs (r - A z2, e - z2)" if opts.get("p.precond") else ""),
+                                 "pairs": pair_text(opts),
                                  "loss": "residual norm ||A(z - e)||^2 / ||A e||^2"}
         else:
             s.reset()

@@ -338,7 +338,9 @@ int sysu_gnn_fcg(sysu_gnn *g, const double *b, double *x, int x0_zero, int maxit
  * aggregation-multigrid hierarchy of the handle's matrix (strength theta,
  * smoother weight omega, coarse-correction scale gamma) and attaches it: from
  * then on sysu_gnn_fcg is preconditioned by the V-cycle whose finest
- * post-smoothing step is the network (use_gnn = 1) or Jacobi (use_gnn = 0),
+ * post-smoothing step is the network (use_gnn = 1) or Jacobi (use_gnn = 0);
+ * the network's decoder then weighs its Jacobi term by omega, so a network
+ * with a zero decoder is exactly the Jacobi step, and
  * sysu_gnn_set_values refreshes its coarse levels, and pairs added with
  * sysu_gnn_add_pair become pairs of the post-smoother,
  * (r, e) -> (r - A z2(r), e - z2(r)) with z2 the cycle before post-smoothing.

@@ -218,7 +218,9 @@ int sysu_gnn_set_multigrid(sysu_gnn *g, int on, double theta, double omega, doub
     }
     return guarded([&] {
         g->net.attach_multigrid(nullptr);
+        g->net.skip = 1.0f;  // the network as the whole preconditioner
         if (!on) return;
+        g->net.skip = (float)omega;  // the cycle's post-smoother: zero decoder = its Jacobi step
         g->mg.omega = omega;
         g->mg.gamma = gamma;
         g->mg.setup(g->M.A, g->M.pat, g->M.val.get(), theta, g->st);
