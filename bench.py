@@ -264,9 +264,9 @@ def spmv_bytes(n: int, nnz: int, sv: int) -> float:
 def spmv_sweep(s, n: int, nnz: int, hbm: float, at=(1, 10, 100), reps: int = 10) -> dict:
     """y = A x on the p' and momentum matrices as assembled after the given outer
     iterations (FP64 values and their FP32 copy), L2 flushed before each product,
-    by three kernel forms: one row per thread over a full grid (the top-level
-    figures), the persistent bulk-copy ring (`ring`) and the per-warp cp.async
-    pipeline (`async`)."""
+    by four kernel forms: one row per thread over a full grid (the top-level
+    figures), the persistent bulk-copy ring (`ring`), the per-warp cp.async
+    pipeline (`async`) and x staged in shared memory per block (`staged_x`)."""
     out = {}
     s.reset()
     done = 0
@@ -278,7 +278,7 @@ def spmv_sweep(s, n: int, nnz: int, hbm: float, at=(1, 10, 100), reps: int = 10)
             for fp32 in (False, True):
                 b = spmv_bytes(n, nnz, 4 if fp32 else 8)
                 res = {}
-                for name, variant in (("stream", 0), ("ring", 100), ("async", 200)):
+                for name, variant in (("stream", 0), ("ring", 100), ("async", 200), ("staged_x", 300)):
                     s.set_option("spmv_variant", variant)
                     ms = s.spmv_timing(which, fp32, reps)
                     gbs = b / (ms / 1000.0) / 1e9
@@ -288,6 +288,7 @@ def spmv_sweep(s, n: int, nnz: int, hbm: float, at=(1, 10, 100), reps: int = 10)
                 entry["algorithmic_bytes"] = b
                 entry["ring"] = res["ring"]
                 entry["async"] = res["async"]
+                entry["staged_x"] = res["staged_x"]
                 row[f"{which}_{'fp32' if fp32 else 'fp64'}"] = entry
         out[f"after_outer_iteration_{k}"] = row
     return out

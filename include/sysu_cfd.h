@@ -209,7 +209,9 @@ int sysu_csr_spmv(int n, const int *rowptr, const int *col, const double *val, c
  * sysu_solver_spmv_timing), process-wide: 0 one row per thread over a full
  * grid (default), 100 persistent ring (matrix streamed through shared memory
  * by bulk copies, one CTA per SM), 200 per-warp cp.async pipeline staging the
- * next slices in shared memory, 10 b + s the persistent grid with s slices
+ * next slices in shared memory, 300 x staged in shared memory per block of 256
+ * rows (the rows' window plus a 96-row halo; other columns read from global
+ * memory), 10 b + s the persistent grid with s slices
  * per warp step and b blocks per SM.  All forms give bit-identical y. */
 int sysu_set_spmv_variant(int variant);
 /* Three systems sharing one sparsity pattern (rowptr, col), values vals[c],

@@ -132,8 +132,9 @@ int sysu_csr_solve(int method, int precond, int n, const int *rowptr, const int 
 }
 
 int sysu_set_spmv_variant(int variant) {
-    if (variant != 0 && variant != sysu::SPMV_RING && variant != sysu::SPMV_ASYNC && !(variant >= 11 && variant <= 99 && (variant % 10 == 1 || variant % 10 == 2 || variant % 10 == 4))) {
-        g_csr_err = "sysu_set_spmv_variant: 0, 100, 200 or 10 b + s with s in {1, 2, 4}";
+    if (variant != 0 && variant != sysu::SPMV_RING && variant != sysu::SPMV_ASYNC && variant != sysu::SPMV_STAGE &&
+        !(variant >= 11 && variant <= 99 && (variant % 10 == 1 || variant % 10 == 2 || variant % 10 == 4))) {
+        g_csr_err = "sysu_set_spmv_variant: 0, 100, 200, 300 or 10 b + s with s in {1, 2, 4}";
         return SYSU_ERR_INPUT;
     }
     sysu::set_spmv_variant(variant);

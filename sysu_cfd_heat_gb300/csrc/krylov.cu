@@ -203,6 +203,43 @@ __global__ void __launch_bounds__(256) k_spmv_stream(int n, const int *__restric
     y[i] = acc;
 }
 
+// The same product with x staged in shared memory: block b (rows r0 .. r0+255)
+// first loads x[r0 - SPMV_HALO, r0 + 256 + SPMV_HALO) with coalesced loads, and
+// every column inside that window is read from there, the rest from global
+// memory.  On the tet and hex meshes most of a row's neighbours lie within a few
+// rows of it (the cells of one hex, the next hex along x), so about half of the
+// gathers become shared-memory reads of a tile fetched in one stream.  Same FMA
+// order as k_spmv_stream: the same bits.
+constexpr int SPMV_HALO = 96;
+template <class V>
+__global__ void __launch_bounds__(256) k_spmv_stage(int n, const int *__restrict__ sl_ptr,
+                                                    const int *__restrict__ sl_w, const int *__restrict__ col,
+                                                    const V *__restrict__ val, const V *__restrict__ x,
+                                                    V *__restrict__ y) {
+    __shared__ V xs[256 + 2 * SPMV_HALO];
+    const int r0 = blockIdx.x * 256;
+    const int lo = r0 - SPMV_HALO;
+    for (int q = threadIdx.x; q < 256 + 2 * SPMV_HALO; q += 256) {
+        const int j = lo + q;
+        xs[q] = (j >= 0 && j < n) ? __ldg(x + j) : (V)0;
+    }
+    __syncthreads();
+    const int i = r0 + threadIdx.x;
+    if (i >= n) return;
+    const int s = i >> 5;
+    const int e = __ldg(sl_ptr + s) + (i & 31);
+    const int w = __ldg(sl_w + s);
+    V acc = (V)0;
+    for (int k = 0; k < w; ++k) {
+        const int c = __ldcs(col + e + 32 * k);
+        const V a = __ldcs(val + e + 32 * k);
+        const unsigned q = (unsigned)(c - lo);
+        const V xv = q < (unsigned)(256 + 2 * SPMV_HALO) ? xs[q] : __ldg(x + c);
+        acc = fma(a, xv, acc);
+    }
+    y[i] = acc;
+}
+
 // The same product with a persistent grid: each warp takes SPW slices at a time
 // (slices s, s + W, ... for W warps in the grid), so every thread has SPW rows'
 // matrix entries in flight before its first gather.
@@ -936,6 +973,8 @@ static void spmv_dispatch(const SellDev &A, const V *val, const V *x, V *y, cuda
         }
         const int G = std::max(1, std::min((A.nslices + SPMV_AT / 32 - 1) / (SPMV_AT / 32), num_sms() * ps));
         k_spmv_async<V><<<G, SPMV_AT, sm, st>>>(A.n, A.nslices, A.sl_ptr.get(), A.sl_w.get(), A.col.get(), val, x, y);
+    } else if (v == SPMV_STAGE) {
+        k_spmv_stage<V><<<(A.n + 255) / 256, 256, 0, st>>>(A.n, A.sl_ptr.get(), A.sl_w.get(), A.col.get(), val, x, y);
     } else if (v == 0 || v == SPMV_RING) {
         k_spmv_stream<V><<<(A.n + 255) / 256, 256, 0, st>>>(A.n, A.sl_ptr.get(), A.sl_w.get(), A.col.get(), val, x, y);
     } else {

@@ -166,6 +166,7 @@ void set_spmv_variant(int v);
 int spmv_variant();
 constexpr int SPMV_RING = 100;   // spmv_variant value that selects spmv_ring in the sweep
 constexpr int SPMV_ASYNC = 200;  // per-warp cp.async pipeline (spmv_stream / spmv_stream32)
+constexpr int SPMV_STAGE = 300;  // x staged in shared memory per block of rows (spmv_stream / spmv_stream32)
 // y = A x by a persistent kernel that streams the matrix through a shared-memory
 // ring with bulk copies (one CTA per SM; cg.cu).  *err (device) is set if a
 // bounded wait in the ring gave up.  val and the column indices 16-byte aligned.

@@ -60,12 +60,16 @@ def test_ring_matches_stream(n, wmin, wmax, wide):
     set_spmv_variant(200)
     y2 = csr_spmv(rowptr, col, val, x)
     assert np.array_equal(y0, y2)
+    set_spmv_variant(300)
+    y3 = csr_spmv(rowptr, col, val, x)
+    set_spmv_variant(0)
+    assert np.array_equal(y0, y3)
     if n <= 20000:
         ref = _numpy_spmv(rowptr, col, val, x)
         np.testing.assert_allclose(y1, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
 
 
-@pytest.mark.parametrize("variant", [100, 200])
+@pytest.mark.parametrize("variant", [100, 200, 300])
 def test_single_row_and_empty(variant):
     set_spmv_variant(variant)
     y = csr_spmv(np.array([0, 1], np.int32), np.array([0], np.int32), np.array([2.5]), np.array([4.0]))
