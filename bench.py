@@ -481,10 +481,17 @@ def c5_learned_run(args):
                 s.iterate(LEARN_C5_MG)
                 s.sync()
                 out["training_multigrid_s"] = time.perf_counter() - t0
-            for f, a in state.items():
-                s.set(f, a)
             for k, v in opts.items():
                 s.set_option(k, v)
+            if name == "multigrid_fcg":
+                # hierarchy set-up and graph capture at the first multigrid solve (the
+                # learned multigrid form's happen in its training): not timed
+                for f, a in state.items():
+                    s.set(f, a)
+                s.CalculateVelocity()
+                s.CalculatePressure()
+            for f, a in state.items():
+                s.set(f, a)
             s.CalculateVelocity()
             s.CalculatePressure()
             s.check()
@@ -652,6 +659,29 @@ def cpu_survey(args) -> dict:
                                "as_shipped_g_iters_per_s": (1.0 / itg[0]) if itg else None,
                                "as_shipped_g": recg, "error": err or errg}
     return out
+
+
+def probe_p(args) -> dict:
+    """--probe-p FORM (profiling runs, not part of the default run): on the C3 case,
+    one outer iteration of the given p' form (after LEARN_ITERS training outer
+    iterations for a learned form), then the momentum and p' solves of the next
+    outer iteration once more; prints the p' solve's time and iterations.  The ncu
+    summaries under profiles/ were captured from these runs."""
+    from sysu_cfd_heat_gb300.solver import NavierStokesSolver
+
+    forms = {name: opts for name, opts, _ in P_FORMS}
+    opts = dict(forms[args.probe_p])
+    with NavierStokesSolver(case_dir(args.workload), dict({"rtc": RTC, "timing": 1, "p.maxit": 100000}, **opts)) as s:
+        if opts.get("p.learned"):
+            s.set_option("p.learn_iters", LEARN_ITERS)
+            s.set_option("p.learn_steps", LEARN_STEPS)
+            s.iterate(LEARN_ITERS)
+        s.iterate(1)
+        s.CalculateVelocity()
+        s.CalculatePressure()
+        s.check()
+        st = s.solve_stats()["p"]
+        return {"form": args.probe_p, "p_ms": s.timing()[0], "p_iters": st["iters"][0], "p_status": st["status"][0]}
 
 
 def max_over_ranks(x: float, w: int) -> float:
@@ -848,6 +878,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the 48-cavity batch form")
     ap.add_argument("--learned-c5", action="store_true",
                     help="only the configuration-5 learned-preconditioner run (4.9 M cells; minutes)")
+    ap.add_argument("--probe-p", default=None, choices=[f for f, _, _ in P_FORMS],
+                    help="only one p' solve of the given form after its set-up (profiling runs)")
     ap.add_argument("--cpu-survey", action="store_true",
                     help="only the CPU baseline of configurations 1-3 next to the GPU (minutes of CPU time)")
     ap.add_argument("--cpu-budget", type=float, default=60.0,
@@ -865,7 +897,10 @@ def main():
         import torch.distributed as dist
 
         dist.init_process_group("gloo")
-    if args.cpu_survey:
+    if args.probe_p:
+        if r == 0:
+            print(json.dumps({"probe_p": probe_p(args)}))
+    elif args.cpu_survey:
         if r == 0:
             print(json.dumps({"cpu_survey": cpu_survey(args)}))
     elif args.learned_c5:
