@@ -229,8 +229,6 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
             if (f == "maxit") { e->maxit = (int)value; return SYSU_OK; }
             if (f == "omega") { e->omega = value; return SYSU_OK; }
             if (f == "mixed") {
-                if (value != 0.0 && e == &o.mom)
-                    return set_err(SYSU_ERR_INPUT, "mixed precision is available for p, ke, t and ts (not momentum)");
                 if (value != 0.0 && e->kind == sysu::SK_GMRES)
                     return set_err(SYSU_ERR_INPUT, "mixed precision is available for CG and BiCGSTAB solves");
                 if (value != 0.0 && e->kind == sysu::SK_CG && e->precond != sysu::PK_JACOBI && e->precond != sysu::PK_AMG)

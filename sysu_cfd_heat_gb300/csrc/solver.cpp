@@ -442,9 +442,14 @@ void SimpleSolver::solve(int slot, const EqOpts &o, const SellDev &A, const doub
     if (x0_zero)
         for (int c = 0; c < nrhs; ++c) launch_fill(x[c], 0.0, A.n, st);
     if (o.mixed) {
-        if (nrhs != 1) throw CaseError{"mixed-precision BiCGSTAB solves one right-hand side"};
         ko.inner_tol = o.inner_tol;
-        bicgstab_solve_mixed(A, val, b[0], x[0], ko, kw, info, st);
+        if (nrhs == 1) {
+            bicgstab_solve_mixed(A, val, b[0], x[0], ko, kw, info, st);
+            return;
+        }
+        // momentum: u, v, w one after another, each with FP32 inner iterations in
+        // FP64 defect correction (statistics per component, as the unbatched form)
+        for (int c = 0; c < nrhs; ++c) bicgstab_solve_mixed(A, val, b[c], x[c], ko, kw, infos.get() + SLOT_N + c, st);
         return;
     }
     if (nrhs == 3 && !opt.mom_batched) {
@@ -949,7 +954,7 @@ std::string SimpleSolver::check_iteration() {
     red_out.download(ro, RED_NSLOT, st);
     flags.download(&hf, 1, st);
     SYSU_CUDA(cudaStreamSynchronize(st));
-    if (!opt.mom_batched || opt.mom.kind == SK_GMRES)
+    if (!opt.mom_batched || opt.mom.kind == SK_GMRES || opt.mom.mixed)
         for (int c = 0; c < 3; ++c) {
             h[SLOT_MOM].status[c] = h[SLOT_N + c].status[0];
             h[SLOT_MOM].iters[c] = h[SLOT_N + c].iters[0];

@@ -129,3 +129,26 @@ def test_mixed_option_rules():
             s.set_option("scalars_batched", 1)
             with pytest.raises(SysuError):
                 s.set_option("t.mixed", 1)
+
+
+def test_momentum_mixed_reaches_the_fp64_fields():
+    """Option mom.mixed: u, v and w each by BiCGSTAB with FP32 inner iterations in
+    FP64 defect correction; solved to a tight tolerance, the SIMPLE fields equal the
+    FP64 form's."""
+    import tempfile
+
+    from sysu_cfd_heat_gb300 import meshgen as mg
+    from sysu_cfd_heat_gb300.solver import NavierStokesSolver
+
+    with tempfile.TemporaryDirectory() as tmp:
+        p = mg.write_case(tmp, mg.lid_cavity_tet(8, 8, 6, jitter=0.2), mg.cavity_param("x", 20, mu=0.0025))
+        out = {}
+        for name, opts in (("fp64", {}), ("mixed", {"mom.mixed": 1, "p.mixed": 1})):
+            with NavierStokesSolver(p, dict({"rtc": 1e-11}, **opts)) as s:
+                assert s.iterate(15) == 15
+                st = s.solve_stats()["mom"]
+                assert all(v == 0 for v in st["status"]), st
+                out[name] = {f: s.get(f) for f in ("U", "V", "W", "P")}
+    for f, a in out["mixed"].items():
+        r = out["fp64"][f]
+        assert np.linalg.norm(a - r) / np.linalg.norm(r) < 1e-8, f
