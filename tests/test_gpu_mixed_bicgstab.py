@@ -120,8 +120,12 @@ def test_mixed_option_rules():
     with tempfile.TemporaryDirectory() as d:
         p = mg.write_case(d, mg.cht_channel(8, 4, 2, 3), mg.cht_param("x", 2, turb=True))
         with NavierStokesSolver(p, {}) as s:
+            s.set_option("mom.mixed", 1)  # BiCGSTAB momentum: allowed
+            s.set_option("mom.mixed", 0)
+            s.set_option("mom.kind", 2)   # GMRES has no mixed form
             with pytest.raises(SysuError):
                 s.set_option("mom.mixed", 1)
+            s.set_option("mom.kind", 1)
             s.set_option("ke.mixed", 1)
             with pytest.raises(SysuError):
                 s.set_option("scalars_batched", 1)
