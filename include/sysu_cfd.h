@@ -214,6 +214,11 @@ int sysu_csr_spmv(int n, const int *rowptr, const int *col, const double *val, c
  * memory), 10 b + s the persistent grid with s slices
  * per warp step and b blocks per SM.  All forms give bit-identical y. */
 int sysu_set_spmv_variant(int variant);
+/* Mean device ms of one y = A x of a host CSR matrix by the current kernel form
+ * (FP64 values, or their FP32 copy when fp32), L2 flushed before each of `reps`
+ * timed products (the procedure of the solver's SpMV sweep). */
+int sysu_csr_spmv_timing(int n, const int *rowptr, const int *col, const double *val, int fp32, int reps,
+                         double *ms);
 /* Three systems sharing one sparsity pattern (rowptr, col), values vals[c],
  * right-hand sides b[c], x[c] (x0 in, solution out), solved by one batched
  * BiCGSTAB + Jacobi launch (the k, eps, T form of option "scalars_batched"). */

@@ -171,6 +171,58 @@ int sysu_csr_spmv(int n, const int *rowptr, const int *col, const double *val, c
     }
 }
 
+// Mean device ms of y = A x for a host CSR matrix (SELL-32 on the device) by the
+// current standalone kernel form, the L2 flushed (256 MB read) before each of
+// `reps` timed products; the same procedure as the solver's SpMV sweep.
+int sysu_csr_spmv_timing(int n, const int *rowptr, const int *col, const double *val, int fp32, int reps,
+                         double *ms) {
+    try {
+        if (n < 1 || !rowptr || !col || !val || !ms) throw ArgError{"n >= 1 and non-null arrays required"};
+        if (reps < 1) reps = 1;
+        OwnedStream os;
+        cudaStream_t st = os.st;
+        {
+            sysu::CsrDevice M;
+            M.load(n, rowptr, col, val, st);
+            sysu::DevBuf<double> x64(n), y64(n);
+            sysu::DevBuf<float> x32(n), y32(n), v32;
+            sysu::DevBuf<unsigned char> flush((size_t)256 << 20);
+            sysu::DevBuf<unsigned> sink(1);
+            SYSU_CUDA(cudaMemsetAsync(flush.get(), 1, flush.size(), st));
+            sysu::fill_sweep_x(n, x64.get(), x32.get(), st);
+            if (fp32) {
+                v32.alloc((size_t)M.A.nnz);
+                sysu::sell_to_fp32(M.A, M.val.get(), v32.get(), st);
+            }
+            cudaEvent_t e0, e1;
+            SYSU_CUDA(cudaEventCreate(&e0));
+            SYSU_CUDA(cudaEventCreate(&e1));
+            double total = 0.0;
+            for (int k = 0; k < reps + 1; ++k) {
+                sysu::l2_flush_read(flush.get(), flush.size(), sink.get(), st);
+                SYSU_CUDA(cudaEventRecord(e0, st));
+                if (fp32) sysu::spmv_stream32(M.A, v32.get(), x32.get(), y32.get(), st);
+                else sysu::spmv_stream(M.A, M.val.get(), x64.get(), y64.get(), st);
+                SYSU_CUDA(cudaEventRecord(e1, st));
+                SYSU_CUDA(cudaEventSynchronize(e1));
+                float t = 0.f;
+                SYSU_CUDA(cudaEventElapsedTime(&t, e0, e1));
+                if (k > 0) total += t;  // the first product warms up
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            *ms = total / reps;
+        }
+        return SYSU_OK;
+    } catch (const ArgError &e) {
+        g_csr_err = e.msg;
+        return SYSU_ERR_INPUT;
+    } catch (const sysu::CaseError &e) {
+        g_csr_err = e.msg;
+        return SYSU_ERR_CUDA;
+    }
+}
+
 // Three systems with one sparsity pattern (rowptr, col) and their own values,
 // solved by one batched BiCGSTAB + Jacobi launch.
 int sysu_csr_bicgstab_batched3(int n, const int *rowptr, const int *col, const double *const *vals,

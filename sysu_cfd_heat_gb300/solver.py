@@ -267,6 +267,22 @@ def csr_solve(rowptr, col, val, b, x0=None, method: str = "CG", precond: str = "
     return x, it.value, rs.value, stt.value
 
 
+def csr_spmv_timing(rowptr, col, val, fp32: bool = False, reps: int = 10) -> float:
+    """Mean device ms of one y = A x (L2 flushed before each) for a host CSR matrix."""
+    L = lib()
+    ip = C.POINTER(C.c_int)
+    rowptr = np.ascontiguousarray(rowptr, np.int32)
+    col = np.ascontiguousarray(col, np.int32)
+    val = np.ascontiguousarray(val, np.float64)
+    ms = C.c_double()
+    code = L.sysu_csr_spmv_timing(len(rowptr) - 1, rowptr.ctypes.data_as(ip), col.ctypes.data_as(ip), _dptr(val),
+                                  1 if fp32 else 0, int(reps), C.byref(ms))
+    if code != 0:
+        L.sysu_csr_last_error.restype = C.c_char_p
+        raise SysuError(code, L.sysu_csr_last_error().decode())
+    return ms.value
+
+
 def set_spmv_variant(variant: int) -> None:
     """Kernel form of the standalone SpMV (csr_spmv, spmv_timing), process-wide:
     0 one row per thread (default), 100 persistent ring with bulk copies."""
