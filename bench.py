@@ -531,22 +531,28 @@ def c5_learned_run(args):
 # The forms of the p' solve timed side by side at a matched residual: every form
 # starts from the same initial state and runs the same outer iterations with p'
 # solved to the 1e-8 relative residual (no iteration cap).
+# every form but the first runs its Krylov solves with FP32 recurrences: p' as
+# named, momentum (u, v, w together) by BiCGSTAB with FP64 residual replacement
+MOM32 = {"mom.mixed": 1}
+MOM32_TEXT = "; momentum u, v, w by one BiCGSTAB with FP32 recurrences + FP64 residual replacement"
 P_FORMS = (
-    ("fp64", {}, "Jacobi-CG, FP64 (the drop-in's method without the reference's 1000-iteration cap)"),
-    ("mixed_fp32_fp64", {"p.mixed": 1}, "Jacobi-CG, FP32 recurrences + FP64 reliable updates"),
-    ("multigrid_fp32_fp64", {"p.precond": 4},
-     "flexible CG, FP32 recurrences + FP64 reliable updates, aggregation-multigrid V-cycle"),
-    ("learned_multigrid_fp32_fp64", {"p.precond": 4, "p.learned": 1, "p.learn_level": 2},
+    ("fp64", {}, "Jacobi-CG, FP64 (the drop-in's method without the reference's 1000-iteration cap); "
+                 "momentum by the FP64 3-RHS BiCGSTAB"),
+    ("mixed_fp32_fp64", {"p.mixed": 1, **MOM32}, "Jacobi-CG, FP32 recurrences + FP64 reliable updates" + MOM32_TEXT),
+    ("multigrid_fp32_fp64", {"p.precond": 4, **MOM32},
+     "flexible CG, FP32 recurrences + FP64 reliable updates, aggregation-multigrid V-cycle" + MOM32_TEXT),
+    ("learned_multigrid_fp32_fp64", {"p.precond": 4, "p.learned": 1, "p.learn_level": 2, **MOM32},
      "as multigrid_fp32_fp64 with the trained message-passing network as the post-smoother of the cycle's "
      "second coarse level"),
-    ("learned_multigrid_level1_fp32_fp64", {"p.precond": 4, "p.learned": 1, "p.learn_level": 1},
+    ("learned_multigrid_level1_fp32_fp64", {"p.precond": 4, "p.learned": 1, "p.learn_level": 1, **MOM32},
      "the same with the network on the first coarse level"),
-    ("learned_multigrid_level0_fp32_fp64", {"p.precond": 4, "p.learned": 1, "p.learn_level": 0},
+    ("learned_multigrid_level0_fp32_fp64", {"p.precond": 4, "p.learned": 1, "p.learn_level": 0, **MOM32},
      "the same with the network as the finest level's post-smoother"),
-    ("learned_network_fp32_fp64", {"p.learned": 1},
-     "flexible CG, FP32 recurrences + FP64 reliable updates, the trained network as the whole preconditioner"),
+    ("learned_network_fp32_fp64", {"p.learned": 1, **MOM32},
+     "flexible CG, FP32 recurrences + FP64 reliable updates, the trained network as the whole preconditioner"
+     + MOM32_TEXT),
 )
-P_OPTION_DEFAULTS = {"p.mixed": 0, "p.learned": 0, "p.precond": 1, "p.learn_level": 2}
+P_OPTION_DEFAULTS = {"p.mixed": 0, "p.learned": 0, "p.precond": 1, "p.learn_level": 2, "mom.mixed": 0}
 
 
 def pair_text(opts) -> str:
@@ -592,12 +598,13 @@ def matched_forms(s, args, n, nnz, hbm):
             s.reset()
             s.iterate(1)  # warm-up: hierarchy set-up, graph capture
         s.reset()
-        tot, pm, pit = 0.0, [], []
+        tot, pm, mm, pit = 0.0, [], [], []
         for k in range(args.steps):
             s.timer_start()
             s.iterate(1)
             tot += s.timer_stop()
             pm.append(s.timing()[0])
+            mm.append(s.timing()[1])
             st = s.solve_stats()["p"]
             pit.append(st["iters"][0])
             if st["status"][0] != 0:
@@ -607,6 +614,7 @@ def matched_forms(s, args, n, nnz, hbm):
             ref = fields
         entry.update({"iters_per_s": args.steps / (tot / 1000.0), "ms_per_step": tot / args.steps,
                       "p_solve_ms_mean": statistics.mean(pm), "p_iters_mean": statistics.mean(pit),
+                      "mom_solve_ms_mean": statistics.mean(mm),
                       "field_rel_l2_vs_fp64": max(float(np.linalg.norm(fields[f] - ref[f]) /
                                                         max(np.linalg.norm(ref[f]), 1e-300)) for f in fields)})
         if name == "mixed_fp32_fp64":
@@ -685,8 +693,9 @@ def probe_p(args) -> dict:
     """--probe-p FORM (profiling runs, not part of the default run): on the C3 case,
     one outer iteration of the given p' form (after LEARN_ITERS training outer
     iterations for a learned form), then the momentum and p' solves of the next
-    outer iteration once more; prints the p' solve's time and iterations.  The ncu
-    summaries under profiles/ were captured from these runs."""
+    outer iteration once more; prints the time and iterations of both solves (the
+    momentum in the form's precision).  The ncu summaries under profiles/ were
+    captured from these runs."""
     from sysu_cfd_heat_gb300.solver import NavierStokesSolver
 
     forms = {name: opts for name, opts, _ in P_FORMS}
@@ -700,8 +709,10 @@ def probe_p(args) -> dict:
         s.CalculateVelocity()
         s.CalculatePressure()
         s.check()
-        st = s.solve_stats()["p"]
-        return {"form": args.probe_p, "p_ms": s.timing()[0], "p_iters": st["iters"][0], "p_status": st["status"][0]}
+        st = s.solve_stats()
+        return {"form": args.probe_p, "p_ms": s.timing()[0], "p_iters": st["p"]["iters"][0],
+                "p_status": st["p"]["status"][0], "mom_ms": s.timing()[1], "mom_iters": st["mom"]["iters"],
+                "mom_status": st["mom"]["status"]}
 
 
 def max_over_ranks(x: float, w: int) -> float:

@@ -82,8 +82,13 @@ int sysu_solver_info(sysu_solver *s, long *out, int n);
  *     momentum, k, eps, T and CG + SSOR for p' and solid T; 0: back to the
  *     default mode, BiCGSTAB + Jacobi and CG + Jacobi, which reach the same
  *     solutions to the tolerance and are faster on the GPU);
- *   "<eq>.mixed" (CG equations p, ts: FP32 inner CG in FP64 defect
- *     correction, stopping on the FP64 residual) and "<eq>.inner_tol";
+ *   "<eq>.mixed" (FP32 recurrences, stopping on the FP64 residual: p and ts
+ *     by CG with FP64 reliable updates; mom, ke, t by BiCGSTAB -- momentum with
+ *     mom_batched as one solve of u, v, w on interleaved FP32 vectors with FP64
+ *     residual replacement, otherwise one system after another with FP32 inner
+ *     iterations in FP64 defect correction; not with GMRES) and
+ *     "<eq>.inner_tol" (0 < inner_tol < 1: the FP32 residual drop between FP64
+ *     residuals; 0.1, 1e-3 for mom);
  *   "p.learned" (1: the p' CG with the learned preconditioner -- the first
  *     "p.learn_iters" solves run the plain method and train the network on
  *     their residual/correction pairs, "p.learn_steps" Adam steps each at rate
@@ -225,6 +230,18 @@ int sysu_csr_spmv_timing(int n, const int *rowptr, const int *col, const double 
 int sysu_csr_bicgstab_batched3(int n, const int *rowptr, const int *col, const double *const *vals,
                                const double *const *b, double *const *x, int maxit, double eps, int *iters,
                                double *res, int *status);
+/* Three right-hand sides b[c] of one matrix (the momentum form: u, v, w of
+ * navier_velocity.cpp:26, solved there one after another by BiCGSTABIter),
+ * x[c] x0 in and solution out, BiCGSTAB + Jacobi (omega D^-1).  mixed 0: the
+ * FP64 batched solve of the SIMPLE path; mixed 1: FP32 recurrences on the
+ * three vectors interleaved per row, x accumulated in FP64, the FP64 residual
+ * b - A x replacing the FP32 one once that fell by inner_tol (0 < inner_tol < 1),
+ * the stopping test ||b - A x|| / ||b|| < eps on it (a component whose
+ * replacements stop lowering it is finished by the FP64 solve).  iters, res,
+ * status: 3 each; refinements: replacements summed over the components. */
+int sysu_csr_bicgstab3(int n, const int *rowptr, const int *col, const double *val, const double *const *b,
+                       double *const *x, int mixed, int maxit, double eps, double omega, double inner_tol,
+                       int *iters, double *res, int *status, int *refinements);
 const char *sysu_csr_last_error(void);
 
 /* ---- aggregation-multigrid hierarchy (host only, no device work) -----------

@@ -79,6 +79,8 @@ def lib() -> C.CDLL:
             "sysu_csr_last_error": (cp, []),
             "sysu_csr_bicgstab_batched3": (C.c_int, [C.c_int, ip, ip, C.POINTER(dp), C.POINTER(dp), C.POINTER(dp),
                                                      C.c_int, C.c_double, ip, dp, ip]),
+            "sysu_csr_bicgstab3": (C.c_int, [C.c_int, ip, ip, dp, C.POINTER(dp), C.POINTER(dp), C.c_int, C.c_int,
+                                             C.c_double, C.c_double, C.c_double, ip, dp, ip, ip]),
             "sysu_setup_phases": (C.c_int, [dp]),
             "sysu_host_alloc": (vp, [C.c_size_t]),
             "sysu_host_free": (None, [vp]),

@@ -177,8 +177,10 @@ void CaseBatch::capture() {
         cudaGraphExecDestroy(exec_);
         exec_ = nullptr;
     }
-    // every allocation and one-time set-up happens in an eager iteration
+    // every allocation and one-time set-up happens in an eager iteration, in the
+    // solve forms that the graph will hold
     for (int k = 0; k < size(); ++k) {
+        at(k).graph_form = true;
         at(k).enqueue_iteration();
         at(k).sync();
         at(k).reset();

@@ -238,7 +238,11 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
                 e->mixed = value != 0.0;
                 return SYSU_OK;
             }
-            if (f == "inner_tol") { e->inner_tol = value; return SYSU_OK; }
+            if (f == "inner_tol") {
+                if (!(value > 0.0 && value < 1.0)) return set_err(SYSU_ERR_INPUT, "inner_tol must lie in (0, 1)");
+                e->inner_tol = value;
+                return SYSU_OK;
+            }
             if (f == "kind") {
                 int kind = (int)value;
                 if (kind != sysu::SK_CG && kind != sysu::SK_BICGSTAB && kind != sysu::SK_GMRES)

@@ -282,6 +282,70 @@ int sysu_csr_bicgstab_batched3(int n, const int *rowptr, const int *col, const d
     }
 }
 
+// Three right-hand sides b[c] of one matrix (the momentum form), x[c] x0 in and
+// solution out: mixed 0 the FP64 batched BiCGSTAB + Jacobi, 1 the same with
+// FP32 recurrences and FP64 residual replacement (inner_tol: the FP32 residual
+// drop that triggers one); iters/res/status per component, refinements = the
+// replacements summed over the components (0 for the FP64 form).
+int sysu_csr_bicgstab3(int n, const int *rowptr, const int *col, const double *val, const double *const *b,
+                       double *const *x, int mixed, int maxit, double eps, double omega, double inner_tol,
+                       int *iters, double *res, int *status, int *refinements) {
+    try {
+        if (n < 1 || !rowptr || !col || !val || !b || !x) throw ArgError{"n >= 1 and non-null arrays required"};
+        for (int c = 0; c < 3; ++c)
+            if (!b[c] || !x[c]) throw ArgError{"b[0..2] and x[0..2] must be non-null"};
+        if (mixed != 0 && mixed != 1) throw ArgError{"mixed: 0 FP64, 1 FP32 recurrences + FP64 replacement"};
+        if (mixed && !(inner_tol > 0.0 && inner_tol < 1.0)) throw ArgError{"inner_tol must lie in (0, 1)"};
+        if (maxit < 0 || !(eps > 0.0)) throw ArgError{"maxit >= 0 and eps > 0 required"};
+        OwnedStream os;
+        cudaStream_t st = os.st;
+        {
+            sysu::CsrDevice M;
+            M.load(n, rowptr, col, val, st);
+            sysu::DevBuf<double> db[3], dx[3];
+            for (int c = 0; c < 3; ++c) {
+                db[c].alloc(n);
+                dx[c].alloc(n);
+                db[c].upload(b[c], n, st);
+                dx[c].upload(x[c], n, st);
+            }
+            sysu::KrylovWork w;
+            sysu::DevBuf<sysu::SolveInfo> info(1);
+            sysu::KrylovOpts o;
+            o.maxit = maxit;
+            o.eps = eps;
+            o.omega = omega;
+            o.jacobi = true;
+            o.inner_tol = inner_tol;
+            const double *bb[3] = {db[0].get(), db[1].get(), db[2].get()};
+            double *xx[3] = {dx[0].get(), dx[1].get(), dx[2].get()};
+            if (mixed) {
+                sysu::Bicg3Mixed m;
+                m.solve(M.A, M.val.get(), bb, xx, o, w, info.get(), st);
+            } else {
+                sysu::bicgstab_solve(M.A, M.val.get(), 3, bb, xx, o, w, info.get(), st);
+            }
+            sysu::SolveInfo h;
+            info.download(&h, 1, st);
+            for (int c = 0; c < 3; ++c) dx[c].download(x[c], n, st);
+            SYSU_CUDA(cudaStreamSynchronize(st));
+            for (int c = 0; c < 3; ++c) {
+                if (iters) iters[c] = h.iters[c];
+                if (res) res[c] = h.res[c];
+                if (status) status[c] = h.err ? sysu::DEV_BARRIER_TIMEOUT : h.status[c];
+            }
+            if (refinements) *refinements = mixed ? h.refinements : 0;
+        }
+        return SYSU_OK;
+    } catch (const ArgError &e) {
+        g_csr_err = e.msg;
+        return SYSU_ERR_INPUT;
+    } catch (const sysu::CaseError &e) {
+        g_csr_err = e.msg;
+        return SYSU_ERR_CUDA;
+    }
+}
+
 const char *sysu_csr_last_error(void) { return g_csr_err.c_str(); }
 
 // Assembled matrix of a solver ("mom", "p", "scalar", "solid") as CSR with the

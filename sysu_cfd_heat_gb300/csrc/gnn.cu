@@ -55,41 +55,10 @@ __device__ __forceinline__ uint32_t bf_pack(float a, float b) {
 __device__ __forceinline__ float bf_round(float a) { return __bfloat162float(__float2bfloat16_rn(a)); }
 
 // The flexible-CG kernels accumulate each thread's rows (a handful) in FP32 and
-// hand those partials to grid_sums in FP64: per-row FP64 arithmetic and
-// conversions run on GB300's FP64 pipe (1/64 of the FP32 rate) and took half of
-// these kernels' time.  Convergence is decided on the FP64 residual b - A x.
-// Block partial sums of NV values -> part[block][NV]; the last block to arrive
-// adds them up (every thread of that block loads a strided share, then a block
-// reduction in a fixed order).  Returns true in exactly one thread (thread 0 of
-// the last block), which then holds the totals in v.
-template <int NV>
-__device__ bool grid_sums(double (&v)[NV], double *part, unsigned *cnt) {
-    __shared__ double sm[NV * 8];
-    __shared__ int s_last;
-    block_sum_t0<NV>(v, sm);
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; ++k) part[(size_t)blockIdx.x * NV + k] = v[k];
-        __threadfence();
-        unsigned prev = atomicAdd(cnt, 1u);
-        s_last = prev == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (!s_last) return false;
-    __threadfence();
-    double t[NV];
-#pragma unroll
-    for (int k = 0; k < NV; ++k) t[k] = 0.0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
-#pragma unroll
-        for (int k = 0; k < NV; ++k) t[k] += __ldcg(part + (size_t)b * NV + k);
-    block_sum_t0<NV>(t, sm);
-    if (threadIdx.x != 0) return false;
-    *cnt = 0;
-#pragma unroll
-    for (int k = 0; k < NV; ++k) v[k] = t[k];
-    return true;
-}
+// hand those partials to grid_sums_f (FP32 warp sums, FP64 block and grid
+// sums): per-row FP64 arithmetic and conversions run on GB300's FP64 pipe (1/64
+// of the FP32 rate) and took half of these kernels' time.  Convergence is
+// decided on the FP64 residual b - A x.
 
 // ---------------------------------------------------------------- forward --
 
@@ -150,7 +119,7 @@ __global__ void __launch_bounds__(GT) k_gnn_fwd(NetArgs a) {
     const float inv_s = *a.inv_s_p, s = *a.s_p;
     const int n = a.g.n, ntiles = (n + GT - 1) / GT;
     const uint32_t a0 = umma::smem_addr(sA), b0 = umma::smem_addr(sB);
-    double zq = 0.0;
+    float zq = 0.f;
     int it = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
         const int row = t * GT + tid;
@@ -292,13 +261,14 @@ __global__ void __launch_bounds__(GT) k_gnn_fwd(NetArgs a) {
                 float zi = s * (a.skip * u + acc);
                 if (a.zbase) zi += a.zbase[row];
                 a.z[row] = zi;
-                if (a.qprev) zq += (double)zi * (double)a.qprev[row];
+                if (a.qprev) zq = fmaf(zi, a.qprev[row], zq);
             }
         }
     }
     if (DEC && a.fs) {
-        double v[1] = {zq};
-        if (grid_sums<1>(v, a.part, &a.fs->cnt[0])) a.fs->zq = v[0];
+        const float fv[1] = {zq};
+        double v[1];
+        if (grid_sums_f<1>(fv, v, a.part, &a.fs->cnt[0])) a.fs->zq = v[0];
     }
     umma::fence_before_sync();
     __syncthreads();
@@ -811,8 +781,9 @@ __global__ void k_fcg_jacobi(FcgArgs a) {
         a.z[i] = zi;
         if (!rs) f0 += zi * a.q[i];
     }
-    double v[1] = {f0};
-    if (grid_sums<1>(v, a.part, &a.fs->cnt[0])) a.fs->zq = v[0];
+    const float fv[1] = {f0};
+    double v[1];
+    if (grid_sums_f<1>(fv, v, a.part, &a.fs->cnt[0])) a.fs->zq = v[0];
 }
 
 // multigrid form, finest level after the coarse correction z2: t = r - A z2, then
@@ -841,8 +812,9 @@ __global__ void k_fcg_mgfine(FcgArgs a, const float *z2, float *t, const float *
             if (!rs) f0 += zi * a.q[i];
         }
     }
-    double v[1] = {f0};
-    if (grid_sums<1>(v, a.part, &a.fs->cnt[0])) {
+    const float fv[1] = {f0};
+    double v[1];
+    if (grid_sums_f<1>(fv, v, a.part, &a.fs->cnt[0])) {
         if (net) {
             double s = sqrt(v[0] / (double)a.g.n);
             a.fs->s2 = (float)s;
@@ -875,8 +847,9 @@ __global__ void k_lvl_resid(GView g, const float *r, const float *zp, float *t, 
         }
     }
     if (!net) return;
-    double v[1] = {f0};
-    if (grid_sums<1>(v, part, &fs->cnt[3])) {
+    const float fv[1] = {f0};
+    double v[1];
+    if (grid_sums_f<1>(fv, v, part, &fs->cnt[3])) {
         double s = sqrt(v[0] / (double)g.n);
         fs->s2 = (float)s;
         fs->inv_s2 = s > 0.0 ? (float)(1.0 / s) : 0.f;
@@ -925,8 +898,9 @@ __global__ void k_fcg_dir(FcgArgs a) {
         f0 += pi * qi;
         f1 += pi * a.r[i];
     }
-    double v[2] = {f0, f1};
-    if (grid_sums<2>(v, a.part, &a.fs->cnt[1])) {
+    const float fv[2] = {f0, f1};
+    double v[2];
+    if (grid_sums_f<2>(fv, v, a.part, &a.fs->cnt[1])) {
         FcgState *f = a.fs;
         double pq = v[0], pr = v[1];
         double alpha = pr / pq;
@@ -965,8 +939,9 @@ __global__ void k_fcg_upd(FcgArgs a) {
         f0 += ri * ri;
         f1 += u * u;
     }
-    double v[2] = {f0, f1};
-    if (grid_sums<2>(v, a.part, &a.fs->cnt[2])) {
+    const float fv[2] = {f0, f1};
+    double v[2];
+    if (grid_sums_f<2>(fv, v, a.part, &a.fs->cnt[2])) {
         FcgState *f = a.fs;
         f->iters += 1;
         f->rr = v[0];

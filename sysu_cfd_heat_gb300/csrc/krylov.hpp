@@ -147,6 +147,36 @@ void bicgstab_solve(const SellDev &A, const double *val, int nrhs, const double 
 void bicgstab_solve_mixed(const SellDev &A, const double *val, const double *b, double *x, const KrylovOpts &o,
                           KrylovWork &w, SolveInfo *info_dev, cudaStream_t st);
 
+// Jacobi weights dinv = omega / a_ii (1 without a preconditioner) and the FP32
+// column-scaled matrix sv = a_ij dinv_j, the operator of the mixed BiCGSTAB forms.
+void jacobi_scaled32(const SellDev &A, const double *val, const KrylovOpts &o, double *dinv, float *sv32,
+                     cudaStream_t st);
+
+// The momentum form of the mixed BiCGSTAB: u, v, w of one matrix (b[c], x[c]
+// with x0 in) by one sequence of flat kernels with FP32 recurrences on vectors
+// interleaved per row, x accumulated in FP64 every iteration, and the FP64
+// residual b - A x replacing the FP32 one once it fell by o.inner_tol; stops
+// each component on ||b - A x|| / ||b|| < eps.  A component whose replacements
+// stop lowering that residual is finished by the FP64 batched BiCGSTAB from its
+// x.  Per-component status, iterations (FP32) and residual in info; refinements
+// = replacements summed over the components.  Iterations run from a captured
+// CUDA graph (recaptured when the arguments change); the host reads the state
+// once per graph.
+class Bicg3Mixed {
+  public:
+    Bicg3Mixed();
+    ~Bicg3Mixed();
+    Bicg3Mixed(const Bicg3Mixed &) = delete;
+    Bicg3Mixed &operator=(const Bicg3Mixed &) = delete;
+    void solve(const SellDev &A, const double *val, const double *const *b, double *const *x, const KrylovOpts &o,
+               KrylovWork &w, SolveInfo *info_dev, cudaStream_t st);
+    int last_refinements = 0;
+
+  private:
+    struct Impl;
+    Impl *d_;
+};
+
 // BiCGSTAB on three systems with one sparsity pattern and their own values
 // vals[c] (and Jacobi diagonals), in one launch: the column indices are read
 // once per product for the three (k, eps and T of one outer iteration).

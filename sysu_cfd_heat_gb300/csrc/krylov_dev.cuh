@@ -246,6 +246,76 @@ __device__ __forceinline__ void st2(double *p, int j, double2 v) { reinterpret_c
 __device__ __forceinline__ float4 ld4(const float *p, int j) { return reinterpret_cast<const float4 *>(p)[j]; }
 __device__ __forceinline__ void st4(float *p, int j, float4 v) { reinterpret_cast<float4 *>(p)[j] = v; }
 
+// Non-persistent kernels: thread 0 of every block publishes its block's NV
+// totals to part[block][NV] and counts its arrival; the last block to arrive
+// adds all partials up (every thread of that block loads a strided share, then
+// a block reduction in a fixed order).  Returns true in exactly one thread
+// (thread 0 of the last block), which then holds the totals in v.  sm: NV * 8
+// doubles of shared memory (blocks of at most 256 threads).
+template <int NV>
+__device__ bool grid_sums_publish(double (&v)[NV], double *part, unsigned *cnt, double *sm) {
+    __shared__ int s_last;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) part[(size_t)blockIdx.x * NV + k] = v[k];
+        __threadfence();
+        unsigned prev = atomicAdd(cnt, 1u);
+        s_last = prev == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    double t[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) t[k] = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) t[k] += __ldcg(part + (size_t)b * NV + k);
+    block_sum_t0<NV>(t, sm);
+    if (threadIdx.x != 0) return false;
+    *cnt = 0;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = t[k];
+    return true;
+}
+
+// Grid sums of FP64 per-thread values (block sum in FP64).
+template <int NV>
+__device__ bool grid_sums(double (&v)[NV], double *part, unsigned *cnt) {
+    __shared__ double sm[NV * 8];
+    block_sum_t0<NV>(v, sm);
+    return grid_sums_publish<NV>(v, part, cnt, sm);
+}
+
+// Grid sums of FP32 per-thread partials.  The warp sums stay in FP32 (a fixed
+// butterfly, so lane 0's total is the same on every run); only the warp
+// totals go to FP64 for the block and grid sums.  An FP64 shuffle tree in
+// every thread runs on GB300's FP64 pipe (1/64 of the FP32 rate): 6 FP64
+// operations per value and thread took 10-20 us of a 2M-row vector pass.
+template <int NV>
+__device__ bool grid_sums_f(const float (&f)[NV], double (&v)[NV], double *part, unsigned *cnt) {
+    __shared__ double sm[NV * 8];
+    float g[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        g[k] = f[k];
+        for (int o = 16; o > 0; o >>= 1) g[k] += __shfl_xor_sync(FULL_MASK, g[k], o);
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) sm[k * nw + warp] = (double)g[k];
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double s = 0.0;
+            for (int w = 0; w < nw; ++w) s += sm[k * nw + w];
+            v[k] = s;
+        }
+    return grid_sums_publish<NV>(v, part, cnt, sm);
+}
+
 int g_num_sms = 0;
 
 int num_sms() {

@@ -409,6 +409,7 @@ void SimpleSolver::solve(int slot, const EqOpts &o, const SellDev &A, const doub
     ko.omega = o.omega;
     ko.jacobi = o.precond == PK_JACOBI;
     SolveInfo *info = infos.get() + slot;
+    if (nrhs == 3) mom_split = true;  // statistics per component, unless the batched form runs below
     if (o.kind == SK_GMRES) {
         // one restarted GMRES per right-hand side (the reference solves u, v, w in turn)
         for (int c = 0; c < nrhs; ++c)
@@ -447,8 +448,19 @@ void SimpleSolver::solve(int slot, const EqOpts &o, const SellDev &A, const doub
             bicgstab_solve_mixed(A, val, b[0], x[0], ko, kw, info, st);
             return;
         }
-        // momentum: u, v, w one after another, each with FP32 inner iterations in
-        // FP64 defect correction (statistics per component, as the unbatched form)
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        SYSU_CUDA(cudaStreamIsCapturing(st, &cap));
+        if (nrhs == 3 && opt.mom_batched && !graph_form && cap == cudaStreamCaptureStatusNone) {
+            // momentum: u, v, w together, FP32 recurrences with FP64 residual replacement
+            mom3.solve(A, val, b, x, ko, kw, info, st);
+            mom_split = false;
+            return;
+        }
+        // momentum unbatched, or in an outer iteration captured into a graph (a
+        // graph cannot wait for the host, which the batched form does between its
+        // chunks; the eager iteration before the capture allocates for this form): u,
+        // v, w one after another, each a persistent solve with FP32 inner
+        // iterations in FP64 defect correction (statistics per component)
         for (int c = 0; c < nrhs; ++c) bicgstab_solve_mixed(A, val, b[c], x[c], ko, kw, infos.get() + SLOT_N + c, st);
         return;
     }
@@ -456,6 +468,7 @@ void SimpleSolver::solve(int slot, const EqOpts &o, const SellDev &A, const doub
         for (int c = 0; c < 3; ++c) bicgstab_solve(A, val, 1, &b[c], &x[c], ko, kw, infos.get() + SLOT_N + c, st);
         return;
     }
+    if (nrhs == 3) mom_split = false;
     bicgstab_solve(A, val, nrhs, b, x, ko, kw, info, st);
 }
 
@@ -954,7 +967,7 @@ std::string SimpleSolver::check_iteration() {
     red_out.download(ro, RED_NSLOT, st);
     flags.download(&hf, 1, st);
     SYSU_CUDA(cudaStreamSynchronize(st));
-    if (!opt.mom_batched || opt.mom.kind == SK_GMRES || opt.mom.mixed)
+    if (mom_split)
         for (int c = 0; c < 3; ++c) {
             h[SLOT_MOM].status[c] = h[SLOT_N + c].status[0];
             h[SLOT_MOM].iters[c] = h[SLOT_N + c].iters[0];

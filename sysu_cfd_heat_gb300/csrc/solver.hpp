@@ -39,8 +39,8 @@ struct EqOpts {
     int maxit = 500;
     double eps = 1e-8;
     double omega = 1.2;
-    int mixed = 0;            // CG only: FP32 inner solves in FP64 defect correction
-    double inner_tol = 0.1;   // FP32 residual drop between reliable updates
+    int mixed = 0;            // FP32 recurrences with FP64 residuals (CG; BiCGSTAB: momentum, k, eps, T)
+    double inner_tol = 0.1;   // FP32 residual drop between FP64 residual updates
     int precond = PK_JACOBI;  // PrecondKind (SSOR and ILU with CG and GMRES)
     int restart = 10;         // GMRES restart length
     // CG only (the p' equation): learned preconditioner.  The first learn_iters
@@ -69,7 +69,11 @@ struct SolverOptions {
     // navier_pressure.cpp:29, navier_scalar.cpp:101,143,374,
     // HeatConductionSolver.cpp:90), with GMRES+SSOR running as
     // BiCGSTAB+Jacobi and CG+SSOR as CG+Jacobi
-    EqOpts mom{SK_BICGSTAB, 500, 1e-8, 1.2};
+    // momentum: the FP64 residual of its mixed form costs as much as a few FP32
+    // iterations (an FP64 product of three right-hand sides), so it is taken
+    // once the FP32 residual fell by 1e-3 (2.0 ms of FP32 iterations and 0.6 ms
+    // of FP64 residuals on the 2M-cell cavity, against 2.5 + 1.6 ms at 0.1)
+    EqOpts mom{SK_BICGSTAB, 500, 1e-8, 1.2, 0, 1e-3};
     EqOpts p{SK_CG, 1000, 1e-6, 1.3};
     EqOpts ke{SK_BICGSTAB, 500, 1e-8, 1.3};
     EqOpts t{SK_BICGSTAB, 500, 1e-8, 1.3};
@@ -150,6 +154,11 @@ class SimpleSolver {
     // learned multigrid form with the network on a coarse level: the network
     // bound to that level's matrix, the hierarchy below that level (for the
     // level's own solves that give its training pairs), scratch
+    Bicg3Mixed mom3;            // momentum with FP32 recurrences (options mom.mixed + mom_batched)
+    bool mom_split = false;     // the last momentum solve left per-component statistics (SLOT_N + c)
+    // the outer iteration is (or is about to be) captured into a CUDA graph: the
+    // solves take forms that never wait for the host (set by the case batch)
+    bool graph_form = false;
     GnnPrecond gnn_c;
     AggMultigrid mg_c;
     int learn_level_built = -1;

@@ -267,6 +267,31 @@ def csr_solve(rowptr, col, val, b, x0=None, method: str = "CG", precond: str = "
     return x, it.value, rs.value, stt.value
 
 
+def csr_bicgstab3(rowptr, col, val, B, X0=None, mixed: bool = False, maxit: int = 500, eps: float = 1e-8,
+                  omega: float = 1.0, inner_tol: float = 0.1):
+    """Three right-hand sides B[c] of one CSR matrix (the momentum form) by BiCGSTAB +
+    Jacobi: FP64, or (mixed) FP32 recurrences with FP64 residual replacement.
+    Returns (X (3 x n), iters[3], res[3], status[3], refinements)."""
+    L = lib()
+    ip, dp = C.POINTER(C.c_int), C.POINTER(C.c_double)
+    rowptr = np.ascontiguousarray(rowptr, np.int32)
+    col = np.ascontiguousarray(col, np.int32)
+    val = np.ascontiguousarray(val, np.float64)
+    n = len(rowptr) - 1
+    B = [np.ascontiguousarray(B[c], np.float64) for c in range(3)]
+    X = [np.zeros(n) if X0 is None else np.array(X0[c], dtype=np.float64) for c in range(3)]
+    bp = (dp * 3)(*[_dptr(b) for b in B])
+    xp = (dp * 3)(*[_dptr(x) for x in X])
+    it, rs, stt, ref = (C.c_int * 3)(), (C.c_double * 3)(), (C.c_int * 3)(), C.c_int()
+    code = L.sysu_csr_bicgstab3(n, rowptr.ctypes.data_as(ip), col.ctypes.data_as(ip), _dptr(val), bp, xp,
+                                1 if mixed else 0, int(maxit), float(eps), float(omega), float(inner_tol), it, rs,
+                                stt, C.byref(ref))
+    if code != 0:
+        L.sysu_csr_last_error.restype = C.c_char_p
+        raise SysuError(code, L.sysu_csr_last_error().decode())
+    return np.stack(X), list(it), list(rs), list(stt), ref.value
+
+
 def csr_spmv_timing(rowptr, col, val, fp32: bool = False, reps: int = 10) -> float:
     """Mean device ms of one y = A x (L2 flushed before each) for a host CSR matrix."""
     L = lib()

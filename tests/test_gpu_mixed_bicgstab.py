@@ -135,10 +135,12 @@ def test_mixed_option_rules():
                 s.set_option("t.mixed", 1)
 
 
-def test_momentum_mixed_reaches_the_fp64_fields():
-    """Option mom.mixed: u, v and w each by BiCGSTAB with FP32 inner iterations in
-    FP64 defect correction; solved to a tight tolerance, the SIMPLE fields equal the
-    FP64 form's."""
+@pytest.mark.parametrize("batched", [1, 0])
+def test_momentum_mixed_reaches_the_fp64_fields(batched):
+    """Option mom.mixed: u, v and w by BiCGSTAB with FP32 recurrences -- together on
+    interleaved vectors with FP64 residual replacement (mom_batched 1), or one after
+    another with FP32 inner iterations in FP64 defect correction (mom_batched 0);
+    solved to a tight tolerance, the SIMPLE fields equal the FP64 form's."""
     import tempfile
 
     from sysu_cfd_heat_gb300 import meshgen as mg
@@ -147,7 +149,7 @@ def test_momentum_mixed_reaches_the_fp64_fields():
     with tempfile.TemporaryDirectory() as tmp:
         p = mg.write_case(tmp, mg.lid_cavity_tet(8, 8, 6, jitter=0.2), mg.cavity_param("x", 20, mu=0.0025))
         out = {}
-        for name, opts in (("fp64", {}), ("mixed", {"mom.mixed": 1, "p.mixed": 1})):
+        for name, opts in (("fp64", {}), ("mixed", {"mom.mixed": 1, "p.mixed": 1, "mom_batched": batched})):
             with NavierStokesSolver(p, dict({"rtc": 1e-11}, **opts)) as s:
                 assert s.iterate(15) == 15
                 st = s.solve_stats()["mom"]
