@@ -88,7 +88,7 @@ int sysu_solver_info(sysu_solver *s, long *out, int n);
  *     residual replacement, otherwise one system after another with FP32 inner
  *     iterations in FP64 defect correction; not with GMRES) and
  *     "<eq>.inner_tol" (0 < inner_tol < 1: the FP32 residual drop between FP64
- *     residuals; 0.1, 1e-3 for mom);
+ *     residuals; 0.1, 1e-4 for mom);
  *   "p.learned" (1: the p' CG with the learned preconditioner -- the first
  *     "p.learn_iters" solves run the plain method and train the network on
  *     their residual/correction pairs, "p.learn_steps" Adam steps each at rate

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <memory>
+#include <type_traits>
 
 #include "amg.hpp"
 #include "krylov_dev.cuh"
@@ -25,6 +26,19 @@ struct MgView {
 };
 
 int flat_blocks(long n) { return (int)std::max(1L, std::min((n + MB - 1) / MB, (long)num_sms() * 8)); }
+
+// f(std::integral_constant<int, G>) for the group width g (1, 2, 4, ..., 32)
+template <class F>
+void with_group(int g, F f) {
+    switch (g) {
+        case 1: f(std::integral_constant<int, 1>{}); break;
+        case 2: f(std::integral_constant<int, 2>{}); break;
+        case 4: f(std::integral_constant<int, 4>{}); break;
+        case 8: f(std::integral_constant<int, 8>{}); break;
+        case 16: f(std::integral_constant<int, 16>{}); break;
+        default: f(std::integral_constant<int, 32>{}); break;
+    }
+}
 
 // coarse value at stored position q = sum of its fine entries (fixed order)
 __global__ void k_mg_galerkin(long npos, const int *gal_ptr, const int *gal_src, const double *fval, double *cval,
@@ -55,30 +69,97 @@ __device__ __forceinline__ float row_times(const MgView &A, int i, const float *
     return s;
 }
 
-// t = r - A (w r)   (pre-smoothing from zero and its residual)
-__global__ void k_mg_down(MgView A, const float *w, const float *r, float *t, const int *done) {
-    if (done && *done) return;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x) {
-        const int base = A.sl_ptr[i >> 5], wd = A.sl_w[i >> 5], lane = i & 31;
-        float s = 0.f;
-        for (int k = 0; k < wd; ++k) {
-            const int pos = base + k * 32 + lane;
-            const int j = A.col[pos];
-            s += A.val[pos] * (w[j] * r[j]);
-        }
-        t[i] = r[i] - s;
+// Coarse levels have wide rows (aggregation merges neighbourhoods) and few of
+// them: one thread per row walks a long chain of dependent loads (column, then
+// the gathered value) while most of the GPU idles; a 500-row level took 10 us.
+// The cycle kernels therefore give each row (or aggregate) a group of G lanes
+// of one warp: lane s of the group takes entries s, s + G, ..., and the partial
+// sums meet in a fixed xor butterfly, so every lane of the group holds the sum
+// and every run adds in the same order.  The loops advance whole warps (the
+// butterfly needs every lane), with the lanes past the end contributing 0.
+constexpr int MG_GROUP_ENTRIES = 6;  // entries per lane aimed at when choosing G
+
+// Lanes per row for `rows` rows of `width` entries: enough that a lane takes
+// about MG_GROUP_ENTRIES entries, but no more than the GPU's resident threads
+// need -- a level that fills the SMs at one row per thread (level 1 of the 2M-row
+// p' system, 250k rows) ran slower with 4 lanes a row (13 -> 20 us), its loads no
+// longer coalesced.
+int mg_group(int width, long rows) {
+    const long cap = (long)num_sms() * 2048;
+    int g = 1;
+    while (g < 32 && (width + g - 1) / g > MG_GROUP_ENTRIES && rows * 2 * g <= cap) g *= 2;
+    return g;
+}
+
+template <int G>
+__device__ __forceinline__ float group_sum(float v) {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(FULL_MASK, v, o);
+    return v;
+}
+
+// lane s's share of row i of A times x (entries s, s + G, ...)
+template <int G>
+__device__ __forceinline__ float row_part(const MgView &A, int i, const float *x, int s) {
+    const int base = A.sl_ptr[i >> 5], wd = A.sl_w[i >> 5], lane = i & 31;
+    float acc = 0.f;
+#pragma unroll 4
+    for (int k = s; k < wd; k += G) {
+        const int pos = base + k * 32 + lane;
+        acc += A.val[pos] * x[A.col[pos]];
+    }
+    return acc;
+}
+
+// the grid-stride walk over n groups of G lanes: f(valid, i, s) with i the
+// group (row or aggregate), s the lane in the group, valid = i < n; whole warps
+// advance together
+template <int G, class F>
+__device__ __forceinline__ void group_loop(int n, F f) {
+    const long total = (long)n * G, stride = (long)gridDim.x * blockDim.x;
+    for (long base = (long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
+        const long vt = base + (threadIdx.x & 31);
+        const bool valid = vt < total;
+        f(valid, valid ? (int)(vt / G) : 0, (int)(vt % G));
     }
 }
 
-// rc[I] = sum of t over the rows of aggregate I (ascending)
+// t = r - A (w r)   (pre-smoothing from zero and its residual)
+template <int G>
+__global__ void k_mg_down(MgView A, const float *w, const float *r, float *t, const int *done) {
+    if (done && *done) return;
+    group_loop<G>(A.n, [&](bool valid, int i, int s) {
+        float acc = 0.f;
+        if (valid) {
+            const int base = A.sl_ptr[i >> 5], wd = A.sl_w[i >> 5], lane = i & 31;
+#pragma unroll 4
+            for (int k = s; k < wd; k += G) {
+                const int pos = base + k * 32 + lane;
+                const int j = A.col[pos];
+                acc += A.val[pos] * (w[j] * r[j]);
+            }
+        }
+        acc = group_sum<G>(acc);
+        if (valid && s == 0) t[i] = r[i] - acc;
+    });
+}
+
+// rc[I] = sum of t over the rows of aggregate I (members in ascending order,
+// lane s taking members s, s + G, ...)
+template <int G>
 __global__ void k_mg_restrict(int nc, const int *mem_ptr, const int *mem_idx, const float *t, float *rc,
                               const int *done) {
     if (done && *done) return;
-    for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < nc; I += gridDim.x * blockDim.x) {
-        float s = 0.f;
-        for (int k = mem_ptr[I]; k < mem_ptr[I + 1]; ++k) s += t[mem_idx[k]];
-        rc[I] = s;
-    }
+    group_loop<G>(nc, [&](bool valid, int i, int s) {
+        float acc = 0.f;
+        if (valid) {
+            const int k1 = mem_ptr[i + 1];
+#pragma unroll 4
+            for (int k = mem_ptr[i] + s; k < k1; k += G) acc += t[mem_idx[k]];
+        }
+        acc = group_sum<G>(acc);
+        if (valid && s == 0) rc[i] = acc;
+    });
 }
 
 // z_i = w_i r_i + gamma zc[agg(i)]
@@ -90,10 +171,14 @@ __global__ void k_mg_prolong(int n, const float *w, const float *r, const int *a
 }
 
 // zout = z + w (r - A z)
+template <int G>
 __global__ void k_mg_post(MgView A, const float *w, const float *r, const float *z, float *zout, const int *done) {
     if (done && *done) return;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x)
-        zout[i] = z[i] + w[i] * (r[i] - row_times(A, i, z));
+    group_loop<G>(A.n, [&](bool valid, int i, int s) {
+        float acc = valid ? row_part<G>(A, i, z, s) : 0.f;
+        acc = group_sum<G>(acc);
+        if (valid && s == 0) zout[i] = z[i] + w[i] * (r[i] - acc);
+    });
 }
 
 // t = r - A z
@@ -368,6 +453,7 @@ void AggMultigrid::setup(const SellDev &A, const SellPattern &pat, const double 
             d->val64.alloc(h.pat.nnz);
             d->val32.alloc(h.pat.nnz);
         }
+        d->grow = mg_group(l > 0 ? d->A.wmax : A.wmax, h.n);
         d->w.alloc(h.n);
         d->r.alloc(h.n);
         d->z.alloc(h.n);
@@ -376,6 +462,9 @@ void AggMultigrid::setup(const SellDev &A, const SellPattern &pat, const double 
             d->agg.upload(h.agg, st);
             d->mem_ptr.upload(h.mem_ptr, st);
             d->mem_idx.upload(h.mem_idx, st);
+            int widest = 1;
+            for (size_t I = 0; I + 1 < h.mem_ptr.size(); ++I) widest = std::max(widest, h.mem_ptr[I + 1] - h.mem_ptr[I]);
+            d->gagg = mg_group(widest, (long)h.mem_ptr.size() - 1);
             d->gal_ptr.upload(h.gal_ptr, st);
             d->gal_src.upload(h.gal_src, st);
         }
@@ -437,8 +526,14 @@ void AggMultigrid::enqueue_down(int l, const float *r, const int *done, cudaStre
     MgLevelDev &c = *lv_[l + 1];
     const SellDev &A = l == 0 ? *A0_ : d.A;
     const float *v32 = l == 0 ? val0_32_ : d.val32.get();
-    k_mg_down<<<flat_blocks(A.n), MB, 0, st>>>(view_of(A, v32), d.w.get(), r, d.t.get(), done);
-    k_mg_restrict<<<flat_blocks(c.n), MB, 0, st>>>(c.n, d.mem_ptr.get(), d.mem_idx.get(), d.t.get(), c.r.get(), done);
+    with_group(d.grow, [&](auto G) {
+        k_mg_down<G.value><<<flat_blocks((long)A.n * G.value), MB, 0, st>>>(view_of(A, v32), d.w.get(), r, d.t.get(),
+                                                                             done);
+    });
+    with_group(d.gagg, [&](auto G) {
+        k_mg_restrict<G.value><<<flat_blocks((long)c.n * G.value), MB, 0, st>>>(c.n, d.mem_ptr.get(), d.mem_idx.get(),
+                                                                                 d.t.get(), c.r.get(), done);
+    });
     g_launches += 2;
 }
 
@@ -455,8 +550,10 @@ void AggMultigrid::enqueue_up(int l, float *zout, const int *done, cudaStream_t 
         post_hook(l, d.r.get(), d.t.get(), zout, done, st);
         return;
     }
-    k_mg_post<<<flat_blocks(d.n), MB, 0, st>>>(view_of(A, d.val32.get()), d.w.get(), d.r.get(), d.t.get(), zout,
-                                                done);
+    with_group(d.grow, [&](auto G) {
+        k_mg_post<G.value><<<flat_blocks((long)d.n * G.value), MB, 0, st>>>(view_of(A, d.val32.get()), d.w.get(),
+                                                                             d.r.get(), d.t.get(), zout, done);
+    });
     ++g_launches;
 }
 
@@ -479,7 +576,10 @@ void AggMultigrid::enqueue_cycle_to_fine(const float *r, float *z, const int *do
     }
     if (persistent && !(post_hook && post_level >= 1)) {
         MgLevelDev &d0 = *lv_[0];
-        k_mg_down<<<flat_blocks(f.n), MB, 0, st>>>(view_of(*A0_, val0_32_), d0.w.get(), r, d0.t.get(), done);
+        with_group(d0.grow, [&](auto G) {
+            k_mg_down<G.value><<<flat_blocks((long)f.n * G.value), MB, 0, st>>>(view_of(*A0_, val0_32_), d0.w.get(),
+                                                                                 r, d0.t.get(), done);
+        });
         ++g_launches;
         MgPersistArgs pa{};
         pa.nlev = L;
@@ -513,10 +613,13 @@ void AggMultigrid::enqueue_cycle_to_fine(const float *r, float *z, const int *do
         ++g_launches;
     } else {  // coarsest too large for the dense inverse: three Jacobi steps from zero
         k_mg_scale<<<flat_blocks(c.n), MB, 0, st>>>(c.n, c.w.get(), c.r.get(), c.z.get(), done);
-        k_mg_post<<<flat_blocks(c.n), MB, 0, st>>>(view_of(c.A, c.val32.get()), c.w.get(), c.r.get(), c.z.get(),
-                                                   c.t.get(), done);
-        k_mg_post<<<flat_blocks(c.n), MB, 0, st>>>(view_of(c.A, c.val32.get()), c.w.get(), c.r.get(), c.t.get(),
-                                                   c.z.get(), done);
+        with_group(c.grow, [&](auto G) {
+            const int gb = flat_blocks((long)c.n * G.value);
+            k_mg_post<G.value><<<gb, MB, 0, st>>>(view_of(c.A, c.val32.get()), c.w.get(), c.r.get(), c.z.get(),
+                                                  c.t.get(), done);
+            k_mg_post<G.value><<<gb, MB, 0, st>>>(view_of(c.A, c.val32.get()), c.w.get(), c.r.get(), c.t.get(),
+                                                  c.z.get(), done);
+        });
         g_launches += 3;
     }
     for (int l = L - 2; l >= 1; --l) enqueue_up(l, lv_[l]->z.get(), done, st);
@@ -539,8 +642,10 @@ void AggMultigrid::apply_fixed(const float *r, float *z2, float *t, const int *f
 
 void AggMultigrid::apply(const float *r, float *z, const int *fs_done, cudaStream_t st) {
     enqueue_cycle_to_fine(r, tmpz_.get(), fs_done, st);
-    k_mg_post<<<flat_blocks(A0_->n), MB, 0, st>>>(view_of(*A0_, val0_32_), lv_[0]->w.get(), r, tmpz_.get(), z,
-                                                  fs_done);
+    with_group(lv_[0]->grow, [&](auto G) {
+        k_mg_post<G.value><<<flat_blocks((long)A0_->n * G.value), MB, 0, st>>>(
+            view_of(*A0_, val0_32_), lv_[0]->w.get(), r, tmpz_.get(), z, fs_done);
+    });
     ++g_launches;
     SYSU_CUDA(cudaGetLastError());
 }

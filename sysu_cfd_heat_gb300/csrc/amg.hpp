@@ -68,6 +68,7 @@ struct MgLevelDev {
     DevBuf<float> w;               // omega / a_ii
     DevBuf<float> r, z, t;         // cycle vectors
     DevBuf<int> agg, mem_ptr, mem_idx, gal_ptr, gal_src;  // to the next level
+    int grow = 1, gagg = 1;        // lanes per row / per aggregate of the cycle kernels
 };
 
 // b = a in FP64 (n values on the device)

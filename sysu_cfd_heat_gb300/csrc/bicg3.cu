@@ -53,9 +53,10 @@ struct M3State {
 struct M3Args {
     int n;
     const int *sl_ptr, *sl_w, *col;
-    const float *sv;    // FP32 column-scaled values a_ij d_j
+    float *sv;          // FP32 column-scaled values a_ij d_j
     const double *val;  // FP64 values (residual replacement)
-    const double *dinv; // FP64 Jacobi weights
+    float *dinv;        // FP32 Jacobi weights
+    double *r0;         // the FP64 residual of x0 (three arrays of n), from k_m3_init
     const double *b[3];
     double *x[3];
     float4 *r, *rtd, *p, *v, *s, *t, *e;
@@ -131,8 +132,24 @@ __device__ __forceinline__ void resid3(const M3Args &a, int i, const bool (&want
     for (int c = 0; c < 3; ++c) r[c] = want[c] ? a.b[c][i] - y[c] : 0.0;
 }
 
-// First pass: ||b||^2 and ||b - A x0||^2 per component, the scale of the FP32
-// vectors, and the vectors' initial contents (rtd = (0, 0, 0, d), p = v = 0).
+// Jacobi weights in FP32, d_i = omega / a_ii (1 without a preconditioner); the
+// diagonal is entry 0 of every row
+__global__ void __launch_bounds__(MB) k_m3_dinv(M3Args a, float omega, int jacobi) {
+    const int i = blockIdx.x * MB + threadIdx.x;
+    if (i >= a.n) return;
+    a.dinv[i] = jacobi ? omega / (float)a.val[a.sl_ptr[i >> 5] + (i & 31)] : 1.f;
+}
+
+// The operator of the FP32 recurrences: sv_e = a_e d_(col e) in FP32 over all
+// stored entries (padding entries hold 0)
+__global__ void __launch_bounds__(MB) k_m3_scale(M3Args a, long nnz) {
+    const long e = (long)blockIdx.x * MB + threadIdx.x;
+    if (e < nnz) a.sv[e] = (float)a.val[e] * a.dinv[a.col[e]];
+}
+
+// First pass: ||b||^2 and ||b - A x0||^2 per component (the residual kept in r0
+// for the set-up replacement), the scale of the FP32 vectors, and the vectors'
+// initial contents (rtd = (0, 0, 0, d), p = v = e = 0).
 __global__ void __launch_bounds__(MB) k_m3_init(M3Args a, int maxit, double eps, double d2) {
     double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     const bool all[3] = {true, true, true};
@@ -144,8 +161,9 @@ __global__ void __launch_bounds__(MB) k_m3_init(M3Args a, int maxit, double eps,
             const double bi = a.b[c][i];
             v[c] = fma(bi, bi, v[c]);
             v[3 + c] = fma(r[c], r[c], v[3 + c]);
+            a.r0[(size_t)c * a.n + i] = r[c];
         }
-        a.rtd[i] = make_float4(0.f, 0.f, 0.f, (float)a.dinv[i]);
+        a.rtd[i] = make_float4(0.f, 0.f, 0.f, a.dinv[i]);
         a.p[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         a.v[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         a.e[i] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -181,32 +199,39 @@ __global__ void __launch_bounds__(MB) k_m3_init(M3Args a, int maxit, double eps,
 
 // FP64 residual replacement for the components that need it: r_c = sig (b - A x)
 // with the scale chosen from the FP32 residual that triggered it; rt_c = r_c
-// when the component restarts.  first: the set-up pass (no stall bookkeeping).
+// when the component restarts.  first: the set-up pass (the residual of x0 from
+// r0, no stall bookkeeping).
 __global__ void __launch_bounds__(MB) k_m3_replace(M3Args a, int first) {
     const M3State *S = a.st;
     if (S->all_done || !S->any_need) return;
     bool want[3], rs[3];
-    float sg[3];
+    double sg[3];
     bool any_rs = false;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         want[c] = S->need[c] && !S->done[c];
         rs[c] = want[c] && S->restart[c];
         any_rs |= rs[c];
-        sg[c] = (float)S->sig_next[c];  // a power of two: exact in FP32
+        sg[c] = S->sig_next[c];
     }
-    double v64[3] = {0.0, 0.0, 0.0};
+    // the norms come from the scaled FP32 residual (sig r ~ 1: no under- or
+    // overflow), summed like the recurrences' dot products; an FP64 square per row
+    // and an FP64 shuffle tree would cost a fifth of this FP64-bound pass
     float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     for (int i = blockIdx.x * MB + threadIdx.x; i < a.n; i += gridDim.x * MB) {
         double r64[3];
-        resid3(a, i, want, r64);
+        if (first) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) r64[c] = want[c] ? a.r0[(size_t)c * a.n + i] : 0.0;
+        } else {
+            resid3(a, i, want, r64);
+        }
         float4 r = a.r[i];
         float4 rt = a.rtd[i];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             if (!want[c]) continue;
-            v64[c] = fma(r64[c], r64[c], v64[c]);
-            const float rn = (float)((double)sg[c] * r64[c]);
+            const float rn = (float)(sg[c] * r64[c]);
             comp(r, c) = rn;
             if (rs[c]) comp(rt, c) = rn;
             f[c] = fmaf(rn, rn, f[c]);
@@ -215,30 +240,24 @@ __global__ void __launch_bounds__(MB) k_m3_replace(M3Args a, int first) {
         a.r[i] = r;
         if (any_rs) a.rtd[i] = rt;
     }
-    double v[9];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        v[c] = v64[c];
-        v[3 + c] = (double)f[c];
-        v[6 + c] = (double)f[3 + c];
-    }
-    if (!grid_sums<9>(v, a.part, &a.st->cnt)) return;
+    double v[6];
+    if (!grid_sums_f<6>(f, v, a.part, &a.st->cnt)) return;
     M3State *W = a.st;
     int all_done = 1;
     for (int c = 0; c < 3; ++c) {
         if (want[c]) {
-            const double rr = v[c];
+            const double rr = v[c] / (sg[c] * sg[c]);  // ||b - A x||^2
             if (!first) W->upd[c] += 1;
             W->rr64[c] = rr;
             W->sig[c] = W->sig_next[c];
-            W->rref[c] = v[3 + c];
+            W->rref[c] = v[c];
             if (rs[c]) {
-                W->rho[c] = v[3 + c];
+                W->rho[c] = v[c];
             } else {
                 // the recurrences go on with the replaced residual: rho on it; the
                 // previous rho is in the old scale, which makes beta carry the
                 // change of scale onto the old p - omega v
-                W->rho[c] = v[6 + c];
+                W->rho[c] = v[3 + c];
                 W->beta[c] = W->omg[c] != 0.0 ? (W->rho[c] / W->rho_prev[c]) * (W->alpha[c] / W->omg[c]) : 0.0;
             }
             if (!first) {
@@ -376,7 +395,7 @@ __global__ void __launch_bounds__(MB, 6) k_m3_at(M3Args a) {
 
 // e += d (alpha p + omega s) ; r = s - omega t ; r.r, rt.r -> rho, beta, and
 // whether a replacement follows
-__global__ void __launch_bounds__(MB) k_m3_upd(M3Args a) {
+__global__ void __launch_bounds__(MB, 6) k_m3_upd(M3Args a) {
     const M3State *S = a.st;
     if (S->all_done) return;
     bool on[3], ea[3];
@@ -487,8 +506,8 @@ __global__ void k_m3_info(const M3State *S, SolveInfo *info, int after_fp64) {
 
 struct Bicg3Mixed::Impl {
     DevBuf<float4> r, rtd, p, v, s, t, e;
-    DevBuf<double> dinv;
-    DevBuf<float> sv32;
+    DevBuf<float> dinv, sv32;
+    DevBuf<double> r0;
     DevBuf<M3State> st;
     DevBuf<double> part;
     int n = 0;
@@ -512,6 +531,7 @@ void Bicg3Mixed::solve(const SellDev &A, const double *val, const double *const 
     if (d.n < n) {
         d.r.alloc(n); d.rtd.alloc(n); d.p.alloc(n); d.v.alloc(n); d.s.alloc(n); d.t.alloc(n); d.e.alloc(n);
         d.dinv.alloc(n);
+        d.r0.alloc((size_t)3 * n);
         d.n = n;
     }
     if (!d.st.size()) d.st.alloc(1);
@@ -535,9 +555,7 @@ void Bicg3Mixed::solve(const SellDev &A, const double *val, const double *const 
         gmax = std::max(gmax, g[k]);
     }
     if (d.part.size() < (size_t)gmax * 9) d.part.alloc((size_t)gmax * 9);
-    // Jacobi weights (FP64) and the FP32 column-scaled matrix
     if (d.sv32.size() < (size_t)A.nnz) d.sv32.alloc(A.nnz);
-    jacobi_scaled32(A, val, o, d.dinv.get(), d.sv32.get(), st);
     SYSU_CUDA(cudaMemsetAsync(d.st.get(), 0, sizeof(M3State), st));
 
     M3Args a;
@@ -549,6 +567,7 @@ void Bicg3Mixed::solve(const SellDev &A, const double *val, const double *const 
     a.sv = d.sv32.get();
     a.val = val;
     a.dinv = d.dinv.get();
+    a.r0 = d.r0.get();
     for (int c = 0; c < 3; ++c) {
         a.b[c] = b[c];
         a.x[c] = x[c];
@@ -557,6 +576,11 @@ void Bicg3Mixed::solve(const SellDev &A, const double *val, const double *const 
     a.e = d.e.get();
     a.st = d.st.get();
     a.part = d.part.get();
+    // FP32 Jacobi weights and column-scaled matrix (FP64 would take a division per
+    // row and a product per entry on the 1/64-rate FP64 pipe: 78 us of 2M rows)
+    k_m3_dinv<<<(n + MB - 1) / MB, MB, 0, st>>>(a, (float)o.omega, o.jacobi ? 1 : 0);
+    if (A.nnz > 0) k_m3_scale<<<(unsigned)((A.nnz + MB - 1) / MB), MB, 0, st>>>(a, A.nnz);
+    g_launches += A.nnz > 0 ? 2 : 1;
     k_m3_init<<<g[0], MB, 0, st>>>(a, o.maxit, o.eps, o.inner_tol * o.inner_tol);
     k_m3_replace<<<g[1], MB, 0, st>>>(a, 1);
     g_launches += 2;

@@ -1144,18 +1144,6 @@ void bicgstab_solve_mixed(const SellDev &A, const double *val, const double *b, 
     bicg_launch(A, vv, false, 1, bb, xx, o, w, info, st, info);
 }
 
-void jacobi_scaled32(const SellDev &A, const double *val, const KrylovOpts &o, double *dinv, float *sv32,
-                     cudaStream_t st) {
-    const int n = A.n;
-    if (n == 0) return;
-    { k_jacobi_dinv<<<(n + KB - 1) / KB, KB, 0, st>>>(view(A, val), o.omega, o.jacobi ? 1 : 0, dinv); ++::sysu::g_launches; }
-    if (A.nnz > 0) {
-        k_scale_cols32<<<(unsigned)((A.nnz + KB - 1) / KB), KB, 0, st>>>(A.nnz, A.col.get(), val, dinv, sv32);
-        ++::sysu::g_launches;
-    }
-    SYSU_CUDA(cudaGetLastError());
-}
-
 void bicgstab_solve_multi(const SellDev &A, const double *const *vals, const double *const *b, double *const *x,
                           const KrylovOpts &o, KrylovWork &w, SolveInfo *info, cudaStream_t st) {
     if (A.n == 0) return;

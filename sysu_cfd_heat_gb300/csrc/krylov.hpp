@@ -147,11 +147,6 @@ void bicgstab_solve(const SellDev &A, const double *val, int nrhs, const double 
 void bicgstab_solve_mixed(const SellDev &A, const double *val, const double *b, double *x, const KrylovOpts &o,
                           KrylovWork &w, SolveInfo *info_dev, cudaStream_t st);
 
-// Jacobi weights dinv = omega / a_ii (1 without a preconditioner) and the FP32
-// column-scaled matrix sv = a_ij dinv_j, the operator of the mixed BiCGSTAB forms.
-void jacobi_scaled32(const SellDev &A, const double *val, const KrylovOpts &o, double *dinv, float *sv32,
-                     cudaStream_t st);
-
 // The momentum form of the mixed BiCGSTAB: u, v, w of one matrix (b[c], x[c]
 // with x0 in) by one sequence of flat kernels with FP32 recurrences on vectors
 // interleaved per row, x accumulated in FP64 every iteration, and the FP64

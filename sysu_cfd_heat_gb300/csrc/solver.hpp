@@ -69,11 +69,11 @@ struct SolverOptions {
     // navier_pressure.cpp:29, navier_scalar.cpp:101,143,374,
     // HeatConductionSolver.cpp:90), with GMRES+SSOR running as
     // BiCGSTAB+Jacobi and CG+SSOR as CG+Jacobi
-    // momentum: the FP64 residual of its mixed form costs as much as a few FP32
-    // iterations (an FP64 product of three right-hand sides), so it is taken
-    // once the FP32 residual fell by 1e-3 (2.0 ms of FP32 iterations and 0.6 ms
-    // of FP64 residuals on the 2M-cell cavity, against 2.5 + 1.6 ms at 0.1)
-    EqOpts mom{SK_BICGSTAB, 500, 1e-8, 1.2, 0, 1e-3};
+    // momentum: an FP64 residual of its mixed form costs as much as an FP32
+    // iteration (an FP64 product for three right-hand sides), so it is taken once
+    // the FP32 residual fell by 1e-4 (2M-cell cavity: 3.1 ms per solve, against
+    // 3.4 ms at 1e-3 and 5.1 ms at 0.1)
+    EqOpts mom{SK_BICGSTAB, 500, 1e-8, 1.2, 0, 1e-4};
     EqOpts p{SK_CG, 1000, 1e-6, 1.3};
     EqOpts ke{SK_BICGSTAB, 500, 1e-8, 1.3};
     EqOpts t{SK_BICGSTAB, 500, 1e-8, 1.3};
