@@ -7,6 +7,7 @@
 // (*done != 0), so a captured chunk of iterations costs little past convergence.
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <memory>
 #include <type_traits>
 
@@ -132,8 +133,20 @@ __global__ void k_mg_down(MgView A, const float *w, const float *r, float *t, co
         float acc = 0.f;
         if (valid) {
             const int base = A.sl_ptr[i >> 5], wd = A.sl_w[i >> 5], lane = i & 31;
-#pragma unroll 4
-            for (int k = s; k < wd; k += G) {
+            int k = s;
+            if (G == 1) {  // one lane a row (the finest level): four entries' loads before their gathers
+                for (; k + 4 <= wd; k += 4) {
+                    const int p0 = base + k * 32 + lane;
+                    const int j0 = A.col[p0], j1 = A.col[p0 + 32], j2 = A.col[p0 + 64], j3 = A.col[p0 + 96];
+                    const float v0 = A.val[p0], v1 = A.val[p0 + 32], v2 = A.val[p0 + 64], v3 = A.val[p0 + 96];
+                    const float y0 = w[j0] * r[j0], y1 = w[j1] * r[j1], y2 = w[j2] * r[j2], y3 = w[j3] * r[j3];
+                    acc += v0 * y0;
+                    acc += v1 * y1;
+                    acc += v2 * y2;
+                    acc += v3 * y3;
+                }
+            }
+            for (; k < wd; k += G) {
                 const int pos = base + k * 32 + lane;
                 const int j = A.col[pos];
                 acc += A.val[pos] * (w[j] * r[j]);
@@ -162,12 +175,28 @@ __global__ void k_mg_restrict(int nc, const int *mem_ptr, const int *mem_idx, co
     });
 }
 
-// z_i = w_i r_i + gamma zc[agg(i)]
+// z_i = w_i r_i + gamma zc[agg(i)]; four rows a thread with 16-byte loads (the
+// level's arrays are whole allocations; r may be the caller's fine residual,
+// which is read four rows at a time only when 16-byte aligned)
 __global__ void k_mg_prolong(int n, const float *w, const float *r, const int *agg, const float *zc, float gamma,
                              float *z, const int *done) {
     if (done && *done) return;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        z[i] = w[i] * r[i] + gamma * zc[agg[i]];
+    const int T = gridDim.x * blockDim.x, t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    int n4 = 0;
+    if ((reinterpret_cast<uintptr_t>(r) & 15) == 0 && (reinterpret_cast<uintptr_t>(z) & 15) == 0) {
+        n4 = n >> 2;
+        for (int j = t0; j < n4; j += T) {
+            const float4 wj = reinterpret_cast<const float4 *>(w)[j], rj = reinterpret_cast<const float4 *>(r)[j];
+            const int4 aj = reinterpret_cast<const int4 *>(agg)[j];
+            float4 zj;
+            zj.x = wj.x * rj.x + gamma * zc[aj.x];
+            zj.y = wj.y * rj.y + gamma * zc[aj.y];
+            zj.z = wj.z * rj.z + gamma * zc[aj.z];
+            zj.w = wj.w * rj.w + gamma * zc[aj.w];
+            reinterpret_cast<float4 *>(z)[j] = zj;
+        }
+    }
+    for (int i = 4 * n4 + t0; i < n; i += T) z[i] = w[i] * r[i] + gamma * zc[agg[i]];
 }
 
 // zout = z + w (r - A z)

@@ -720,6 +720,29 @@ struct FcgArgs {
     int stall_max;
 };
 
+// Row i of the FP32 matrix times x, the column indices and values of four
+// entries loaded before their gathers (the sum runs in entry order, as a plain
+// loop's); default cache policy, so the matrix stays in L2 between the kernels
+// of an iteration that read it
+__device__ __forceinline__ float sell_dot32(const GView &g, int i, const float *x) {
+    const int lane = i & 31;
+    int e = g.sl_ptr[i >> 5] + lane;
+    const int w = g.sl_w[i >> 5];
+    float acc = 0.f;
+    int k = 0;
+    for (; k + 4 <= w; k += 4, e += 128) {
+        const int c0 = g.col[e], c1 = g.col[e + 32], c2 = g.col[e + 64], c3 = g.col[e + 96];
+        const float v0 = g.val[e], v1 = g.val[e + 32], v2 = g.val[e + 64], v3 = g.val[e + 96];
+        const float x0 = x[c0], x1 = x[c1], x2 = x[c2], x3 = x[c3];
+        acc += v0 * x0;
+        acc += v1 * x1;
+        acc += v2 * x2;
+        acc += v3 * x3;
+    }
+    for (; k < w; ++k, e += 32) acc += g.val[e] * x[g.col[e]];
+    return acc;
+}
+
 __device__ __forceinline__ double spmv64_row(const GView &g, const double *val64, const double *x, int row) {
     const int sl = row >> 5, lane = row & 31;
     const int base = g.sl_ptr[sl], w = g.sl_w[sl];
@@ -794,14 +817,7 @@ __global__ void k_fcg_mgfine(FcgArgs a, const float *z2, float *t, const float *
     const bool net = fine_net && a.fs->use_gnn, rs = a.fs->restart;
     float f0 = 0.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.g.n; i += gridDim.x * blockDim.x) {
-        const int sl = i >> 5, lane = i & 31;
-        const int base = a.g.sl_ptr[sl], wd = a.g.sl_w[sl];
-        float az = 0.f;
-        for (int k = 0; k < wd; ++k) {
-            int pos = base + k * 32 + lane;
-            az += a.g.val[pos] * z2[a.g.col[pos]];
-        }
-        const float ti = a.r[i] - az;
+        const float ti = a.r[i] - sell_dot32(a.g, i, z2);
         if (net) {
             t[i] = ti;
             const float u = a.g.dinv[i] * ti;
@@ -884,13 +900,7 @@ __global__ void k_fcg_dir(FcgArgs a) {
     const float bf = (float)beta;
     float f0 = 0.f, f1 = 0.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.g.n; i += gridDim.x * blockDim.x) {
-        const int sl = i >> 5, lane = i & 31;
-        const int base = a.g.sl_ptr[sl], w = a.g.sl_w[sl];
-        float az = 0.f;
-        for (int k = 0; k < w; ++k) {
-            int pos = base + k * 32 + lane;
-            az += a.g.val[pos] * a.z[a.g.col[pos]];
-        }
+        const float az = sell_dot32(a.g, i, a.z);
         float qi = rs ? az : az - bf * a.q[i];
         float pi = rs ? a.z[i] : a.z[i] - bf * a.p[i];
         a.q[i] = qi;
@@ -924,20 +934,44 @@ __global__ void k_fcg_dir(FcgArgs a) {
     }
 }
 
+// e += alpha p, r -= alpha q; r.r and |D^-1 r|^2.  Four rows a thread with
+// 16-byte loads (the arrays are whole allocations, 16-byte aligned): a pure
+// vector pass, where one row a thread left it at half of HBM.
+__device__ __forceinline__ void fcg_upd_row(float al, float &r, float &e, float p, float q, float d, float &f0,
+                                            float &f1) {
+    if (al != 0.f) {
+        e += al * p;
+        r -= al * q;
+    }
+    const float u = d * r;
+    f0 += r * r;
+    f1 += u * u;
+}
+
 __global__ void k_fcg_upd(FcgArgs a) {
     if (a.fs->done) return;
     const float al = (float)a.fs->alpha;
     float f0 = 0.f, f1 = 0.f;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.g.n; i += gridDim.x * blockDim.x) {
-        float ri = a.r[i];
+    const int n4 = a.g.n >> 2, T = gridDim.x * blockDim.x, t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int j = t0; j < n4; j += T) {
+        float4 r = ld4(a.r, j), e = ld4(a.e, j);
+        const float4 p = ld4(a.p, j), q = ld4(a.q, j), d = ld4(a.g.dinv, j);
+        fcg_upd_row(al, r.x, e.x, p.x, q.x, d.x, f0, f1);
+        fcg_upd_row(al, r.y, e.y, p.y, q.y, d.y, f0, f1);
+        fcg_upd_row(al, r.z, e.z, p.z, q.z, d.z, f0, f1);
+        fcg_upd_row(al, r.w, e.w, p.w, q.w, d.w, f0, f1);
         if (al != 0.f) {
-            a.e[i] += al * a.p[i];
-            ri -= al * a.q[i];
-            a.r[i] = ri;
+            st4(a.e, j, e);
+            st4(a.r, j, r);
         }
-        const float u = a.g.dinv[i] * ri;
-        f0 += ri * ri;
-        f1 += u * u;
+    }
+    for (int i = 4 * n4 + t0; i < a.g.n; i += T) {
+        float r = a.r[i], e = a.e[i];
+        fcg_upd_row(al, r, e, a.p[i], a.q[i], a.g.dinv[i], f0, f1);
+        if (al != 0.f) {
+            a.e[i] = e;
+            a.r[i] = r;
+        }
     }
     const float fv[2] = {f0, f1};
     double v[2];
