@@ -409,10 +409,12 @@ def c2_form(args):
     """Configuration 2 on the GPU (k-epsilon CHT channel, 256,000 + 51,200 cells, volumetric
     source 1e6 W/m^3 in the solid): outer iterations/s of the sequential form (the
     reference's order, FP64), of the batched scalar form (u, v, w as one 3-RHS BiCGSTAB;
-    k, eps and T as one three-matrix launch) and of the mixed-precision form (p', k, eps,
-    T and the solid T with FP32 inner iterations in FP64 defect correction), all from the
-    initial state; the mixed form's fields after the steps against the sequential
-    form's (relative L2)."""
+    k, eps and T as one three-matrix launch), of the mixed-precision form (p' by the
+    Jacobi-CG with FP32 recurrences; momentum, k, eps, T and the solid T with FP32
+    iterations and FP64 residuals) and of the multigrid form (the same with p' by the
+    multigrid flexible CG), all from the initial state, p' at the reference's
+    1000-iteration cap; the last outer iteration's p' iterations and status, and the
+    mixed forms' fields after the steps against the sequential form's (relative L2)."""
     from sysu_cfd_heat_gb300.solver import NavierStokesSolver
 
     p = c2_case_dir()
@@ -422,9 +424,10 @@ def c2_form(args):
         info = s.info()
         fields = ("U", "V", "W", "P", "T", "TE", "ED", "solid_T")
         ref = {}
+        mixed = {"scalars_batched": 0, "ke.mixed": 1, "t.mixed": 1, "ts.mixed": 1, "mom.mixed": 1}
         forms = (("sequential_fp64", {"scalars_batched": 0}), ("batched_scalars_fp64", {"scalars_batched": 1}),
-                 ("mixed_fp32_fp64", {"scalars_batched": 0, "p.mixed": 1, "ke.mixed": 1, "t.mixed": 1,
-                                      "ts.mixed": 1}))
+                 ("mixed_fp32_fp64", dict(mixed, **{"p.mixed": 1, "p.precond": 1})),
+                 ("multigrid_fp32_fp64", dict(mixed, **{"p.mixed": 0, "p.precond": 4})))
         for name, opts in forms:
             for k, v in opts.items():
                 s.set_option(k, v)
@@ -437,14 +440,16 @@ def c2_form(args):
             st = s.solve_stats()
             out[name] = {"iters_per_s": done / (ms / 1000.0), "ms_per_step": ms / done,
                          "k_eps_T_iters_last": [st["k"]["iters"][0], st["eps"]["iters"][0], st["T"]["iters"][0]],
+                         "p_iters_last": st["p"]["iters"][0], "p_status_last": st["p"]["status"][0],
                          "max_residual_after": float(max(s.Residual))}
             if name == "sequential_fp64":
                 ref = {f: s.get(f) for f in fields}
-            elif name == "mixed_fp32_fp64":
+            elif name in ("mixed_fp32_fp64", "multigrid_fp32_fp64"):
                 out[name]["field_rel_l2_vs_fp64"] = max(
                     float(np.linalg.norm(s.get(f) - ref[f]) / max(np.linalg.norm(ref[f]), 1e-300)) for f in fields)
-        for k in ("p.mixed", "ke.mixed", "t.mixed", "ts.mixed"):
+        for k in ("p.mixed", "ke.mixed", "t.mixed", "ts.mixed", "mom.mixed"):
             s.set_option(k, 0)
+        s.set_option("p.precond", 1)
         out["cells"] = {"fluid": info["Ncel"], "solid": info["solid_Ncel"]}
         out["steps"] = steps
     return out
