@@ -359,7 +359,22 @@ def batch_form(args):
         ms_m = b.replay(args.steps)
         b.check()
         err_m = max(float(np.linalg.norm(c.get("U") - u) / max(np.linalg.norm(u), 1e-300)) for c, u in zip(b.cases, u64))
+        # p' by the multigrid flexible CG as well (each case's hierarchy built in the
+        # capture's eager iteration; both solves loop on the device inside the graph)
         for c in b.cases:
+            c.set_option("p.mixed", 0)
+            c.set_option("p.precond", 4)
+            c.reset()
+        b.capture()
+        b.replay(args.warmup)
+        for c in b.cases:
+            c.reset()
+        ms_g = b.replay(args.steps)
+        b.check()
+        err_g = max(float(np.linalg.norm(c.get("U") - u) / max(np.linalg.norm(u), 1e-300)) for c, u in zip(b.cases, u64))
+        for c in b.cases:
+            c.set_option("p.precond", 1)
+            c.set_option("p.mixed", 1)
             c.set_option("mom.mixed", 0)
         b.set_caps([0] * len(cases))
         for c in b.cases:
@@ -379,9 +394,15 @@ def batch_form(args):
             "precision": "momentum BiCGSTAB FP64, p' CG FP32 recurrences + FP64 reliable updates, eps 1e-8",
             "fp32_momentum_too": {"ms_per_batch_iteration": ms_m / args.steps,
                                   "speedup_vs_sequential": seq_ms / ms_m if ms_m > 0 else None,
-                                  "precision": "momentum BiCGSTAB with FP32 inner iterations in FP64 defect "
-                                               "correction (u, v, w one after another), p' as above",
+                                  "precision": "momentum u, v, w by one BiCGSTAB with FP32 recurrences + FP64 "
+                                               "residual replacement (its loop a WHILE node of the graph), p' as above",
                                   "U_rel_l2_vs_fp64_momentum_max_over_cases": err_m},
+            "multigrid_pressure_too": {"ms_per_batch_iteration": ms_g / args.steps,
+                                       "speedup_vs_sequential": seq_ms / ms_g if ms_g > 0 else None,
+                                       "precision": "momentum as fp32_momentum_too, p' by flexible CG (FP32 "
+                                                    "recurrences + FP64 reliable updates) with the aggregation-"
+                                                    "multigrid cycle, its loop a WHILE node of the graph",
+                                       "U_rel_l2_vs_fp64_momentum_max_over_cases": err_g},
             "autotuner": {"candidates_sms": list(DEFAULT_CAPS), "sm_cap": tune["sm_cap"],
                           "measured_makespan_ms": tune["measured_makespan_ms"], "seconds": tune_s},
             "mesh_generation_seconds": gen_s}

@@ -17,7 +17,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libsysucfd.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SRCS = ["krylov.cu", "cg.cu", "gmres.cu", "fv.cu", "noalloc.cu", "gnn.cu", "amg.cu", "bicg3.cu"]
+CU_SRCS = ["krylov.cu", "cg.cu", "gmres.cu", "fv.cu", "noalloc.cu", "gnn.cu", "amg.cu", "bicg3.cu", "graph_loop.cu"]
 CPP_SRCS = ["case.cpp", "solver.cpp", "capi.cpp", "csr_api.cpp", "laspack_gpu.cpp", "output.cpp",
             "gnn_api.cpp", "batch.cpp", "amg_setup.cpp"]
 

@@ -131,6 +131,8 @@ class AggMultigrid {
     float sgn() const { return sgn_; }
     const float *w0() const { return lv_[0]->w.get(); }
     int err_flag(cudaStream_t st);  // nonzero if a bounded wait or the inverse failed
+    // the same flag in device memory (0 until set), for reading with other results
+    const int *err_dev() const { return err_.get(); }
 
   private:
     struct View;

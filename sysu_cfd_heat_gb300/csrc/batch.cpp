@@ -177,10 +177,8 @@ void CaseBatch::capture() {
         cudaGraphExecDestroy(exec_);
         exec_ = nullptr;
     }
-    // every allocation and one-time set-up happens in an eager iteration, in the
-    // solve forms that the graph will hold
+    // every allocation and one-time set-up happens in an eager iteration
     for (int k = 0; k < size(); ++k) {
-        at(k).graph_form = true;
         at(k).enqueue_iteration();
         at(k).sync();
         at(k).reset();

@@ -31,6 +31,7 @@
 // a CUDA graph of CH iterations; kernels of finished solves return at once.
 #include <cstring>
 
+#include "graph_loop.hpp"
 #include "krylov_dev.cuh"
 
 namespace sysu {
@@ -44,6 +45,8 @@ struct M3State {
     double rho[3], rho_prev[3], alpha[3], omg[3], beta[3], rref[3];
     int it[3], status[3], done[3], need[3], restart[3], skip[3], early[3], upd[3], stall[3];
     int all_done, any_need, maxit;
+    int loops;    // graph loop: bodies run (the loop's bound)
+    int stalled;  // a component handed to the FP64 solve
     double d2;
     // arrival count of grid_sums: the phases run one after another on one
     // stream, and the last block resets it before its kernel ends
@@ -484,9 +487,10 @@ __global__ void __launch_bounds__(MB) k_m3_flush(M3Args a, int final) {
     }
 }
 
-// statistics; after_fp64: the FP64 solve that finished stalled components
-// wrote its own, and the FP32 iterations are added to its counts
-__global__ void k_m3_info(const M3State *S, SolveInfo *info, int after_fp64) {
+// statistics, and whether a component stalled; after_fp64: the FP64 solve that
+// finished stalled components wrote its own, and the FP32 iterations are added
+// to its counts
+__global__ void k_m3_info(M3State *S, SolveInfo *info, int after_fp64) {
     for (int c = 0; c < 3; ++c) {
         if (after_fp64) {
             info->iters[c] += S->it[c];
@@ -499,10 +503,25 @@ __global__ void k_m3_info(const M3State *S, SolveInfo *info, int after_fp64) {
         info->res[c] = sqrt(S->rr64[c] / S->bb[c]);
     }
     info->refinements = S->upd[0] + S->upd[1] + S->upd[2];
-    if (!after_fp64) info->err = 0;
+    if (!after_fp64) {
+        info->err = 0;
+        S->stalled = S->status[0] == DEV_STALLED || S->status[1] == DEV_STALLED || S->status[2] == DEV_STALLED;
+    }
 }
 
 }  // namespace
+
+// Everything a captured solve bakes in: kernel arguments, grids, the scalars
+// the set-up kernels take and the FP64 fallback's buffers.
+struct M3Key {
+    M3Args a;
+    int g[8];
+    int maxit, jacobi, sm_cap;
+    double eps, d2, omega;
+    long nnz;
+    SolveInfo *info;
+    const void *wbuf[10];
+};
 
 struct Bicg3Mixed::Impl {
     DevBuf<float4> r, rtd, p, v, s, t, e;
@@ -511,10 +530,9 @@ struct Bicg3Mixed::Impl {
     DevBuf<M3State> st;
     DevBuf<double> part;
     int n = 0;
-    int g[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // grid of each kernel: init, replace, dir, av, s, at, upd, flush
-    cudaGraphExec_t exec = nullptr;
+    cudaGraphExec_t exec = nullptr;  // the whole solve, for streams that are not capturing
     long launches = 0;
-    M3Args key{};
+    M3Key key{};
     ~Impl() {
         if (exec) cudaGraphExecDestroy(exec);
     }
@@ -522,6 +540,61 @@ struct Bicg3Mixed::Impl {
 
 Bicg3Mixed::Bicg3Mixed() : d_(new Impl) {}
 Bicg3Mixed::~Bicg3Mixed() { delete d_; }
+
+// The solve as stream work on st (capturing): the FP32 set-up, the iterations
+// as a graph WHILE node (CH iterations a body; the body's last kernel ends the
+// loop once every component is done, or after a bound of bodies -- each
+// iteration counts towards maxit and a component stalls after three
+// replacements without progress, so the bound is never what ends a solve), and
+// the FP64 solve of stalled components as an IF node.
+static void m3_enqueue(const M3Key &k, const SellDev &A, const double *val, const double *const *b, double *const *x,
+                       const KrylovOpts &o, KrylovWork &w, cudaStream_t st) {
+    const M3Args &a = k.a;
+    const int n = a.n;
+    const int *g = k.g;
+    SYSU_CUDA(cudaMemsetAsync(a.st, 0, sizeof(M3State), st));
+    // FP32 Jacobi weights and column-scaled matrix (FP64 would take a division per
+    // row and a product per entry on the 1/64-rate FP64 pipe: 78 us of 2M rows)
+    k_m3_dinv<<<(n + MB - 1) / MB, MB, 0, st>>>(a, (float)k.omega, k.jacobi);
+    if (k.nnz > 0) k_m3_scale<<<(unsigned)((k.nnz + MB - 1) / MB), MB, 0, st>>>(a, k.nnz);
+    k_m3_init<<<g[0], MB, 0, st>>>(a, k.maxit, k.eps, k.d2);
+    k_m3_replace<<<g[1], MB, 0, st>>>(a, 1);
+    g_launches += k.nnz > 0 ? 4 : 3;
+    SYSU_CUDA(cudaGetLastError());
+    cudaStream_t side = graph_side_stream();
+    const int bound = k.maxit / CH + 8;
+    cudaGraphConditionalHandle loop = graph_cond_handle(st, 1);
+    graph_cond_node(st, side, loop, cudaGraphCondTypeWhile, [&](cudaStream_t s) {
+        for (int it = 0; it < CH; ++it) {
+            k_m3_dir<<<g[2], MB, 0, s>>>(a);
+            k_m3_av<<<g[3], MB, 0, s>>>(a);
+            k_m3_s<<<g[4], MB, 0, s>>>(a);
+            k_m3_at<<<g[5], MB, 0, s>>>(a);
+            k_m3_upd<<<g[6], MB, 0, s>>>(a);
+            k_m3_flush<<<g[7], MB, 0, s>>>(a, 0);
+            k_m3_replace<<<g[1], MB, 0, s>>>(a, 0);
+        }
+        g_launches += 7 * CH;
+        SYSU_CUDA(cudaGetLastError());
+        graph_loop_tail(loop, &a.st->all_done, &a.st->loops, bound, s);
+    });
+    // e of a component that the loop bound left unfinished (returns at once when
+    // every component ended at a replacement)
+    k_m3_flush<<<g[7], MB, 0, st>>>(a, 1);
+    k_m3_info<<<1, 1, 0, st>>>(a.st, k.info, 0);
+    g_launches += 2;
+    SYSU_CUDA(cudaGetLastError());
+    cudaGraphConditionalHandle fb = graph_cond_handle(st, 0);
+    graph_if_flag(fb, &a.st->stalled, st);
+    graph_cond_node(st, side, fb, cudaGraphCondTypeIf, [&](cudaStream_t s) {
+        // the FP64 batched solve from the current x (components already below eps
+        // take no iteration), then the FP32 iterations added to its counts
+        bicgstab_solve(A, val, 3, b, x, o, w, k.info, s);
+        k_m3_info<<<1, 1, 0, s>>>(a.st, k.info, 1);
+        ++g_launches;
+        SYSU_CUDA(cudaGetLastError());
+    });
+}
 
 void Bicg3Mixed::solve(const SellDev &A, const double *val, const double *const *b, double *const *x,
                        const KrylovOpts &o, KrylovWork &w, SolveInfo *info, cudaStream_t st) {
@@ -547,19 +620,19 @@ void Bicg3Mixed::solve(const SellDev &A, const double *val, const double *const 
         res[6] = coresident_blocks(k_m3_upd, MB);
         res[7] = coresident_blocks(k_m3_flush, MB);
     }
-    int g[8], gmax = 1;
-    for (int k = 0; k < 8; ++k) {
-        int b = res[k];
-        if (w.sm_cap > 0) b = std::min(b, w.sm_cap * std::max(1, res[k] / num_sms()));
-        g[k] = std::max(1, std::min((n + MB - 1) / MB, b));
-        gmax = std::max(gmax, g[k]);
+    M3Key k;
+    std::memset(&k, 0, sizeof(k));  // padding too: the key is compared as bytes
+    int gmax = 1;
+    for (int j = 0; j < 8; ++j) {
+        int nb = res[j];
+        if (w.sm_cap > 0) nb = std::min(nb, w.sm_cap * std::max(1, res[j] / num_sms()));
+        k.g[j] = std::max(1, std::min((n + MB - 1) / MB, nb));
+        gmax = std::max(gmax, k.g[j]);
     }
     if (d.part.size() < (size_t)gmax * 9) d.part.alloc((size_t)gmax * 9);
     if (d.sv32.size() < (size_t)A.nnz) d.sv32.alloc(A.nnz);
-    SYSU_CUDA(cudaMemsetAsync(d.st.get(), 0, sizeof(M3State), st));
-
-    M3Args a;
-    std::memset(&a, 0, sizeof(a));  // padding too: the graph key compares bytes
+    bicgstab_prepare(A, 3, w, st);  // the FP64 fallback's scratch, ahead of any capture
+    M3Args &a = k.a;
     a.n = n;
     a.sl_ptr = A.sl_ptr.get();
     a.sl_w = A.sl_w.get();
@@ -576,62 +649,45 @@ void Bicg3Mixed::solve(const SellDev &A, const double *val, const double *const 
     a.e = d.e.get();
     a.st = d.st.get();
     a.part = d.part.get();
-    // FP32 Jacobi weights and column-scaled matrix (FP64 would take a division per
-    // row and a product per entry on the 1/64-rate FP64 pipe: 78 us of 2M rows)
-    k_m3_dinv<<<(n + MB - 1) / MB, MB, 0, st>>>(a, (float)o.omega, o.jacobi ? 1 : 0);
-    if (A.nnz > 0) k_m3_scale<<<(unsigned)((A.nnz + MB - 1) / MB), MB, 0, st>>>(a, A.nnz);
-    g_launches += A.nnz > 0 ? 2 : 1;
-    k_m3_init<<<g[0], MB, 0, st>>>(a, o.maxit, o.eps, o.inner_tol * o.inner_tol);
-    k_m3_replace<<<g[1], MB, 0, st>>>(a, 1);
-    g_launches += 2;
-    SYSU_CUDA(cudaGetLastError());
-    if (!d.exec || std::memcmp(g, d.g, sizeof(g)) != 0 || std::memcmp(&a, &d.key, sizeof(M3Args)) != 0) {
+    k.maxit = o.maxit;
+    k.jacobi = o.jacobi ? 1 : 0;
+    k.sm_cap = w.sm_cap;
+    k.eps = o.eps;
+    k.d2 = o.inner_tol * o.inner_tol;
+    k.omega = o.omega;
+    k.nnz = A.nnz;
+    k.info = info;
+    const void *wb[10] = {w.r.get(), w.rt.get(), w.p.get(), w.v.get(), w.s.get(),
+                          w.t.get(), w.dinv.get(), w.partials.get(), w.sval.get(), w.barrier.get()};
+    std::memcpy(k.wbuf, wb, sizeof(wb));
+    if (stream_capturing(st)) {  // inside the caller's graph (the case batch)
+        m3_enqueue(k, A, val, b, x, o, w, st);
+        return;
+    }
+    if (!d.exec || std::memcmp(&k, &d.key, sizeof(M3Key)) != 0) {
         if (d.exec) cudaGraphExecDestroy(d.exec);
         d.exec = nullptr;
+        const long before = g_launches.load();
         cudaGraph_t graph;
         SYSU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        for (int k = 0; k < CH; ++k) {
-            k_m3_dir<<<g[2], MB, 0, st>>>(a);
-            k_m3_av<<<g[3], MB, 0, st>>>(a);
-            k_m3_s<<<g[4], MB, 0, st>>>(a);
-            k_m3_at<<<g[5], MB, 0, st>>>(a);
-            k_m3_upd<<<g[6], MB, 0, st>>>(a);
-            k_m3_flush<<<g[7], MB, 0, st>>>(a, 0);
-            k_m3_replace<<<g[1], MB, 0, st>>>(a, 0);
+        try {
+            m3_enqueue(k, A, val, b, x, o, w, st);
+        } catch (...) {
+            cudaGraph_t junk = nullptr;
+            cudaStreamEndCapture(st, &junk);
+            if (junk) cudaGraphDestroy(junk);
+            throw;
         }
         SYSU_CUDA(cudaStreamEndCapture(st, &graph));
-        SYSU_CUDA(cudaGraphInstantiate(&d.exec, graph, 0));
+        d.launches = g_launches.load() - before;
+        g_launches -= d.launches;
+        cudaError_t e = cudaGraphInstantiate(&d.exec, graph, 0);
         cudaGraphDestroy(graph);
-        d.launches = 7 * CH;
-        std::memcpy(d.g, g, sizeof(g));
-        std::memcpy(&d.key, &a, sizeof(M3Args));
+        SYSU_CUDA(e);
+        std::memcpy(&d.key, &k, sizeof(M3Key));
     }
-    // a component stalls after three replacements without progress, and each
-    // iteration counts towards maxit: the bound ends the loop in any case
-    M3State h{};
-    const long bound = (long)o.maxit + 4L * CH;
-    for (long it = 0; it < bound; it += CH) {
-        SYSU_CUDA(cudaGraphLaunch(d.exec, st));
-        g_launches += d.launches;
-        SYSU_CUDA(cudaMemcpyAsync(&h, d.st.get(), sizeof(M3State), cudaMemcpyDeviceToHost, st));
-        SYSU_CUDA(cudaStreamSynchronize(st));
-        if (h.all_done) break;
-    }
-    // e of a component that the loop bound left unfinished (returns at once
-    // when every component ended at a replacement)
-    k_m3_flush<<<g[7], MB, 0, st>>>(a, 1);
-    k_m3_info<<<1, 1, 0, st>>>(d.st.get(), info, 0);
-    g_launches += 2;
-    SYSU_CUDA(cudaGetLastError());
-    last_refinements = h.upd[0] + h.upd[1] + h.upd[2];
-    if (h.status[0] == DEV_STALLED || h.status[1] == DEV_STALLED || h.status[2] == DEV_STALLED) {
-        // the FP64 batched solve from the current x (components already below
-        // eps take no iteration), then the FP32 iterations added to its counts
-        bicgstab_solve(A, val, 3, b, x, o, w, info, st);
-        k_m3_info<<<1, 1, 0, st>>>(d.st.get(), info, 1);
-        ++g_launches;
-        SYSU_CUDA(cudaGetLastError());
-    }
+    SYSU_CUDA(cudaGraphLaunch(d.exec, st));
+    g_launches += d.launches;
 }
 
 }  // namespace sysu

@@ -20,6 +20,7 @@
 #include <random>
 
 #include "gnn.hpp"
+#include "graph_loop.hpp"
 #include "krylov_dev.cuh"
 #include "umma.cuh"
 
@@ -785,6 +786,7 @@ __global__ void k_fcg_init(FcgArgs a, int x0_zero, double eps, int maxit, int us
         f->need_update = 0;
         f->fallback_at = -1;
         f->maxit = maxit;
+        f->loops = 0;
         f->zq = f->pq = f->pq_prev = f->pr = f->alpha = 0.0;
     }
 }
@@ -1053,9 +1055,9 @@ int blocks_flat(int n) { return std::max(1, std::min((n + FB - 1) / FB, num_sms(
 }  // namespace
 
 void GnnPrecond::drop_graphs() {
-    for (ChunkGraph &g : graphs_) {
+    for (SolveGraph &g : graphs_) {
         if (g.exec) cudaGraphExecDestroy(g.exec);
-        g = ChunkGraph{};
+        g = SolveGraph{};
     }
 }
 
@@ -1106,6 +1108,10 @@ void GnnPrecond::bind(const SellDev &A, const double *val64, const float *val32,
     const size_t n = (size_t)n_;
     dinv_.alloc(n);
     refresh(st);
+    double d0 = 0.0;  // the matrix's sign (entry 0 is row 0's diagonal)
+    SYSU_CUDA(cudaMemcpyAsync(&d0, val64_, sizeof(double), cudaMemcpyDeviceToHost, st));
+    SYSU_CUDA(cudaStreamSynchronize(st));
+    sgn_ = d0 < 0.0 ? -1.0f : 1.0f;
     if (p_.size() == 0) {
         p_.alloc(GNN_NPARAM_PAD);
         m_.alloc(GNN_NPARAM_PAD);
@@ -1140,14 +1146,13 @@ void GnnPrecond::bind(const SellDev &A, const double *val64, const float *val32,
     count_ = next_ = 0;
 }
 
+// New values of the bound matrix (same pattern and the same sign convention,
+// which bind read): the Jacobi weights.  No host round trip, so a refresh can be
+// part of a captured outer iteration.
 void GnnPrecond::refresh(cudaStream_t st) {
     k_gnn_dinv<<<(n_ + FB - 1) / FB, FB, 0, st>>>(n_, A_->sl_ptr.get(), val64_, dinv_.get());
     ++g_launches;
     SYSU_CUDA(cudaGetLastError());
-    double d0 = 0.0;
-    SYSU_CUDA(cudaMemcpyAsync(&d0, val64_, sizeof(double), cudaMemcpyDeviceToHost, st));
-    SYSU_CUDA(cudaStreamSynchronize(st));
-    sgn_ = d0 < 0.0 ? -1.0f : 1.0f;
 }
 
 void GnnPrecond::refresh_bf16(cudaStream_t st) {
@@ -1457,17 +1462,31 @@ void GnnPrecond::fcg_iteration(const void *args, bool use_gnn, cudaStream_t st) 
     SYSU_CUDA(cudaGetLastError());
 }
 
+// Everything a captured flexible-CG solve bakes in: its kernels' arguments, the
+// caller's b, x and statistics pointers, the initial kernel's scalars and the
+// attached cycle's parameters.
+struct FcgKey {
+    FcgArgs a;
+    const double *b_in;
+    double *x_out;
+    SolveInfo *info;
+    int x0_zero, maxit, use_gnn, chunk, gflat, net_level, post_level, hook, mg_persistent;
+    double eps, mg_gamma;
+    float skip;
+    const void *mg;
+};
+
 void GnnPrecond::fcg(const double *b, double *x, bool x0_zero, const KrylovOpts &o, bool use_gnn, SolveInfo *info_dev,
                      cudaStream_t st) {
     if (!bound()) throw CaseError{"learned preconditioner: no matrix bound"};
-    // the iterations run from a CUDA graph over fixed buffers: b and x are copied in and out
+    // the iterations run over fixed buffers: b and x are copied in and out
     if (b64_.size() < (size_t)n_) {
         b64_.alloc(n_);
         x64_.alloc(n_);
     }
-    SYSU_CUDA(cudaMemcpyAsync(b64_.get(), b, sizeof(double) * n_, cudaMemcpyDeviceToDevice, st));
-    if (!x0_zero) SYSU_CUDA(cudaMemcpyAsync(x64_.get(), x, sizeof(double) * n_, cudaMemcpyDeviceToDevice, st));
-    FcgArgs a{};
+    FcgKey k;
+    std::memset(&k, 0, sizeof(k));  // padding too: the key is compared as bytes
+    FcgArgs &a = k.a;
     a.g = gview(*A_, val32_, dinv_.get());
     a.val64 = val64_;
     a.sgn = sgn_;
@@ -1482,51 +1501,84 @@ void GnnPrecond::fcg(const double *b, double *x, bool x0_zero, const KrylovOpts 
     a.part = part_.get();
     a.inner_tol2 = o.inner_tol * o.inner_tol;
     a.stall_max = stall_max;
-    if (x0_zero) {
-        k_fcg_zero<<<(n_ + FB - 1) / FB, FB, 0, st>>>(n_, a.x);
-        ++g_launches;
+    k.b_in = b;
+    k.x_out = x;
+    k.info = info_dev;
+    k.x0_zero = x0_zero ? 1 : 0;
+    k.maxit = o.maxit;
+    k.use_gnn = use_gnn ? 1 : 0;
+    k.chunk = check_every;
+    k.gflat = gflat_;
+    k.eps = o.eps;
+    k.skip = skip;
+    k.mg = mg_;
+    if (mg_) {
+        k.net_level = net_level;
+        k.post_level = mg_->post_level;
+        k.hook = mg_->post_hook ? 1 : 0;
+        k.mg_persistent = mg_->persistent ? 1 : 0;
+        k.mg_gamma = mg_->gamma;
     }
-    k_fcg_init<<<gflat_, FB, 0, st>>>(a, x0_zero ? 1 : 0, o.eps, o.maxit, use_gnn ? 1 : 0);
-    ++g_launches;
-    SYSU_CUDA(cudaGetLastError());
-    // (re)capture the chunk graph when its arguments changed
-    ChunkGraph &cg = graphs_[(mg_ ? 2 : 0) + (use_gnn ? 1 : 0)];
-    if (!cg.exec || cg.inner_tol != o.inner_tol || cg.stall_max != stall_max || cg.chunk != check_every ||
-        cg.val32 != val32_ || cg.dinv != dinv_.get() || cg.mg != mg_ ||
-        (mg_ && (cg.mg_gamma != mg_->gamma || cg.mg_persistent != mg_->persistent || cg.net_level != net_level))) {
-        if (cg.exec) cudaGraphExecDestroy(cg.exec);
-        cg.exec = nullptr;
-        long before = g_launches.load();
+    // b, x0 in; the iterations as a WHILE node (check_every a body; the body's last
+    // kernel ends the loop once the solve is done, or after maxit / check_every + 8
+    // bodies -- the solve stops at maxit itself); x and the statistics out
+    auto enqueue = [&](cudaStream_t s) {
+        SYSU_CUDA(cudaMemcpyAsync(b64_.get(), b, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+        if (!x0_zero) SYSU_CUDA(cudaMemcpyAsync(x64_.get(), x, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+        if (x0_zero) {
+            k_fcg_zero<<<(n_ + FB - 1) / FB, FB, 0, s>>>(n_, a.x);
+            ++g_launches;
+        }
+        k_fcg_init<<<gflat_, FB, 0, s>>>(a, x0_zero ? 1 : 0, o.eps, o.maxit, use_gnn ? 1 : 0);
+        ++g_launches;
+        SYSU_CUDA(cudaGetLastError());
+        const int bound = o.maxit / std::max(1, check_every) + 8;
+        cudaGraphConditionalHandle loop = graph_cond_handle(s, 1);
+        graph_cond_node(s, graph_side_stream(), loop, cudaGraphCondTypeWhile, [&](cudaStream_t bs) {
+            for (int c = 0; c < check_every; ++c) fcg_iteration(&a, use_gnn, bs);
+            graph_loop_tail(loop, &a.fs->done, &a.fs->loops, bound, bs);
+        });
+        SYSU_CUDA(cudaMemcpyAsync(x, x64_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+        k_fcg_info<<<1, 1, 0, s>>>(fs_.get(), info_dev);
+        ++g_launches;
+        SYSU_CUDA(cudaGetLastError());
+    };
+    if (stream_capturing(st)) {  // inside the caller's graph: errors surface in the statuses
+        enqueue(st);
+        return;
+    }
+    const unsigned char *kb = reinterpret_cast<const unsigned char *>(&k);
+    SolveGraph *sg = nullptr;
+    for (SolveGraph &g : graphs_)
+        if (g.exec && g.key.size() == sizeof(k) && std::memcmp(g.key.data(), kb, sizeof(k)) == 0) sg = &g;
+    if (!sg) {
+        sg = &graphs_[graph_next_];
+        graph_next_ = (graph_next_ + 1) % 4;
+        if (sg->exec) cudaGraphExecDestroy(sg->exec);
+        *sg = SolveGraph{};
+        const long before = g_launches.load();
         cudaGraph_t g;
         SYSU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        for (int c = 0; c < check_every; ++c) fcg_iteration(&a, use_gnn, st);
+        try {
+            enqueue(st);
+        } catch (...) {
+            cudaGraph_t junk = nullptr;
+            cudaStreamEndCapture(st, &junk);
+            if (junk) cudaGraphDestroy(junk);
+            throw;
+        }
         SYSU_CUDA(cudaStreamEndCapture(st, &g));
-        cg.launches = g_launches.load() - before;
-        g_launches -= cg.launches;
-        SYSU_CUDA(cudaGraphInstantiate(&cg.exec, g, 0));
+        sg->launches = g_launches.load() - before;
+        g_launches -= sg->launches;
+        cudaError_t e = cudaGraphInstantiate(&sg->exec, g, 0);
         cudaGraphDestroy(g);
-        cg.inner_tol = o.inner_tol;
-        cg.stall_max = stall_max;
-        cg.chunk = check_every;
-        cg.val32 = val32_;
-        cg.dinv = dinv_.get();
-        cg.mg = mg_;
-        cg.mg_gamma = mg_ ? mg_->gamma : 0.0;
-        cg.mg_persistent = mg_ ? mg_->persistent : false;
-        cg.net_level = net_level;
+        SYSU_CUDA(e);
+        sg->key.assign(kb, kb + sizeof(k));
     }
-    int done = 0;
-    for (int it = 0; it < o.maxit && !done; it += check_every) {
-        SYSU_CUDA(cudaGraphLaunch(cg.exec, st));
-        g_launches += cg.launches;
-        SYSU_CUDA(cudaMemcpyAsync(&done, &fs_.get()->done, sizeof(int), cudaMemcpyDeviceToHost, st));
-        SYSU_CUDA(cudaStreamSynchronize(st));
-    }
-    SYSU_CUDA(cudaMemcpyAsync(x, x64_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, st));
-    k_fcg_info<<<1, 1, 0, st>>>(fs_.get(), info_dev);
-    ++g_launches;
-    SYSU_CUDA(cudaGetLastError());
-    check_err(st);
+    SYSU_CUDA(cudaGraphLaunch(sg->exec, st));
+    g_launches += sg->launches;
+    // a network that timed out on a tensor-core wait (the plain cycle sets nothing)
+    if (use_gnn || (mg_ && mg_->post_hook)) check_err(st);
 }
 
 GnnPrecond::~GnnPrecond() { drop_graphs(); }

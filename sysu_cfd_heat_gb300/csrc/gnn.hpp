@@ -45,6 +45,7 @@ struct FcgState {
     double zq, pq, pq_prev, pr, alpha;
     double res;
     int iters, refinements, done, status, use_gnn, stall, restart, need_update, fallback_at, maxit;
+    int loops;  // graph loop: bodies run (the loop's bound)
     float inv_s, s;
     float inv_s2, s2;  // multigrid form: scale of the post-smoother's input
     unsigned cnt[4];
@@ -155,20 +156,16 @@ class GnnPrecond {
     void check_err(cudaStream_t st);
     void fcg_iteration(const void *args, bool use_gnn, cudaStream_t st);
 
-    // a captured chunk of check_every flexible-CG iterations
-    // (index: 2 * multigrid attached + network on)
-    struct ChunkGraph {
+    // A whole flexible-CG solve captured as a graph (its iterations a WHILE
+    // node, graph_loop.hpp), for streams that are not capturing; the four most
+    // recent argument sets (the bytes of everything the capture bakes in) are kept.
+    struct SolveGraph {
         cudaGraphExec_t exec = nullptr;
-        double inner_tol = 0.0;
-        int stall_max = 0, chunk = 0;
         long launches = 0;
-        const float *val32 = nullptr, *dinv = nullptr;
-        const AggMultigrid *mg = nullptr;
-        double mg_gamma = 0.0;  // a kernel argument of the captured cycle
-        bool mg_persistent = false;
-        int net_level = 0;
+        std::vector<unsigned char> key;
     };
-    ChunkGraph graphs_[4];
+    SolveGraph graphs_[4];
+    int graph_next_ = 0;
     void drop_graphs();
     void transform_pair(int k, cudaStream_t st);
 

@@ -1086,6 +1086,12 @@ static void bicg_launch(const SellDev &A, const double *const *vals, bool multi,
     ++::sysu::g_launches;
 }
 
+void bicgstab_prepare(const SellDev &A, int nrhs, KrylovWork &w, cudaStream_t st) {
+    if (A.n == 0) return;
+    w.ensure(A.n, nrhs == 1 ? 1 : 3, bicg_max_blocks(-1, false), st);
+    if (w.sval.size() < (size_t)A.nnz) w.sval.alloc(A.nnz);
+}
+
 void bicgstab_solve(const SellDev &A, const double *val, int nrhs, const double *const *b, double *const *x,
                     const KrylovOpts &o, KrylovWork &w, SolveInfo *info, cudaStream_t st) {
     if (A.n == 0) return;

@@ -136,6 +136,10 @@ void cg_solve_mixed(const SellDev &A, const double *val, const float *val32, con
 void cg_solve(const SellDev &A, const double *val, const double *b, double *x, bool x0_zero,
               const KrylovOpts &o, KrylovWork &w, SolveInfo *info_dev, cudaStream_t st);
 
+// The scratch bicgstab_solve needs for nrhs right-hand sides of one matrix,
+// allocated ahead (a solve captured into a graph must not allocate).
+void bicgstab_prepare(const SellDev &A, int nrhs, KrylovWork &w, cudaStream_t st);
+
 // BiCGSTAB on nrhs (1..3) right-hand sides sharing one matrix; b[c], x[c].
 void bicgstab_solve(const SellDev &A, const double *val, int nrhs, const double *const *b, double *const *x,
                     const KrylovOpts &o, KrylovWork &w, SolveInfo *info_dev, cudaStream_t st);
@@ -154,9 +158,10 @@ void bicgstab_solve_mixed(const SellDev &A, const double *val, const double *b, 
 // each component on ||b - A x|| / ||b|| < eps.  A component whose replacements
 // stop lowering that residual is finished by the FP64 batched BiCGSTAB from its
 // x.  Per-component status, iterations (FP32) and residual in info; refinements
-// = replacements summed over the components.  Iterations run from a captured
-// CUDA graph (recaptured when the arguments change); the host reads the state
-// once per graph.
+// = replacements summed over the components.  The solve never waits for the
+// host: its iterations are a WHILE node of a CUDA graph (graph_loop.hpp), so on
+// a stream being captured it joins the caller's graph, and otherwise it runs as
+// its own graph (captured once, again when its arguments change).
 class Bicg3Mixed {
   public:
     Bicg3Mixed();
@@ -165,7 +170,6 @@ class Bicg3Mixed {
     Bicg3Mixed &operator=(const Bicg3Mixed &) = delete;
     void solve(const SellDev &A, const double *val, const double *const *b, double *const *x, const KrylovOpts &o,
                KrylovWork &w, SolveInfo *info_dev, cudaStream_t st);
-    int last_refinements = 0;
 
   private:
     struct Impl;

@@ -2,6 +2,7 @@
 // one stream; the only host synchronisation per outer iteration is the read
 // of the residual monitor and the solve status words in check_iteration().
 #include "solver.hpp"
+#include "graph_loop.hpp"
 
 #include <sys/stat.h>
 
@@ -448,19 +449,16 @@ void SimpleSolver::solve(int slot, const EqOpts &o, const SellDev &A, const doub
             bicgstab_solve_mixed(A, val, b[0], x[0], ko, kw, info, st);
             return;
         }
-        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-        SYSU_CUDA(cudaStreamIsCapturing(st, &cap));
-        if (nrhs == 3 && opt.mom_batched && !graph_form && cap == cudaStreamCaptureStatusNone) {
-            // momentum: u, v, w together, FP32 recurrences with FP64 residual replacement
+        if (nrhs == 3 && opt.mom_batched) {
+            // momentum: u, v, w together, FP32 recurrences with FP64 residual
+            // replacement (graph-resident: also inside a captured outer iteration)
             mom3.solve(A, val, b, x, ko, kw, info, st);
             mom_split = false;
             return;
         }
-        // momentum unbatched, or in an outer iteration captured into a graph (a
-        // graph cannot wait for the host, which the batched form does between its
-        // chunks; the eager iteration before the capture allocates for this form): u,
-        // v, w one after another, each a persistent solve with FP32 inner
-        // iterations in FP64 defect correction (statistics per component)
+        // momentum unbatched: u, v, w one after another, each a persistent solve
+        // with FP32 inner iterations in FP64 defect correction (statistics per
+        // component)
         for (int c = 0; c < nrhs; ++c) bicgstab_solve_mixed(A, val, b[c], x[c], ko, kw, infos.get() + SLOT_N + c, st);
         return;
     }
@@ -548,17 +546,15 @@ void SimpleSolver::solve_learned(const EqOpts &o, const double *val, const doubl
     ko.omega = o.omega;
     ko.jacobi = true;
     ko.inner_tol = o.inner_tol;
-    auto mg_check = [&] {
-        if (use_mg && mg.err_flag(st)) throw CaseError{"p' multigrid: a bounded wait timed out or the coarsest level is singular"};
-    };
+    // the multigrid's error flag (a bounded wait timed out, the coarsest level is
+    // singular) is read with the outer iteration's other results (check_iteration)
     if (!o.learned) {
         gnn.fcg(b, x, x0_zero, ko, false, info, st);
-        mg_check();
         return;
     }
+    if (stream_capturing(st)) throw CaseError{"the learned p' form trains on the host's schedule: not in a captured graph"};
     if (p_solves++ >= o.learn_iters) {
         gnn.fcg(b, x, x0_zero, ko, true, info, st);
-        mg_check();
         return;
     }
     auto plain = [&](double eps, bool zero) {
@@ -963,10 +959,13 @@ std::string SimpleSolver::check_iteration() {
     SolveInfo h[SLOT_N + 3];
     double ro[RED_NSLOT];
     int hf = 0;
+    int mgerr = 0;
     infos.download(h, SLOT_N + 3, st);
     red_out.download(ro, RED_NSLOT, st);
     flags.download(&hf, 1, st);
+    if (mg.ready()) SYSU_CUDA(cudaMemcpyAsync(&mgerr, mg.err_dev(), sizeof(int), cudaMemcpyDeviceToHost, st));
     SYSU_CUDA(cudaStreamSynchronize(st));
+    if (mgerr) throw CaseError{"p' multigrid: a bounded wait timed out or the coarsest level is singular"};
     if (mom_split)
         for (int c = 0; c < 3; ++c) {
             h[SLOT_MOM].status[c] = h[SLOT_N + c].status[0];

@@ -156,9 +156,6 @@ class SimpleSolver {
     // level's own solves that give its training pairs), scratch
     Bicg3Mixed mom3;            // momentum with FP32 recurrences (options mom.mixed + mom_batched)
     bool mom_split = false;     // the last momentum solve left per-component statistics (SLOT_N + c)
-    // the outer iteration is (or is about to be) captured into a CUDA graph: the
-    // solves take forms that never wait for the host (set by the case batch)
-    bool graph_form = false;
     GnnPrecond gnn_c;
     AggMultigrid mg_c;
     int learn_level_built = -1;

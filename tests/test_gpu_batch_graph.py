@@ -48,10 +48,10 @@ def test_graph_replay_equals_cases_alone():
 
 
 def test_graph_replay_with_mixed_momentum():
-    """Option mom.mixed inside a captured outer iteration: the graph cannot wait
-    for the host, so u, v, w run as three persistent mixed solves there -- the
-    fields equal those of each case alone in that (unbatched) form, and stay
-    within the solve tolerance of the batched mixed form used outside graphs."""
+    """Option mom.mixed inside a captured outer iteration: the momentum solve's
+    iterations are a WHILE node of the batch's graph (no host round trip); the
+    fields equal those of each case alone with the same SM cap, and stay within the
+    solve tolerance of the unbatched mixed form (u, v, w one after another)."""
     spec = [(6, 100.0), (9, 400.0)]
     iters = 8
     opts = dict(OPTS, **{"mom.mixed": 1})
@@ -67,12 +67,40 @@ def test_graph_replay_with_mixed_momentum():
                 st = s.solve_stats()["mom"]
                 assert st["status"] == [0, 0, 0] and min(st["iters"]) > 0, st
         for k, p in enumerate(params):
-            with NavierStokesSolver(p, dict(opts, sm_cap=[2, 4][k], mom_batched=0)) as s:
+            with NavierStokesSolver(p, dict(opts, sm_cap=[2, 4][k])) as s:
                 assert s.iterate(iters) == iters
                 for f in ("U", "V", "W", "P"):
                     assert np.array_equal(s.get(f), got[k][f]), (k, f)
-            with NavierStokesSolver(p, opts) as s:
+            with NavierStokesSolver(p, dict(opts, mom_batched=0)) as s:
                 s.iterate(iters)
                 for f in ("U", "V", "W", "P"):
                     a = s.get(f)
                     assert np.linalg.norm(a - got[k][f]) <= 1e-6 * np.linalg.norm(a) + 1e-14, (k, f)
+
+
+def test_graph_replay_with_multigrid_pressure():
+    """p' by the multigrid flexible CG (option p.precond 4) and mixed momentum inside
+    the batch's graph: both solves loop on the device (WHILE nodes), the hierarchy is
+    built in the eager iteration before the capture; the fields equal those of each
+    case alone with the same SM cap."""
+    spec = [(7, 100.0), (10, 400.0), (12, 900.0)]
+    iters = 6
+    opts = dict(OPTS, **{"mom.mixed": 1, "p.precond": 4, "p.mixed": 0})
+    with tempfile.TemporaryDirectory() as d:
+        params = _cases(d, spec)
+        caps = [2, 4, 2]
+        with CaseBatch(params, opts) as b:
+            b.set_caps(caps)
+            b.capture()
+            b.replay(iters)
+            b.check()
+            got = [{f: s.get(f) for f in ("U", "V", "W", "P")} for s in b.cases]
+            for s in b.cases:
+                st = s.solve_stats()
+                assert st["p"]["status"][0] == 0 and st["p"]["iters"][0] > 0, st["p"]
+                assert st["mom"]["status"] == [0, 0, 0], st["mom"]
+        for k, p in enumerate(params):
+            with NavierStokesSolver(p, dict(opts, sm_cap=caps[k])) as s:
+                assert s.iterate(iters) == iters
+                for f in ("U", "V", "W", "P"):
+                    assert np.array_equal(s.get(f), got[k][f]), (k, f)
