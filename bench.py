@@ -726,6 +726,8 @@ def probe_p(args) -> dict:
 
     forms = {name: opts for name, opts, _ in P_FORMS}
     opts = dict(forms[args.probe_p])
+    if args.host_loops:
+        opts["graph_loops"] = 0  # per-kernel profiling: profilers skip kernels of graphs with conditional nodes
     with NavierStokesSolver(case_dir(args.workload), dict({"rtc": RTC, "timing": 1, "p.maxit": 100000}, **opts)) as s:
         if opts.get("p.learned"):
             s.set_option("p.learn_iters", LEARN_ITERS)
@@ -935,6 +937,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the 48-cavity batch form")
     ap.add_argument("--learned-c5", action="store_true",
                     help="only the configuration-5 learned-preconditioner run (4.9 M cells; minutes)")
+    ap.add_argument("--host-loops", action="store_true",
+                    help="with --probe-p: the host drives the solves' loops (for per-kernel ncu captures)")
     ap.add_argument("--probe-p", default=None, choices=[f for f, _, _ in P_FORMS],
                     help="only one p' solve of the given form after its set-up (profiling runs)")
     ap.add_argument("--cpu-survey", action="store_true",

@@ -101,6 +101,10 @@ int sysu_solver_info(sysu_solver *s, long *out, int n);
  *   "sm_cap" (SMs' worth of blocks the persistent Krylov solves may use, 0 = all;
  *     set per case by the batch autotuner);
  *   "rtc" sets every eq's eps; "mom_batched" (1: u,v,w as one 3-RHS solve);
+ *   "graph_loops" (1, default: the mixed momentum and the multigrid p' solves
+ *     loop on the device as CUDA graph WHILE nodes, which lets them run inside a
+ *     captured graph; 0: the host drives those loops -- for per-kernel profiling,
+ *     since profilers skip the kernels of graphs with conditional nodes);
  *   "solid_source" (W/m^3, an extension); "fatal_checks"; "timing". */
 int sysu_solver_set_option(sysu_solver *s, const char *key, double value);
 int sysu_solver_get_option(sysu_solver *s, const char *key, double *value);

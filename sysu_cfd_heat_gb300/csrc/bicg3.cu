@@ -541,59 +541,79 @@ struct Bicg3Mixed::Impl {
 Bicg3Mixed::Bicg3Mixed() : d_(new Impl) {}
 Bicg3Mixed::~Bicg3Mixed() { delete d_; }
 
-// The solve as stream work on st (capturing): the FP32 set-up, the iterations
-// as a graph WHILE node (CH iterations a body; the body's last kernel ends the
-// loop once every component is done, or after a bound of bodies -- each
-// iteration counts towards maxit and a component stalls after three
-// replacements without progress, so the bound is never what ends a solve), and
-// the FP64 solve of stalled components as an IF node.
-static void m3_enqueue(const M3Key &k, const SellDev &A, const double *val, const double *const *b, double *const *x,
-                       const KrylovOpts &o, KrylovWork &w, cudaStream_t st) {
+// Stream work of a solve, in pieces: the FP32 set-up; CH iterations; after the
+// iterations, the unfinished components' flush and the statistics (which also
+// record whether a component stalled); the FP64 solve of stalled components.
+static void m3_setup(const M3Key &k, cudaStream_t st) {
     const M3Args &a = k.a;
     const int n = a.n;
-    const int *g = k.g;
     SYSU_CUDA(cudaMemsetAsync(a.st, 0, sizeof(M3State), st));
     // FP32 Jacobi weights and column-scaled matrix (FP64 would take a division per
     // row and a product per entry on the 1/64-rate FP64 pipe: 78 us of 2M rows)
     k_m3_dinv<<<(n + MB - 1) / MB, MB, 0, st>>>(a, (float)k.omega, k.jacobi);
     if (k.nnz > 0) k_m3_scale<<<(unsigned)((k.nnz + MB - 1) / MB), MB, 0, st>>>(a, k.nnz);
-    k_m3_init<<<g[0], MB, 0, st>>>(a, k.maxit, k.eps, k.d2);
-    k_m3_replace<<<g[1], MB, 0, st>>>(a, 1);
+    k_m3_init<<<k.g[0], MB, 0, st>>>(a, k.maxit, k.eps, k.d2);
+    k_m3_replace<<<k.g[1], MB, 0, st>>>(a, 1);
     g_launches += k.nnz > 0 ? 4 : 3;
     SYSU_CUDA(cudaGetLastError());
+}
+
+static void m3_chunk(const M3Key &k, cudaStream_t s) {
+    const M3Args &a = k.a;
+    const int *g = k.g;
+    for (int it = 0; it < CH; ++it) {
+        k_m3_dir<<<g[2], MB, 0, s>>>(a);
+        k_m3_av<<<g[3], MB, 0, s>>>(a);
+        k_m3_s<<<g[4], MB, 0, s>>>(a);
+        k_m3_at<<<g[5], MB, 0, s>>>(a);
+        k_m3_upd<<<g[6], MB, 0, s>>>(a);
+        k_m3_flush<<<g[7], MB, 0, s>>>(a, 0);
+        k_m3_replace<<<g[1], MB, 0, s>>>(a, 0);
+    }
+    g_launches += 7 * CH;
+    SYSU_CUDA(cudaGetLastError());
+}
+
+static void m3_finish(const M3Key &k, cudaStream_t st) {
+    // e of a component that the loop bound left unfinished (returns at once when
+    // every component ended at a replacement)
+    k_m3_flush<<<k.g[7], MB, 0, st>>>(k.a, 1);
+    k_m3_info<<<1, 1, 0, st>>>(k.a.st, k.info, 0);
+    g_launches += 2;
+    SYSU_CUDA(cudaGetLastError());
+}
+
+static void m3_fp64(const M3Key &k, const SellDev &A, const double *val, const double *const *b, double *const *x,
+                    const KrylovOpts &o, KrylovWork &w, cudaStream_t s) {
+    // the FP64 batched solve from the current x (components already below eps take
+    // no iteration), then the FP32 iterations added to its counts
+    bicgstab_solve(A, val, 3, b, x, o, w, k.info, s);
+    k_m3_info<<<1, 1, 0, s>>>(k.a.st, k.info, 1);
+    ++g_launches;
+    SYSU_CUDA(cudaGetLastError());
+}
+
+// The solve as stream work on st (capturing): the set-up, the iterations as a
+// graph WHILE node (the body's last kernel ends the loop once every component is
+// done, or after a bound of bodies -- each iteration counts towards maxit and a
+// component stalls after three replacements without progress, so the bound is
+// never what ends a solve), the finish, and the FP64 solve of stalled
+// components as an IF node.
+static void m3_enqueue(const M3Key &k, const SellDev &A, const double *val, const double *const *b, double *const *x,
+                       const KrylovOpts &o, KrylovWork &w, cudaStream_t st) {
+    m3_setup(k, st);
     cudaStream_t side = graph_side_stream();
     const int bound = k.maxit / CH + 8;
     cudaGraphConditionalHandle loop = graph_cond_handle(st, 1);
     graph_cond_node(st, side, loop, cudaGraphCondTypeWhile, [&](cudaStream_t s) {
-        for (int it = 0; it < CH; ++it) {
-            k_m3_dir<<<g[2], MB, 0, s>>>(a);
-            k_m3_av<<<g[3], MB, 0, s>>>(a);
-            k_m3_s<<<g[4], MB, 0, s>>>(a);
-            k_m3_at<<<g[5], MB, 0, s>>>(a);
-            k_m3_upd<<<g[6], MB, 0, s>>>(a);
-            k_m3_flush<<<g[7], MB, 0, s>>>(a, 0);
-            k_m3_replace<<<g[1], MB, 0, s>>>(a, 0);
-        }
-        g_launches += 7 * CH;
-        SYSU_CUDA(cudaGetLastError());
-        graph_loop_tail(loop, &a.st->all_done, &a.st->loops, bound, s);
+        m3_chunk(k, s);
+        graph_loop_tail(loop, &k.a.st->all_done, &k.a.st->loops, bound, s);
     });
-    // e of a component that the loop bound left unfinished (returns at once when
-    // every component ended at a replacement)
-    k_m3_flush<<<g[7], MB, 0, st>>>(a, 1);
-    k_m3_info<<<1, 1, 0, st>>>(a.st, k.info, 0);
-    g_launches += 2;
-    SYSU_CUDA(cudaGetLastError());
+    m3_finish(k, st);
     cudaGraphConditionalHandle fb = graph_cond_handle(st, 0);
-    graph_if_flag(fb, &a.st->stalled, st);
-    graph_cond_node(st, side, fb, cudaGraphCondTypeIf, [&](cudaStream_t s) {
-        // the FP64 batched solve from the current x (components already below eps
-        // take no iteration), then the FP32 iterations added to its counts
-        bicgstab_solve(A, val, 3, b, x, o, w, k.info, s);
-        k_m3_info<<<1, 1, 0, s>>>(a.st, k.info, 1);
-        ++g_launches;
-        SYSU_CUDA(cudaGetLastError());
-    });
+    graph_if_flag(fb, &k.a.st->stalled, st);
+    graph_cond_node(st, side, fb, cudaGraphCondTypeIf,
+                    [&](cudaStream_t s) { m3_fp64(k, A, val, b, x, o, w, s); });
 }
 
 void Bicg3Mixed::solve(const SellDev &A, const double *val, const double *const *b, double *const *x,
@@ -662,6 +682,42 @@ void Bicg3Mixed::solve(const SellDev &A, const double *val, const double *const 
     std::memcpy(k.wbuf, wb, sizeof(wb));
     if (stream_capturing(st)) {  // inside the caller's graph (the case batch)
         m3_enqueue(k, A, val, b, x, o, w, st);
+        return;
+    }
+    if (!device_loop) {
+        // host-driven form, for per-kernel profiling (profilers skip the kernels of
+        // graphs with conditional nodes): the same kernels, CH iterations a captured
+        // graph, the host reading the state after each
+        k.maxit = -1 - k.maxit;  // a different cache entry from the device loop's
+        if (!d.exec || std::memcmp(&k, &d.key, sizeof(M3Key)) != 0) {
+            if (d.exec) cudaGraphExecDestroy(d.exec);
+            d.exec = nullptr;
+            const long before = g_launches.load();
+            cudaGraph_t graph;
+            SYSU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            m3_chunk(k, st);
+            SYSU_CUDA(cudaStreamEndCapture(st, &graph));
+            d.launches = g_launches.load() - before;
+            g_launches -= d.launches;
+            cudaError_t e = cudaGraphInstantiate(&d.exec, graph, 0);
+            cudaGraphDestroy(graph);
+            SYSU_CUDA(e);
+            std::memcpy(&d.key, &k, sizeof(M3Key));
+        }
+        k.maxit = o.maxit;
+        m3_setup(k, st);
+        M3State h{};
+        for (long it = 0; it < (long)o.maxit + 4L * CH; it += CH) {
+            SYSU_CUDA(cudaGraphLaunch(d.exec, st));
+            g_launches += d.launches;
+            SYSU_CUDA(cudaMemcpyAsync(&h, d.st.get(), sizeof(M3State), cudaMemcpyDeviceToHost, st));
+            SYSU_CUDA(cudaStreamSynchronize(st));
+            if (h.all_done) break;
+        }
+        m3_finish(k, st);
+        SYSU_CUDA(cudaMemcpyAsync(&h, d.st.get(), sizeof(M3State), cudaMemcpyDeviceToHost, st));
+        SYSU_CUDA(cudaStreamSynchronize(st));
+        if (h.stalled) m3_fp64(k, A, val, b, x, o, w, st);
         return;
     }
     if (!d.exec || std::memcmp(&k, &d.key, sizeof(M3Key)) != 0) {

@@ -168,6 +168,7 @@ int sysu_solver_set_option(sysu_solver *s, const char *key, double value) {
         return SYSU_OK;
     }
     if (k == "mom_batched") { o.mom_batched = value != 0.0; return SYSU_OK; }
+    if (k == "graph_loops") { o.graph_loops = value != 0.0; return SYSU_OK; }
     if (k == "sm_cap") { s->impl->kw.sm_cap = std::max(0, (int)value); return SYSU_OK; }
     if (k == "spmv_variant") { sysu::set_spmv_variant((int)value); return SYSU_OK; }
     if (k == "convection") {
@@ -339,6 +340,7 @@ int sysu_solver_get_option(sysu_solver *s, const char *key, double *value) {
     sysu::SolverOptions &o = s->impl->opt;
     std::string k(key);
     if (k == "mom_batched") { *value = o.mom_batched; return SYSU_OK; }
+    if (k == "graph_loops") { *value = o.graph_loops; return SYSU_OK; }
     if (k == "scalars_batched") { *value = o.scalars_batched; return SYSU_OK; }
     if (k == "gradient") { *value = s->impl->gradient_scheme; return SYSU_OK; }
     if (k == "convection") { *value = o.convection; return SYSU_OK; }

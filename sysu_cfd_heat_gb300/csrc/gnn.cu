@@ -1519,10 +1519,8 @@ void GnnPrecond::fcg(const double *b, double *x, bool x0_zero, const KrylovOpts 
         k.mg_persistent = mg_->persistent ? 1 : 0;
         k.mg_gamma = mg_->gamma;
     }
-    // b, x0 in; the iterations as a WHILE node (check_every a body; the body's last
-    // kernel ends the loop once the solve is done, or after maxit / check_every + 8
-    // bodies -- the solve stops at maxit itself); x and the statistics out
-    auto enqueue = [&](cudaStream_t s) {
+    // b, x0 in; the iterations; x and the statistics out
+    auto prologue = [&](cudaStream_t s) {
         SYSU_CUDA(cudaMemcpyAsync(b64_.get(), b, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
         if (!x0_zero) SYSU_CUDA(cudaMemcpyAsync(x64_.get(), x, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
         if (x0_zero) {
@@ -1532,19 +1530,66 @@ void GnnPrecond::fcg(const double *b, double *x, bool x0_zero, const KrylovOpts 
         k_fcg_init<<<gflat_, FB, 0, s>>>(a, x0_zero ? 1 : 0, o.eps, o.maxit, use_gnn ? 1 : 0);
         ++g_launches;
         SYSU_CUDA(cudaGetLastError());
+    };
+    auto epilogue = [&](cudaStream_t s) {
+        SYSU_CUDA(cudaMemcpyAsync(x, x64_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+        k_fcg_info<<<1, 1, 0, s>>>(fs_.get(), info_dev);
+        ++g_launches;
+        SYSU_CUDA(cudaGetLastError());
+    };
+    // the iterations as a WHILE node: check_every a body; the body's last kernel
+    // ends the loop once the solve is done, or after maxit / check_every + 8
+    // bodies (the solve stops at maxit itself)
+    auto enqueue = [&](cudaStream_t s) {
+        prologue(s);
         const int bound = o.maxit / std::max(1, check_every) + 8;
         cudaGraphConditionalHandle loop = graph_cond_handle(s, 1);
         graph_cond_node(s, graph_side_stream(), loop, cudaGraphCondTypeWhile, [&](cudaStream_t bs) {
             for (int c = 0; c < check_every; ++c) fcg_iteration(&a, use_gnn, bs);
             graph_loop_tail(loop, &a.fs->done, &a.fs->loops, bound, bs);
         });
-        SYSU_CUDA(cudaMemcpyAsync(x, x64_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
-        k_fcg_info<<<1, 1, 0, s>>>(fs_.get(), info_dev);
-        ++g_launches;
-        SYSU_CUDA(cudaGetLastError());
+        epilogue(s);
     };
     if (stream_capturing(st)) {  // inside the caller's graph: errors surface in the statuses
         enqueue(st);
+        return;
+    }
+    if (!device_loop) {
+        // host-driven form, for per-kernel profiling (profilers skip the kernels of
+        // graphs with conditional nodes): the same kernels, check_every
+        // iterations a captured graph, the host reading `done` after each
+        k.chunk = -check_every;  // a different cache entry from the device loop's
+        const unsigned char *kc = reinterpret_cast<const unsigned char *>(&k);
+        SolveGraph *cg = nullptr;
+        for (SolveGraph &g : graphs_)
+            if (g.exec && g.key.size() == sizeof(k) && std::memcmp(g.key.data(), kc, sizeof(k)) == 0) cg = &g;
+        if (!cg) {
+            cg = &graphs_[graph_next_];
+            graph_next_ = (graph_next_ + 1) % 4;
+            if (cg->exec) cudaGraphExecDestroy(cg->exec);
+            *cg = SolveGraph{};
+            const long before = g_launches.load();
+            cudaGraph_t g;
+            SYSU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            for (int c = 0; c < check_every; ++c) fcg_iteration(&a, use_gnn, st);
+            SYSU_CUDA(cudaStreamEndCapture(st, &g));
+            cg->launches = g_launches.load() - before;
+            g_launches -= cg->launches;
+            cudaError_t e = cudaGraphInstantiate(&cg->exec, g, 0);
+            cudaGraphDestroy(g);
+            SYSU_CUDA(e);
+            cg->key.assign(kc, kc + sizeof(k));
+        }
+        prologue(st);
+        int done = 0;
+        for (int it = 0; it < o.maxit + check_every && !done; it += check_every) {
+            SYSU_CUDA(cudaGraphLaunch(cg->exec, st));
+            g_launches += cg->launches;
+            SYSU_CUDA(cudaMemcpyAsync(&done, &fs_.get()->done, sizeof(int), cudaMemcpyDeviceToHost, st));
+            SYSU_CUDA(cudaStreamSynchronize(st));
+        }
+        epilogue(st);
+        if (use_gnn || (mg_ && mg_->post_hook)) check_err(st);
         return;
     }
     const unsigned char *kb = reinterpret_cast<const unsigned char *>(&k);

@@ -145,6 +145,10 @@ class GnnPrecond {
              cudaStream_t st);
     int stall_max = 30;
     int check_every = 8;
+    // false: the host drives the iterations (a captured chunk of check_every
+    // iterations, `done` read after each) -- for per-kernel profiling; profilers
+    // skip the kernels of graphs with conditional nodes
+    bool device_loop = true;
     FcgState last_state(cudaStream_t st);
 
   private:

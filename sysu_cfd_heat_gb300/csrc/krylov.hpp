@@ -170,6 +170,10 @@ class Bicg3Mixed {
     Bicg3Mixed &operator=(const Bicg3Mixed &) = delete;
     void solve(const SellDev &A, const double *val, const double *const *b, double *const *x, const KrylovOpts &o,
                KrylovWork &w, SolveInfo *info_dev, cudaStream_t st);
+    // false: the host drives the iterations (a captured chunk of them, the state
+    // read after each) -- for per-kernel profiling; profilers skip the kernels of
+    // graphs with conditional nodes.  A capturing stream always gets the device loop.
+    bool device_loop = true;
 
   private:
     struct Impl;

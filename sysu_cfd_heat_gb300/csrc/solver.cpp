@@ -404,6 +404,7 @@ void SimpleSolver::grad_limited(DomainDev &d, FieldSet &fs, int nfield, const do
 
 void SimpleSolver::solve(int slot, const EqOpts &o, const SellDev &A, const double *val, int nrhs,
                          const double *const *b, double *const *x, bool x0_zero) {
+    mom3.device_loop = gnn.device_loop = gnn_c.device_loop = opt.graph_loops;
     KrylovOpts ko;
     ko.maxit = o.maxit;
     ko.eps = o.eps;

@@ -106,6 +106,9 @@ struct SolverOptions {
         mom_batched = true;
     }
     bool mom_batched = true;      // u, v, w as one 3-RHS solve
+    // the mixed momentum and multigrid p' solves loop on the device (graph WHILE
+    // nodes); false: the host drives them, for per-kernel profiling
+    bool graph_loops = true;
     int convection = 0;           // convection of momentum and fluid scalars: 0 the reference's upwind + deferred correction, 1 hybrid
     double solid_source = 0.0;    // W/m^3 (extension; the reference has none)
     bool fatal_checks = true;     // the reference's convergence checks

@@ -270,3 +270,26 @@ def test_useless_coarse_level_network_still_converges():
             s.check()
             st = s.solve_stats()["p"]
     assert st["status"][0] == 0 and st["res"][0] < 1e-8, st
+
+
+def test_host_driven_loops_give_the_same_fields():
+    """Option graph_loops 0 (the host drives the multigrid FCG and mixed momentum
+    iterations, as per-kernel profiling needs) runs the same kernels as the device
+    loops (graph WHILE nodes): bit-identical fields and the same iteration counts."""
+    import tempfile
+
+    from sysu_cfd_heat_gb300 import meshgen as mg
+    from sysu_cfd_heat_gb300.solver import NavierStokesSolver
+
+    with tempfile.TemporaryDirectory() as tmp:
+        p = mg.write_case(tmp, mg.lid_cavity_tet(9, 8, 7, jitter=0.2), mg.cavity_param("x", 20, mu=0.0025))
+        out = {}
+        for loops in (1, 0):
+            opts = {"rtc": 1e-8, "p.precond": 4, "p.maxit": 5000, "mom.mixed": 1, "graph_loops": loops}
+            with NavierStokesSolver(p, opts) as s:
+                assert s.iterate(5) == 5
+                st = s.solve_stats()
+                out[loops] = ({f: s.get(f) for f in ("U", "V", "W", "P")}, st["p"]["iters"][0], st["mom"]["iters"])
+    for f in ("U", "V", "W", "P"):
+        assert np.array_equal(out[0][0][f], out[1][0][f]), f
+    assert out[0][1] == out[1][1] and out[0][2] == out[1][2]
