@@ -266,7 +266,10 @@ def spmv_sweep(s, n: int, nnz: int, hbm: float, at=(1, 10, 100), reps: int = 10)
     iterations (FP64 values and their FP32 copy), L2 flushed before each product,
     by four kernel forms: one row per thread over a full grid (the top-level
     figures), the persistent bulk-copy ring (`ring`), the per-warp cp.async
-    pipeline (`async`) and x staged in shared memory per block (`staged_x`)."""
+    pipeline (`async`) and x staged in shared memory per block (`staged_x`); and
+    the first and last of those in steady state (`steady`, `staged_x_steady`:
+    products back to back alternating between two full copies of the operands,
+    more than the L2 holds, as the products of an iterative solve run)."""
     out = {}
     s.reset()
     done = 0
@@ -283,12 +286,19 @@ def spmv_sweep(s, n: int, nnz: int, hbm: float, at=(1, 10, 100), reps: int = 10)
                     ms = s.spmv_timing(which, fp32, reps)
                     gbs = b / (ms / 1000.0) / 1e9
                     res[name] = {"ms": ms, "GB/s": gbs, "frac_of_hbm": gbs / hbm}
+                for name, variant in (("stream", 0), ("staged_x", 300)):
+                    s.set_option("spmv_variant", variant)
+                    ms = s.spmv_timing(which, fp32, reps, steady=True)
+                    gbs = b / (ms / 1000.0) / 1e9
+                    res[name + "_steady"] = {"ms": ms, "GB/s": gbs, "frac_of_hbm": gbs / hbm}
                 s.set_option("spmv_variant", 0)
                 entry = dict(res["stream"])
                 entry["algorithmic_bytes"] = b
                 entry["ring"] = res["ring"]
                 entry["async"] = res["async"]
                 entry["staged_x"] = res["staged_x"]
+                entry["steady"] = res["stream_steady"]
+                entry["staged_x_steady"] = res["staged_x_steady"]
                 row[f"{which}_{'fp32' if fp32 else 'fp64'}"] = entry
         out[f"after_outer_iteration_{k}"] = row
     return out

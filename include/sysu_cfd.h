@@ -161,6 +161,13 @@ int sysu_solver_cg_phases(sysu_solver *s, unsigned long long *out, int n);
  * products on a fixed x, FP64 values or (fp32 != 0) their FP32 copy, with L2
  * flushed before every product. */
 int sysu_solver_spmv_timing(sysu_solver *s, const char *which, int fp32, int reps, double *ms);
+/* The same product timed in steady state: 2 * max(reps, 2) products back to back,
+ * alternating between the matrix (values, column indices, slice table) with its x
+ * and y and a full copy of all of them -- more than the L2 holds for the 2M-row
+ * systems, so each product reads its operands from HBM as one inside an iterative
+ * solve does, without the launch ramp and tail of a single timed product.
+ * *ms = mean per product. */
+int sysu_solver_spmv_timing_steady(sysu_solver *s, const char *which, int fp32, int reps, double *ms);
 /* Residual[0..9] of the last iteration (navier.h:65). */
 int sysu_solver_residuals(sysu_solver *s, double *out10);
 /* Per solve slot (mom u/v/w, p', k, eps, T, solid T): iterations, residual,

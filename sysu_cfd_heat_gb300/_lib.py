@@ -67,6 +67,7 @@ def lib() -> C.CDLL:
             "sysu_kernel_launches": (C.c_long, []),
             "sysu_solver_cg_phases": (C.c_int, [vp, vp, C.c_int]),
             "sysu_solver_spmv_timing": (C.c_int, [vp, cp, C.c_int, C.c_int, dp]),
+            "sysu_solver_spmv_timing_steady": (C.c_int, [vp, cp, C.c_int, C.c_int, dp]),
             "sysu_solver_output": (C.c_int, [vp, cp]),
             "sysu_solver_save_transient_old_data": (C.c_int, [vp]),
             "sysu_solver_volume_average": (C.c_int, [vp, cp, C.c_double, C.c_int]),

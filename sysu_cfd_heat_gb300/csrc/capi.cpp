@@ -579,7 +579,15 @@ long sysu_kernel_launches(void) { return sysu::g_launches.load(); }
 int sysu_solver_spmv_timing(sysu_solver *s, const char *which, int fp32, int reps, double *ms) {
     if (!s || !which || !ms) return set_err(SYSU_ERR_INPUT, "null argument");
     return guarded([&] {
-        *ms = s->impl->spmv_timing(which, fp32 != 0, reps);
+        *ms = s->impl->spmv_timing(which, fp32 != 0, reps, false);
+        return SYSU_OK;
+    });
+}
+
+int sysu_solver_spmv_timing_steady(sysu_solver *s, const char *which, int fp32, int reps, double *ms) {
+    if (!s || !which || !ms) return set_err(SYSU_ERR_INPUT, "null argument");
+    return guarded([&] {
+        *ms = s->impl->spmv_timing(which, fp32 != 0, reps, true);
         return SYSU_OK;
     });
 }

@@ -1071,7 +1071,7 @@ void SimpleSolver::volume_average(const std::string &dir, double t, int out_iter
     append_tot_line(cs, dir + "/tot.dat", t, out_iter, R.data(), P.data(), T.data());
 }
 
-double SimpleSolver::spmv_timing(const std::string &which, bool fp32, int reps) {
+double SimpleSolver::spmv_timing(const std::string &which, bool fp32, int reps, bool steady) {
     const DomainDev *d = &fd;
     const DevBuf<double> *v = nullptr;
     if (which == "mom") v = &f.Amom;
@@ -1096,6 +1096,59 @@ double SimpleSolver::spmv_timing(const std::string &which, bool fp32, int reps) 
         sell_to_fp32(A, v->get(), v32.get(), st);
     }
     double total = 0.0;
+    if (steady) {
+        // products back to back, alternating between the matrix (values, column
+        // indices, slice table) with x, y and a copy of all of them: 2 x 152 MB
+        // (FP64, 2M rows) streamed in turn, more than the L2 holds, so every product
+        // reads its operands from HBM as a product inside an iterative solve does,
+        // without the launch ramp and tail a single timed product carries
+        SellDev B;
+        B.n = A.n;
+        B.nslices = A.nslices;
+        B.wmax = A.wmax;
+        B.nnz = A.nnz;
+        B.nnz_true = A.nnz_true;
+        B.sl_ptr.alloc(A.sl_ptr.size());
+        B.sl_w.alloc(A.sl_w.size());
+        B.col.alloc(A.col.size());
+        SYSU_CUDA(cudaMemcpyAsync(B.sl_ptr.get(), A.sl_ptr.get(), sizeof(int) * A.sl_ptr.size(), cudaMemcpyDeviceToDevice, st));
+        SYSU_CUDA(cudaMemcpyAsync(B.sl_w.get(), A.sl_w.get(), sizeof(int) * A.sl_w.size(), cudaMemcpyDeviceToDevice, st));
+        SYSU_CUDA(cudaMemcpyAsync(B.col.get(), A.col.get(), sizeof(int) * A.col.size(), cudaMemcpyDeviceToDevice, st));
+        DevBuf<double> v64b, x64b(n), y64b(n);
+        DevBuf<float> v32b, x32b(n), y32b(n);
+        fill_sweep_x((long)n, x64b.get(), x32b.get(), st);
+        if (fp32) {
+            v32b.alloc((size_t)A.nnz);
+            SYSU_CUDA(cudaMemcpyAsync(v32b.get(), v32.get(), sizeof(float) * A.nnz, cudaMemcpyDeviceToDevice, st));
+        } else {
+            v64b.alloc((size_t)A.nnz);
+            SYSU_CUDA(cudaMemcpyAsync(v64b.get(), v->get(), sizeof(double) * A.nnz, cudaMemcpyDeviceToDevice, st));
+        }
+        auto product = [&](int k) {
+            const bool second = k & 1;
+            const SellDev &M = second ? B : A;
+            if (ring && fp32) spmv_ring32(M, second ? v32b.get() : v32.get(), second ? x32b.get() : x32.get(),
+                                          second ? y32b.get() : y32.get(), err.get(), st);
+            else if (ring) spmv_ring(M, second ? v64b.get() : v->get(), second ? x64b.get() : x64.get(),
+                                     second ? y64b.get() : y64.get(), err.get(), st);
+            else if (fp32) spmv_stream32(M, second ? v32b.get() : v32.get(), second ? x32b.get() : x32.get(),
+                                         second ? y32b.get() : y32.get(), st);
+            else spmv_stream(M, second ? v64b.get() : v->get(), second ? x64b.get() : x64.get(),
+                             second ? y64b.get() : y64.get(), st);
+        };
+        const int K = 2 * std::max(reps, 2);
+        for (int k = 0; k < 4; ++k) product(k);  // warm-up
+        SYSU_CUDA(cudaEventRecord(ev[4], st));
+        for (int k = 0; k < K; ++k) product(k);
+        SYSU_CUDA(cudaEventRecord(ev[5], st));
+        SYSU_CUDA(cudaEventSynchronize(ev[5]));
+        float ms = 0.f;
+        SYSU_CUDA(cudaEventElapsedTime(&ms, ev[4], ev[5]));
+        int e = 0;
+        SYSU_CUDA(cudaMemcpy(&e, err.get(), sizeof(int), cudaMemcpyDeviceToHost));
+        if (e != 0) throw CaseError{"spmv_timing: a bounded wait of the ring SpMV gave up"};
+        return ms / K;
+    }
     for (int k = 0; k < reps + 1; ++k) {
         l2_flush_read(flush.get(), flush.size(), sink.get(), st);
         SYSU_CUDA(cudaEventRecord(ev[4], st));

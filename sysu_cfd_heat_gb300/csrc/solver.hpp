@@ -228,7 +228,10 @@ class SimpleSolver {
     // Standalone SpMV sweep on an assembled matrix ("mom", "p", "scalar", "solid"):
     // mean device time (ms) of one y = A x over `reps` products, FP64 or FP32
     // values, L2 flushed (256 MB write) before each product.
-    double spmv_timing(const std::string &which, bool fp32, int reps);
+    // Mean device ms of one y = A x of an assembled matrix by the current kernel
+    // form: L2 flushed before each of `reps` timed products, or (steady) products
+    // back to back alternating between two full copies of the operands
+    double spmv_timing(const std::string &which, bool fp32, int reps, bool steady = false);
 
   private:
     void alloc_fields(FieldSet &fs, const DomainDev &d, bool solid);

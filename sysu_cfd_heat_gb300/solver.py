@@ -165,10 +165,13 @@ class NavierStokesSolver:
         check(lib().sysu_solver_timing(self._h, C.byref(p), C.byref(m)))
         return p.value, m.value
 
-    def spmv_timing(self, which: str = "p", fp32: bool = False, reps: int = 10) -> float:
-        """Mean device ms of one standalone y = A x on an assembled matrix (L2 flushed)."""
+    def spmv_timing(self, which: str = "p", fp32: bool = False, reps: int = 10, steady: bool = False) -> float:
+        """Mean device ms of one standalone y = A x on an assembled matrix: L2 flushed
+        before each product, or (steady) products back to back alternating between
+        two full copies of the operands."""
         ms = C.c_double()
-        check(lib().sysu_solver_spmv_timing(self._h, which.encode(), int(fp32), int(reps), C.byref(ms)))
+        fn = lib().sysu_solver_spmv_timing_steady if steady else lib().sysu_solver_spmv_timing
+        check(fn(self._h, which.encode(), int(fp32), int(reps), C.byref(ms)))
         return ms.value
 
     def cg_phases(self) -> np.ndarray:
