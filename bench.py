@@ -676,7 +676,7 @@ def matched_forms(s, args, n, nnz, hbm):
 def cpu_survey(args) -> dict:
     """--cpu-survey (not part of the default run; minutes of CPU time): the
     reference's CPU build on configurations 1-3 next to the GPU path on the same
-    cases, 1 core pinned, the measurement SURVEY-style:
+    cases, 1 core pinned:
     * C1, the 24^3 hex cavity at Re 100: all 300 outer iterations;
     * C2, the k-epsilon CHT channel (256,000 + 51,200 cells) without the solid's
       volumetric source, which the reference cannot express: mean over outer

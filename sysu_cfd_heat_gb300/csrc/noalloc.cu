@@ -151,8 +151,8 @@ __global__ void __launch_bounds__(NA_KB) k_na_cg(NaArgs a) {
     double *partials = dinv + NA_MAX_ROWS;
     const int n = a.n, T = gridDim.x * NA_KB, t0 = blockIdx.x * NA_KB + threadIdx.x;
     // k_na_dinv ran before this launch on the same stream: every block reads the
-    // same verdict, so on a malformed matrix all leave together, before any row
-    // loop or barrier
+    // same check result, so on a malformed matrix all leave together, before any
+    // row loop or barrier
     if (__ldcg(&h->bad) != NA_GOOD) return;
     int parity = 0;
     double v3[3] = {0.0, 0.0, 0.0};

@@ -146,7 +146,7 @@ def test_noalloc_reports_a_malformed_matrix_without_solving():
         msg = lib.sysu_noalloc_last_error().decode()
         assert f"row {row} " in msg, msg
         assert bool(torch.all(d_x == 0.5))
-    # a well-formed call afterwards is unaffected by the stored verdict
+    # a well-formed call afterwards is unaffected by the stored check result
     d_rp, d_cl, d_vl = (torch.from_numpy(a).cuda() for a in (rp, cl, vl))
     d_x = torch.zeros(n, dtype=torch.float64, device="cuda")
     torch.cuda.synchronize()
