@@ -520,9 +520,12 @@ void SimpleSolver::solve_learned(const EqOpts &o, const double *val, const doubl
             }
             gnn_c.loss_kind = o.learn_kind;
             gnn_c.skip = (float)o.mg_omega;
-            mg_c.omega = o.mg_omega;
-            mg_c.gamma = o.mg_gamma;
-            mg_c.refresh(mg.level_val64(lvl), mg.level_val32(lvl), st);
+            if (p_solves < o.learn_iters) {
+                // the level's own hierarchy serves the training pairs' level solves only
+                mg_c.omega = o.mg_omega;
+                mg_c.gamma = o.mg_gamma;
+                mg_c.refresh(mg.level_val64(lvl), mg.level_val32(lvl), st);
+            }
             gnn_c.refresh(st);
             if (gnn_c.multigrid() != &mg_c) gnn_c.attach_multigrid(&mg_c);
             mg.post_level = lvl;
