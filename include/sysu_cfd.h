@@ -253,6 +253,11 @@ int sysu_csr_bicgstab_batched3(int n, const int *rowptr, const int *col, const d
 int sysu_csr_bicgstab3(int n, const int *rowptr, const int *col, const double *val, const double *const *b,
                        double *const *x, int mixed, int maxit, double eps, double omega, double inner_tol,
                        int *iters, double *res, int *status, int *refinements);
+/* Self-test of the device-side solve loops (CUDA graph WHILE nodes, whose
+ * last kernel ends the loop when the solve's stop flag is set or after a bound of
+ * bodies): *bodies = the number of bodies run when the flag is set after stop_at
+ * bodies (never, for stop_at <= 0) and the bound is `bound`; min(stop_at, bound). */
+int sysu_graph_loop_selftest(int bound, int stop_at, int *bodies);
 const char *sysu_csr_last_error(void);
 
 /* ---- aggregation-multigrid hierarchy (host only, no device work) -----------

@@ -78,6 +78,7 @@ def lib() -> C.CDLL:
             "sysu_set_spmv_variant": (C.c_int, [C.c_int]),
             "sysu_csr_spmv_timing": (C.c_int, [C.c_int, ip, ip, dp, C.c_int, C.c_int, dp]),
             "sysu_csr_last_error": (cp, []),
+            "sysu_graph_loop_selftest": (C.c_int, [C.c_int, C.c_int, ip]),
             "sysu_csr_bicgstab_batched3": (C.c_int, [C.c_int, ip, ip, C.POINTER(dp), C.POINTER(dp), C.POINTER(dp),
                                                      C.c_int, C.c_double, ip, dp, ip]),
             "sysu_csr_bicgstab3": (C.c_int, [C.c_int, ip, ip, dp, C.POINTER(dp), C.POINTER(dp), C.c_int, C.c_int,

@@ -10,6 +10,7 @@
 #include "../../include/sysu_cfd.h"
 #include "csr_device.hpp"
 #include "gnn.hpp"
+#include "graph_loop.hpp"
 #include "handles.hpp"
 
 
@@ -336,6 +337,24 @@ int sysu_csr_bicgstab3(int n, const int *rowptr, const int *col, const double *v
             }
             if (refinements) *refinements = mixed ? h.refinements : 0;
         }
+        return SYSU_OK;
+    } catch (const ArgError &e) {
+        g_csr_err = e.msg;
+        return SYSU_ERR_INPUT;
+    } catch (const sysu::CaseError &e) {
+        g_csr_err = e.msg;
+        return SYSU_ERR_CUDA;
+    }
+}
+
+// Self-test of the device-side solve loops (CUDA graph WHILE nodes): *bodies =
+// the number of loop bodies run when the stop flag is set after stop_at bodies
+// (never, for stop_at <= 0) and the loop is bounded to `bound` bodies.
+int sysu_graph_loop_selftest(int bound, int stop_at, int *bodies) {
+    try {
+        if (bound < 1 || !bodies) throw ArgError{"bound >= 1 and a non-null output required"};
+        OwnedStream os;
+        *bodies = sysu::graph_loop_selftest(bound, stop_at, os.st);
         return SYSU_OK;
     } catch (const ArgError &e) {
         g_csr_err = e.msg;

@@ -14,6 +14,11 @@ __global__ void k_loop_tail(cudaGraphConditionalHandle h, const int *stop, int *
     cudaGraphSetConditional(h, (*stop == 0 && c < bound) ? 1u : 0u);
 }
 
+// self-test body: sets the stop flag once `stop_at` bodies have run
+__global__ void k_loop_stop_at(int *stop, const int *bodies, int stop_at) {
+    if (*bodies >= stop_at) *stop = 1;
+}
+
 __global__ void k_if_flag(cudaGraphConditionalHandle h, const int *flag) {
     cudaGraphSetConditional(h, *flag != 0 ? 1u : 0u);
 }
@@ -76,6 +81,43 @@ void graph_if_flag(cudaGraphConditionalHandle h, const int *flag, cudaStream_t s
     k_if_flag<<<1, 1, 0, st>>>(h, flag);
     ++g_launches;
     SYSU_CUDA(cudaGetLastError());
+}
+
+namespace {
+__global__ void k_loop_body_count(int *bodies) { *bodies += 1; }
+}  // namespace
+
+int graph_loop_selftest(int bound, int stop_at, cudaStream_t st) {
+    if (bound < 1) throw CaseError{"graph_loop_selftest: bound must be >= 1"};
+    DevBuf<int> d(3);  // stop flag, loop count, bodies run
+    d.zero(st);
+    cudaGraph_t g;
+    SYSU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    try {
+        cudaGraphConditionalHandle h = graph_cond_handle(st, 1);
+        graph_cond_node(st, graph_side_stream(), h, cudaGraphCondTypeWhile, [&](cudaStream_t s) {
+            k_loop_body_count<<<1, 1, 0, s>>>(d.get() + 2);
+            if (stop_at > 0) k_loop_stop_at<<<1, 1, 0, s>>>(d.get(), d.get() + 2, stop_at);
+            graph_loop_tail(h, d.get(), d.get() + 1, bound, s);
+        });
+    } catch (...) {
+        cudaGraph_t junk = nullptr;
+        cudaStreamEndCapture(st, &junk);
+        if (junk) cudaGraphDestroy(junk);
+        throw;
+    }
+    SYSU_CUDA(cudaStreamEndCapture(st, &g));
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    SYSU_CUDA(e);
+    int h[3] = {0, 0, 0};
+    e = cudaGraphLaunch(exec, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d.get(), sizeof(h), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaGraphExecDestroy(exec);
+    SYSU_CUDA(e);
+    return h[2];
 }
 
 cudaStream_t graph_side_stream() {

@@ -40,4 +40,9 @@ void graph_if_flag(cudaGraphConditionalHandle h, const int *flag, cudaStream_t s
 // and device, created on first use).
 cudaStream_t graph_side_stream();
 
+// Self-test of the loop's two exits: a WHILE node whose body counts its runs and
+// sets the stop flag after `stop_at` of them (never, for stop_at <= 0), with the
+// given bound; returns the number of bodies that ran (min(stop_at, bound)).
+int graph_loop_selftest(int bound, int stop_at, cudaStream_t st);
+
 }  // namespace sysu
