@@ -27,8 +27,11 @@
 //
 // Each phase is one flat kernel over all rows; the last block to finish a
 // phase reduces the partial sums (fixed order: run-to-run deterministic) and
-// derives the next scalars into the device state.  Iterations are captured in
-// a CUDA graph of CH iterations; kernels of finished solves return at once.
+// derives the next scalars into the device state.  CH iterations are the body
+// of a CUDA graph WHILE node whose last kernel ends the loop (graph_loop.hpp);
+// the FP64 finish of stalled components is an IF node.  The solve never waits
+// for the host (device_loop false: the host drives the same body, for
+// per-kernel profiling).
 #include <cstring>
 
 #include "graph_loop.hpp"
