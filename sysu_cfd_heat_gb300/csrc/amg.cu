@@ -3,8 +3,9 @@
 //
 // Every cycle kernel is a flat grid-stride loop over rows (SELL-32: thread i
 // reads row i's entries at sl_ptr[i/32] + 32 k + i%32, so a warp's loads are
-// coalesced) and returns at once when the flexible CG it serves has finished
-// (*done != 0), so a captured chunk of iterations costs little past convergence.
+// coalesced; on coarse levels a group of lanes per row) and returns at once when
+// the flexible CG it serves has finished (*done != 0), so the rest of a loop body
+// of iterations costs little past convergence.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>

@@ -140,7 +140,10 @@ class GnnPrecond {
     // when the network fails to reduce the residual for `stall_max` iterations,
     // or a direction loses positivity, the same preconditioner without the
     // network takes over for the rest of the solve.
-    // Stops on the FP64 residual ||b - A x|| / ||b|| < eps.
+    // Stops on the FP64 residual ||b - A x|| / ||b|| < eps.  The iterations are
+    // the body (check_every of them) of a CUDA graph WHILE node, so the solve
+    // never waits for the host: on a stream being captured it joins the
+    // caller's graph, otherwise it runs as its own graph (graph_loop.hpp).
     void fcg(const double *b, double *x, bool x0_zero, const KrylovOpts &o, bool use_gnn, SolveInfo *info_dev,
              cudaStream_t st);
     int stall_max = 30;
