@@ -81,3 +81,24 @@ def test_single_row_and_empty(variant):
 def test_bad_variant_rejected():
     with pytest.raises(RuntimeError):
         set_spmv_variant(7)
+
+
+@pytest.mark.parametrize("variant", [0, 300])
+def test_steady_state_timing_of_an_assembled_matrix(variant):
+    """sysu_solver_spmv_timing_steady (products back to back, alternating between
+    the operands and a full copy of them) runs on an assembled matrix and gives a
+    per-product time in the range of the flushed single-product timing."""
+    import tempfile
+
+    from sysu_cfd_heat_gb300 import meshgen as mg
+    from sysu_cfd_heat_gb300.solver import NavierStokesSolver
+
+    with tempfile.TemporaryDirectory() as tmp:
+        p = mg.write_case(tmp, mg.lid_cavity_tet(20, 18, 16, jitter=0.2), mg.cavity_param("x", 5, mu=0.01))
+        with NavierStokesSolver(p, {"rtc": 1e-8, "spmv_variant": variant}) as s:
+            s.iterate(1)
+            for which in ("p", "mom"):
+                for fp32 in (False, True):
+                    steady = s.spmv_timing(which, fp32, 4, steady=True)
+                    flushed = s.spmv_timing(which, fp32, 4)
+                    assert 0.0 < steady < 10.0 * flushed + 1.0, (which, fp32, steady, flushed)
