@@ -463,6 +463,19 @@ __global__ void __launch_bounds__(MB, 6) k_m3_upd(M3Args a) {
         }
         need |= W->need[c];
     }
+    // a replacement costs about as much for one component as for three (the
+    // matrix pass is shared): a running component whose FP32 residual has fallen
+    // by sqrt(inner_tol) since its last replacement is replaced along with the due
+    // ones, which saves the pass it would take an iteration or two later
+    if (need)
+        for (int c = 0; c < 3; ++c) {
+            if (!on[c] || ea[c] || W->need[c]) continue;
+            const double rr = v[c], sc2 = W->sig[c] * W->sig[c];
+            if (isfinite(rr) && rr > 0.0 && rr * rr <= W->d2 * W->rref[c] * W->rref[c]) {
+                W->need[c] = 1;
+                W->sig_next[c] = pow2_scale(rr / sc2);
+            }
+        }
     W->any_need = need;
 }
 
